@@ -1,0 +1,398 @@
+"""
+Benchmark: FP64 g_z prism-station pair evaluations per second on one GB300.
+
+Workload (N=1): the 1e6-prism topography layer (1000 x 1000 prisms on a
+200 m grid, 200 km square, Gaussian-sum tops, bottoms at -10 000 m, densities
+U(1800, 3100)) with its 500 x 500-station survey at 2000 m + N(0, 50 m)
+(harmonica_gb300.synthetic.layer_topography_1e6, seeded; synthetic data).
+The full survey is 2.5e11 pairs; a STEP is one batch of the survey
+(``--stations-per-step`` consecutive stations, default 5000) against all 1e6
+prisms, the batches walking through the survey step after step.  Per-pair
+cost is uniform, so pairs/s over batches equals pairs/s over the full survey.
+
+* ``value``: pairs/s with the layer and survey resident in HBM, timed with
+  CUDA events around each step's launches on the launching stream.
+* ``e2e``: pairs/s through the public drop-in call
+  ``layer.prism_layer.gravity(coords, "g_z")`` with host (numpy) buffers:
+  host->device copies of the layer and the batch, the kernels and the
+  device->host copy of the result are inside the timed region.
+* ``roofline``: FP64-pipe bound.  ``achieved`` is the algorithmic FP64 flop
+  rate of the layer kernel, 720 flop per pair (8 vertices x (~16 basic +
+  sqrt + 2 log + 1 atan2) at basic=1, sqrt=4, log=20, atan2=30), over the
+  average kernel time; ``peak`` is the FP64 fused multiply-add rate measured
+  live by the hg_fp64_peak_probe launch (no FP64 figure exists in the
+  measured peak file).
+* ``cpu_baseline``: the CPU oracle (a C/OpenMP restatement of the reference's
+  per-vertex loop) on all host cores, on a bounded sample of stations of the
+  same workload.
+
+``--impl reference`` times the reference's CPU path instead (the oracle port:
+the reference's numba + choclo stack is not installable offline) and prints
+its own JSON line.
+"""
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+ALGO_FLOP_PER_PAIR_GZ = 720.0
+METRIC = "FP64 g_z prism-station pairs/s"
+WORKLOAD = "layer_topography_1e6: 1000x1000 prisms (200 m grid), 500x500 stations, g_z"
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--stations-per-step", type=int, default=5000)
+    p.add_argument("--cpu-sample-stations", type=int, default=32)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi during a region."""
+
+    QUERY = (
+        "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+        "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+        "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+    )
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True,
+            )
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {
+            "sm_mhz": float(np.median(sm)) if sm else None,
+            "sm_max_mhz": smax,
+            "reasons": sorted(reasons),
+            "samples": len(sm),
+        }
+
+
+def fp64_peak(torch, lib):
+    """Measured FP64 FMA peak (TFLOP/s) of this GPU via hg_fp64_peak_probe."""
+    n_threads = 152 * 8 * 256
+    iters = 4000
+    out = torch.empty(n_threads, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    best = 0.0
+    for _ in range(4):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        rc = lib.hg_fp64_peak_probe(out.data_ptr(), n_threads, iters, stream)
+        b.record()
+        torch.cuda.synchronize()
+        assert rc == 0
+        flops = n_threads * iters * 16.0
+        best = max(best, flops / (a.elapsed_time(b) * 1e-3) / 1e12)
+    return best
+
+
+def cpu_baseline(layer, coords, n_stations, threads):
+    """Oracle (per-vertex C/OpenMP restatement of the reference loop) on a sample."""
+    from oracle import prism_oracle
+
+    prism_oracle.build_oracle()
+    idx = np.linspace(0, coords[0].size - 1, n_stations).astype(np.int64)
+    sample = tuple(np.ascontiguousarray(c[idx]) for c in coords)
+    t0 = time.perf_counter()
+    prism_oracle.layer_gravity(
+        sample, layer["easting"], layer["northing"], layer["bottom"], layer["top"],
+        layer["density"], "g_z", n_threads=threads,
+    )
+    dt = time.perf_counter() - t0
+    pairs = n_stations * layer["top"].size
+    return pairs / dt, dt, pairs
+
+
+def run_reference(args, rank, world):
+    """The reference's CPU path (oracle port) on all host threads."""
+    if rank != 0:
+        return
+    from harmonica_gb300 import synthetic
+
+    layer = synthetic.layer_topography_1e6()
+    coords = layer["coordinates"]
+    threads = os.cpu_count() or 1
+    n = max(1, args.cpu_sample_stations)
+    for _ in range(max(0, min(args.warmup, 1))):
+        cpu_baseline(layer, coords, max(1, n // 8), threads)
+    rates, times = [], []
+    for _ in range(args.steps):
+        rate, dt, pairs = cpu_baseline(layer, coords, n, threads)
+        rates.append(rate)
+        times.append(dt)
+    value = float(np.sum([n * layer["top"].size for _ in times]) / np.sum(times))
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": value,
+        "unit": "pairs/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": float(np.mean(times) * 1e3),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic",
+        "config": {
+            "workload": WORKLOAD,
+            "step": f"{n} stations (strided sample of the survey) x 1e6 prisms on the CPU",
+        },
+        "cpu_baseline": {
+            "value": value,
+            "unit": "pairs/s",
+            "cores": threads,
+            "kind": "port",
+            "sample": f"{n} of 250000 stations x all 1e6 prisms per step",
+        },
+        "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "note": "harmonica's numba+choclo path is not installable offline; the oracle "
+                "port (C/OpenMP per-vertex restatement) stands in for it",
+    }
+    print(json.dumps(line))
+
+
+def main():
+    args = parse_args()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    import torch
+
+    import harmonica_gb300 as hg
+    from harmonica_gb300 import _native, synthetic
+    from harmonica_gb300.layer import layer_forward_device
+
+    _native.build()
+    lib = _native.lib()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    layer = synthetic.layer_topography_1e6()
+    coords = layer["coordinates"]
+    n_total = coords[0].size
+    B = args.stations_per_step
+    mask = 1 << 3  # g_z
+    n_prisms = layer["top"].size
+
+    # resident layer and survey
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).to(dev)  # noqa: E731
+    ce, cn = T(layer["easting"]), T(layer["northing"])
+    bt, tp, rho = T(layer["bottom"]), T(layer["top"]), T(layer["density"])
+    de, dn, du = (T(c) for c in coords)
+
+    # each rank walks its own batches of the survey (no collective on the data path)
+    def batch(step):
+        k = (step * world + rank) % ((n_total + B - 1) // B)
+        lo = k * B
+        hi = min(lo + B, n_total)
+        return lo, hi
+
+    ws_bytes = _native.ctypes.c_size_t(0)
+    _native.check(lib.hg_layer_forward_workspace(B, ce.numel(), cn.numel(), mask,
+                                                 _native.ctypes.byref(ws_bytes)))
+    launches_per_step = 2 if ws_bytes.value else 1
+
+    flush = torch.empty(256 * 1024 * 1024 // 8, dtype=torch.float64, device=dev)
+
+    def step_device(step):
+        lo, hi = batch(step)
+        return layer_forward_device(de[lo:hi], dn[lo:hi], du[lo:hi], ce, cn, bt, tp, rho, mask,
+                                    0.0)
+
+    for s in range(args.warmup):
+        step_device(s)
+    torch.cuda.synchronize()
+    peak = fp64_peak(torch, lib)
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    barrier()
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    pairs = 0
+    t_wall = time.perf_counter()
+    for s in range(args.steps):
+        flush.fill_(float(s))  # L2 flush between timed steps (outside the events)
+        starts[s].record()
+        out = step_device(args.warmup + s)
+        ends[s].record()
+        lo, hi = batch(args.warmup + s)
+        pairs += (hi - lo) * n_prisms
+    torch.cuda.synchronize()
+    barrier()
+    wall = time.perf_counter() - t_wall
+    clocks = sampler.stop()
+    step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    dev_time = sum(step_ms) * 1e-3
+    if world > 1:
+        t = torch.tensor([dev_time], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        dev_time = float(t.item())
+        pt = torch.tensor([float(pairs)], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(pt)
+        pairs = int(pt.item())
+    value = pairs / dev_time
+    del out
+
+    # end-to-end through the public drop-in API with host buffers
+    e2e = None
+    if not args.no_e2e:
+        L = hg.prism_layer((layer["easting"], layer["northing"]), layer["top"], layer["bottom"],
+                           properties={"density": layer["density"]})
+        host_batches = []
+        for s in range(args.steps):
+            lo, hi = batch(args.warmup + s)
+            host_batches.append(tuple(np.ascontiguousarray(c[lo:hi]) for c in coords))
+        L.prism_layer.gravity(host_batches[0], field="g_z")  # warm
+        barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_pairs = 0
+        for hb in host_batches:
+            L.prism_layer.gravity(hb, field="g_z")
+            e2e_pairs += hb[0].size * n_prisms
+        torch.cuda.synchronize()
+        e2e_time = time.perf_counter() - t0
+        if world > 1:
+            t = torch.tensor([e2e_time], dtype=torch.float64, device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            e2e_time = float(t.item())
+            e2e_pairs *= world
+        h2d = 8 * (3 * B + layer["easting"].size + layer["northing"].size + 3 * n_prisms)
+        e2e = {"value": e2e_pairs / e2e_time, "unit": "pairs/s", "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": 8 * B}
+
+    base = None
+    if rank == 0 and not args.no_cpu_baseline:
+        rate, dt, sample_pairs = cpu_baseline(layer, coords, args.cpu_sample_stations,
+                                              os.cpu_count() or 1)
+        base = {"value": rate, "unit": "pairs/s", "cores": os.cpu_count() or 1, "kind": "port",
+                "sample": f"{args.cpu_sample_stations} strided stations x all 1e6 prisms "
+                          f"({sample_pairs:.3g} pairs, {dt:.1f} s)"}
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+    avg_launch_s = dev_time / args.steps
+    achieved = ALGO_FLOP_PER_PAIR_GZ * (pairs / world / args.steps) / avg_launch_s / 1e12
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "pairs/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": wall / args.steps * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic",
+        "config": {
+            "workload": WORKLOAD,
+            "step": f"{B} consecutive survey stations x all 1e6 prisms ({B * n_prisms:.3g} pairs)",
+            "full_survey_steps": (n_total + B - 1) // B,
+            "l2": "flushed between timed steps (256 MB write)",
+            "parallelism": f"stations sharded over {world} GPU(s), no collective",
+        },
+        "roofline": {
+            "bound": "fp64",
+            "achieved": achieved,
+            "peak": peak,
+            "unit": "TFLOP/s",
+            "frac": achieved / peak,
+            "traffic": None,
+            "flop_per_pair": ALGO_FLOP_PER_PAIR_GZ,
+            "peak_source": "measured live: hg_fp64_peak_probe (FP64 FMA chains)",
+        },
+        "cpu_baseline": base,
+        "e2e": e2e,
+        "gpu_launches": launches_per_step * args.steps,
+        "clocks": clocks,
+        "step_ms": step_ms,
+    }
+    print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

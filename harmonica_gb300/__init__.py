@@ -1,0 +1,30 @@
+"""
+harmonica_gb300: Harmonica's right-rectangular-prism gravity forward model on
+NVIDIA GB300 (sm_103a).
+
+Drop-in entry points (same signatures, errors, warnings and units as
+harmonica):
+
+* :func:`prism_gravity` -- ``harmonica.prism_gravity``
+* :func:`prism_layer` and the ``prism_layer`` accessor
+  (:class:`DatasetAccessorPrismLayer`) -- ``harmonica.prism_layer``
+
+The all-pairs sums run in hand-written CUDA kernels behind the C ABI declared
+in ``include/harmonica_gb300.h``; :func:`build` compiles them in-tree.
+"""
+
+from ._native import build
+from .fields import FIELDS
+from .gravity import check_prisms, prism_gravity, prism_gravity_fields
+from .layer import DatasetAccessorPrismLayer, PrismLayer, prism_layer
+
+__all__ = [
+    "FIELDS",
+    "DatasetAccessorPrismLayer",
+    "PrismLayer",
+    "build",
+    "check_prisms",
+    "prism_gravity",
+    "prism_gravity_fields",
+    "prism_layer",
+]

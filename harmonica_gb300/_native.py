@@ -1,0 +1,173 @@
+"""
+Build and load the native library ``libharmonica_gb300.so`` (CUDA kernels for
+sm_103a plus the C ABI declared in ``include/harmonica_gb300.h``).
+
+The library is built in-tree (``harmonica_gb300/_build/``) by :func:`build`
+and loaded with :mod:`ctypes`.  There is no fallback: if the library is
+missing, :func:`lib` raises, so a GPU run can never silently compute on the
+CPU.
+"""
+
+import ctypes
+import os
+import shutil
+import subprocess
+import threading
+
+PKG_DIR = os.path.dirname(os.path.abspath(__file__))
+REPO_DIR = os.path.dirname(PKG_DIR)
+CSRC_DIR = os.path.join(PKG_DIR, "csrc")
+BUILD_DIR = os.path.join(PKG_DIR, "_build")
+LIB_NAME = "libharmonica_gb300.so"
+LIB_PATH = os.path.join(BUILD_DIR, LIB_NAME)
+HEADERS = (
+    os.path.join(REPO_DIR, "include", "harmonica_gb300.h"),
+    os.path.join(REPO_DIR, "include", "harmonica_gb300_bench.h"),
+)
+
+#: translation units compiled into the library
+SOURCES = ("prism_forward.cu", "bench_probe.cu")
+
+ARCH_FLAGS = ("-gencode", "arch=compute_103a,code=sm_103a")
+
+_lock = threading.Lock()
+_lib = None
+
+
+def nvcc_path():
+    cand = shutil.which("nvcc")
+    if cand:
+        return cand
+    default = "/usr/local/cuda/bin/nvcc"
+    if os.path.exists(default):
+        return default
+    raise RuntimeError("nvcc not found: cannot build the harmonica_gb300 CUDA library")
+
+
+def _sources():
+    return [os.path.join(CSRC_DIR, s) for s in SOURCES]
+
+
+def _deps():
+    deps = _sources() + list(HEADERS)
+    deps += [
+        os.path.join(CSRC_DIR, f) for f in os.listdir(CSRC_DIR) if f.endswith((".cuh", ".h"))
+    ]
+    return deps
+
+
+def is_stale():
+    if not os.path.exists(LIB_PATH):
+        return True
+    t = os.path.getmtime(LIB_PATH)
+    return any(os.path.getmtime(d) > t for d in _deps())
+
+
+def build(force=False, verbose=False):
+    """Compile every CUDA translation unit for sm_103a into one shared library.
+
+    Objects are compiled in parallel, then linked with nvcc (static cudart).
+    """
+    if not force and not is_stale():
+        return LIB_PATH
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    nvcc = nvcc_path()
+    common = [
+        nvcc, *ARCH_FLAGS, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+        "--expt-relaxed-constexpr", "-I", os.path.join(REPO_DIR, "include"),
+    ]
+    procs = []
+    objs = []
+    for src in _sources():
+        obj = os.path.join(BUILD_DIR, os.path.basename(src) + ".o")
+        objs.append(obj)
+        cmd = common + ["-c", src, "-o", obj]
+        if verbose:
+            cmd.insert(1, "-Xptxas=-v")
+        procs.append((cmd, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))
+    for cmd, p in procs:
+        out, _ = p.communicate()
+        if p.returncode != 0:
+            raise RuntimeError(
+                "nvcc failed:\n" + " ".join(cmd) + "\n" + out.decode(errors="replace")
+            )
+        if verbose and out:
+            print(out.decode(errors="replace"))
+    tmp = LIB_PATH + ".tmp"
+    link = [nvcc, *ARCH_FLAGS, "-shared", "-o", tmp, *objs]
+    res = subprocess.run(link, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
+    if res.returncode != 0:
+        raise RuntimeError("nvcc link failed:\n" + res.stdout.decode(errors="replace"))
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+_c_double_p = ctypes.c_void_p  # device pointers travel as integers
+
+#: ctypes prototypes of every exported symbol (must match include/harmonica_gb300.h)
+PROTOTYPES = {
+    "hg_version": (ctypes.c_int, []),
+    "hg_last_error": (ctypes.c_char_p, []),
+    "hg_pack_prisms": (
+        ctypes.c_int,
+        [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
+         ctypes.c_void_p],
+    ),
+    "hg_prism_forward_workspace": (
+        ctypes.c_int,
+        [ctypes.c_int64, ctypes.c_int64, ctypes.c_uint32, ctypes.POINTER(ctypes.c_size_t)],
+    ),
+    "hg_prism_forward": (
+        ctypes.c_int,
+        [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+         ctypes.c_int64, ctypes.c_int64, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p,
+         ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p],
+    ),
+    "hg_fp64_peak_probe": (
+        ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_void_p]
+    ),
+    "hg_layer_forward_workspace": (
+        ctypes.c_int,
+        [ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_uint32,
+         ctypes.POINTER(ctypes.c_size_t)],
+    ),
+    "hg_layer_forward": (
+        ctypes.c_int,
+        [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+         ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
+         ctypes.c_void_p, ctypes.c_double, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p,
+         ctypes.c_size_t, ctypes.c_void_p],
+    ),
+}
+
+
+def lib():
+    """Return the loaded native library; raise if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(
+                f"harmonica_gb300 native library not found at {LIB_PATH}; "
+                "build it with harmonica_gb300.build() (needs nvcc)"
+            )
+        handle = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in PROTOTYPES.items():
+            fn = getattr(handle, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = handle
+    return _lib
+
+
+class NativeError(RuntimeError):
+    """Error reported by the native library through its return code."""
+
+
+def check(rc):
+    if rc != 0:
+        msg = lib().hg_last_error()
+        raise NativeError(f"harmonica_gb300 native call failed ({rc}): {msg.decode()}")

@@ -1,0 +1,399 @@
+// All-pairs prism gravity forward kernels and their C ABI (see
+// include/harmonica_gb300.h).
+//
+// Work decomposition: one thread owns one observation point and keeps its
+// running sums in registers; a CTA owns a tile of kThreads points and walks a
+// CHUNK of the prism list, staged kTile prisms at a time in shared memory as
+// structure-of-arrays (every lane of a warp reads the same prism: a broadcast,
+// no bank conflicts).  The grid is (point tiles) x (prism chunks); with more
+// than one chunk each CTA writes its partial sums to a workspace and a second
+// kernel adds the chunks in fixed order, so results do not depend on
+// scheduling.  The arithmetic is FP64 throughout.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "../../include/harmonica_gb300.h"
+#include "prism_math.cuh"
+
+namespace hg {
+
+constexpr int kThreads = 128;  // observation points per CTA
+constexpr int kTile = 128;     // prisms staged per shared-memory tile
+constexpr int kSmCount = 152;
+
+thread_local std::string g_last_error;
+
+int set_error(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+int cuda_check(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return HG_OK;
+  return set_error(HG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// ---------------------------------------------------------------------------
+// Prism sources: how a CTA stages prism p of the list into shared memory.
+struct ListSource {
+  const double* soa;  // 7 rows of stride
+  int64_t stride;
+  __device__ __forceinline__ void load(int64_t p, double& w, double& e, double& s, double& n,
+                                       double& b, double& t, double& rho, bool& null) const {
+    w = soa[p];
+    e = soa[stride + p];
+    s = soa[2 * stride + p];
+    n = soa[3 * stride + p];
+    b = soa[4 * stride + p];
+    t = soa[5 * stride + p];
+    rho = soa[6 * stride + p];
+    // gravity.py:475-480: zero volume or zero density
+    null = (w == e) || (s == n) || (b == t) || (rho == 0.0);
+  }
+};
+
+struct LayerSource {
+  const double* ce;
+  const double* cn;
+  const double* bottom;
+  const double* top;
+  const double* density;
+  int64_t n_east;
+  double threshold;
+  __device__ __forceinline__ void load(int64_t p, double& w, double& e, double& s, double& n,
+                                       double& b, double& t, double& rho, bool& null) const {
+    // half spacings from the first two centres, as layer.py:582-583
+    const double half_e = (ce[1] - ce[0]) / 2.0;
+    const double half_n = (cn[1] - cn[0]) / 2.0;
+    int64_t k = p / n_east, j = p - k * n_east;
+    w = ce[j] - half_e;
+    e = ce[j] + half_e;
+    s = cn[k] - half_n;
+    n = cn[k] + half_n;
+    b = bottom[p];
+    t = top[p];
+    rho = density[p];
+    // layer.py:596-607; zero-thickness prisms add exactly zero and are skipped too
+    null = (rho == 0.0) || isnan(rho) || (t - b < threshold) || isnan(t) || isnan(b) || (b == t);
+  }
+};
+
+template <int F> struct NumOut { static constexpr int value = 1; };
+template <> struct NumOut<kAll> { static constexpr int value = kNumFields; };
+
+__device__ __forceinline__ bool is_tensor(int f) { return f >= kGee && f <= kGnz; }
+
+// out_mask: for kAll, which of the ten fields are written (compact rows).
+template <int F, class Source>
+__global__ void __launch_bounds__(kThreads) forward_kernel(
+    const double* __restrict__ oe, const double* __restrict__ on, const double* __restrict__ ou,
+    int64_t n_obs, Source src, int64_t n_prisms, int64_t chunk, uint32_t out_mask,
+    double* __restrict__ dst, int64_t dst_chunk_stride, int scale_output, int check_singular,
+    int32_t* __restrict__ flag) {
+  constexpr int NF = NumOut<F>::value;
+  __shared__ double sh_w[kTile], sh_e[kTile], sh_s[kTile], sh_n[kTile], sh_b[kTile], sh_t[kTile],
+      sh_rho[kTile];
+  __shared__ int sh_null[kTile];
+
+  const int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x;
+  const bool active = i < n_obs;
+  const double pe = active ? oe[i] : 0.0;
+  const double pn = active ? on[i] : 0.0;
+  const double pu = active ? ou[i] : 0.0;
+
+  double acc[NF];
+#pragma unroll
+  for (int f = 0; f < NF; f++) acc[f] = 0.0;
+  bool singular_seen = false;
+
+  const int64_t p0 = (int64_t)blockIdx.y * chunk;
+  const int64_t p1 = min(p0 + chunk, n_prisms);
+  for (int64_t base = p0; base < p1; base += kTile) {
+    const int cnt = (int)min((int64_t)kTile, p1 - base);
+    __syncthreads();
+    if (threadIdx.x < cnt) {
+      double w, e, s, n, b, t, rho;
+      bool null;
+      src.load(base + threadIdx.x, w, e, s, n, b, t, rho, null);
+      sh_w[threadIdx.x] = w;
+      sh_e[threadIdx.x] = e;
+      sh_s[threadIdx.x] = s;
+      sh_n[threadIdx.x] = n;
+      sh_b[threadIdx.x] = b;
+      sh_t[threadIdx.x] = t;
+      sh_rho[threadIdx.x] = rho;
+      sh_null[threadIdx.x] = null;
+    }
+    __syncthreads();
+    for (int p = 0; p < cnt; p++) {
+      Rel q;
+      q.x1 = sh_w[p] - pe;
+      q.x2 = sh_e[p] - pe;
+      q.y1 = sh_s[p] - pn;
+      q.y2 = sh_n[p] - pn;
+      q.z1 = sh_b[p] - pu;
+      q.z2 = sh_t[p] - pu;
+      if (check_singular && active) {
+        if (F == kAll) {
+#pragma unroll
+          for (int f = kGee; f <= kGnz; f++)
+            if ((out_mask >> f) & 1u) singular_seen |= singular_for(f, q);
+        } else if (is_tensor(F)) {
+          singular_seen |= singular_for(F, q);
+        }
+      }
+      if (sh_null[p]) continue;  // uniform across the CTA
+      const double rho = sh_rho[p];
+      PairTerms T;
+      pair_terms<F>(q, T);
+      if (F == kAll) {
+#pragma unroll
+        for (int f = 0; f < kNumFields; f++) {
+          double v = combine(f, q, T);
+          if (is_tensor(f) && singular_for(f, q)) v = quiet_nan();
+          acc[f] = fma(rho, v, acc[f]);
+        }
+      } else {
+        double v = combine(F, q, T);
+        if (is_tensor(F) && singular_for(F, q)) v = quiet_nan();
+        acc[0] = fma(rho, v, acc[0]);
+      }
+    }
+  }
+  if (singular_seen) atomicOr(flag, 1);
+  if (!active) return;
+  double* d = dst + (int64_t)blockIdx.y * dst_chunk_stride;
+  if (F == kAll) {
+    int row = 0;
+#pragma unroll
+    for (int f = 0; f < kNumFields; f++) {
+      if ((out_mask >> f) & 1u) {
+        d[(int64_t)row * n_obs + i] = scale_output ? acc[f] * field_scale(f) : acc[f];
+        row++;
+      }
+    }
+  } else {
+    d[i] = scale_output ? acc[0] * field_scale(F) : acc[0];
+  }
+}
+
+struct RowFields {
+  int f[kNumFields];
+};
+
+// out[row][i] = scale(field of row) * sum_c part[c][row][i], chunks in order.
+__global__ void reduce_chunks_kernel(const double* __restrict__ part, int64_t n_chunks,
+                                     int64_t chunk_stride, int64_t n_obs, int n_rows,
+                                     RowFields row_field, double* __restrict__ out) {
+  int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t total = (int64_t)n_rows * n_obs;
+  if (idx >= total) return;
+  int row = (int)(idx / n_obs);
+  double s = 0.0;
+  for (int64_t c = 0; c < n_chunks; c++) s += part[c * chunk_stride + idx];
+  out[idx] = s * field_scale(row_field.f[row]);
+}
+
+__global__ void pack_prisms_kernel(const double* __restrict__ aos, const double* __restrict__ rho,
+                                   int64_t n, double* __restrict__ soa, int64_t stride) {
+  int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+#pragma unroll
+  for (int c = 0; c < 6; c++) soa[c * stride + p] = aos[6 * p + c];
+  soa[6 * stride + p] = rho[p];
+}
+
+// ---------------------------------------------------------------------------
+struct Plan {
+  int64_t n_tiles;   // observation tiles (grid.x)
+  int64_t n_chunks;  // prism chunks (grid.y)
+  int64_t chunk;     // prisms per chunk (multiple of kTile)
+  int n_rows;        // output rows
+  bool all;          // fused all-field kernel
+  int single_field;  // when !all
+  size_t workspace_bytes;
+};
+
+int popcount10(uint32_t m) {
+  int c = 0;
+  for (int f = 0; f < kNumFields; f++) c += (m >> f) & 1u;
+  return c;
+}
+
+Plan make_plan(int64_t n_obs, int64_t n_prisms, uint32_t mask) {
+  Plan p;
+  p.n_rows = popcount10(mask);
+  p.all = p.n_rows != 1;
+  p.single_field = -1;
+  if (!p.all)
+    for (int f = 0; f < kNumFields; f++)
+      if ((mask >> f) & 1u) p.single_field = f;
+  p.n_tiles = (n_obs + kThreads - 1) / kThreads;
+  // Enough CTAs for several waves over all SMs; split the prisms when the
+  // observation tiles alone cannot fill the GPU.
+  const int64_t target = (int64_t)kSmCount * 8;
+  int64_t n_prism_tiles = (n_prisms + kTile - 1) / kTile;
+  if (n_prism_tiles < 1) n_prism_tiles = 1;
+  int64_t want = (target + p.n_tiles - 1) / p.n_tiles;
+  if (want < 1) want = 1;
+  if (want > n_prism_tiles) want = n_prism_tiles;
+  if (want > 65535) want = 65535;
+  int64_t tiles_per_chunk = (n_prism_tiles + want - 1) / want;
+  p.chunk = tiles_per_chunk * kTile;
+  p.n_chunks = (n_prisms + p.chunk - 1) / p.chunk;
+  if (p.n_chunks < 1) p.n_chunks = 1;
+  p.workspace_bytes =
+      p.n_chunks > 1 ? (size_t)p.n_chunks * p.n_rows * n_obs * sizeof(double) : 0;
+  return p;
+}
+
+template <class Source>
+int launch_forward(const Plan& plan, const double* oe, const double* on, const double* ou,
+                   int64_t n_obs, const Source& src, int64_t n_prisms, uint32_t mask, double* out,
+                   int32_t* flag, void* workspace, cudaStream_t stream, bool check_singular) {
+  if (n_obs == 0) return HG_OK;
+  if (plan.n_tiles > 2147483647LL) return set_error(HG_ERR_INVALID, "too many observation points");
+  const bool direct = plan.n_chunks == 1;
+  double* dst = out;
+  int64_t chunk_stride = 0;
+  bool own_ws = false;
+  if (!direct) {
+    if (workspace == nullptr) {
+      cudaError_t e = cudaMallocAsync(&workspace, plan.workspace_bytes, stream);
+      if (e != cudaSuccess) return cuda_check(e, "cudaMallocAsync(workspace)");
+      own_ws = true;
+    }
+    dst = static_cast<double*>(workspace);
+    chunk_stride = (int64_t)plan.n_rows * n_obs;
+  }
+  if (n_prisms == 0) {
+    cudaError_t e = cudaMemsetAsync(out, 0, sizeof(double) * plan.n_rows * n_obs, stream);
+    if (own_ws) cudaFreeAsync(workspace, stream);
+    return cuda_check(e, "cudaMemsetAsync(out)");
+  }
+  if (flag == nullptr) check_singular = false;
+  dim3 grid((unsigned)plan.n_tiles, (unsigned)plan.n_chunks);
+  const int scale = direct ? 1 : 0;
+  const int cs = check_singular ? 1 : 0;
+  int32_t* fl = flag;
+  if (plan.all) {
+    forward_kernel<kAll, Source><<<grid, kThreads, 0, stream>>>(
+        oe, on, ou, n_obs, src, n_prisms, plan.chunk, mask, dst, chunk_stride, scale, cs, fl);
+  } else {
+    switch (plan.single_field) {
+#define HG_CASE(FF)                                                                            \
+  case FF:                                                                                     \
+    forward_kernel<FF, Source><<<grid, kThreads, 0, stream>>>(oe, on, ou, n_obs, src, n_prisms, \
+                                                             plan.chunk, mask, dst,            \
+                                                             chunk_stride, scale, cs, fl);     \
+    break;
+      HG_CASE(0) HG_CASE(1) HG_CASE(2) HG_CASE(3) HG_CASE(4)
+      HG_CASE(5) HG_CASE(6) HG_CASE(7) HG_CASE(8) HG_CASE(9)
+#undef HG_CASE
+      default: return set_error(HG_ERR_INVALID, "bad field");
+    }
+  }
+  int rc = cuda_check(cudaGetLastError(), "forward_kernel launch");
+  if (rc != HG_OK) return rc;
+  if (!direct) {
+    RowFields rf{};
+    int r = 0;
+    for (int f = 0; f < kNumFields; f++)
+      if ((mask >> f) & 1u) rf.f[r++] = f;
+    int64_t total = (int64_t)plan.n_rows * n_obs;
+    int threads = 256;
+    int64_t blocks = (total + threads - 1) / threads;
+    reduce_chunks_kernel<<<(unsigned)blocks, threads, 0, stream>>>(
+        dst, plan.n_chunks, chunk_stride, n_obs, plan.n_rows, rf, out);
+    rc = cuda_check(cudaGetLastError(), "reduce_chunks_kernel launch");
+    if (own_ws) cudaFreeAsync(workspace, stream);
+    if (rc != HG_OK) return rc;
+  }
+  return HG_OK;
+}
+
+bool valid_mask(uint32_t m) { return m != 0 && (m & ~HG_FIELD_MASK_ALL) == 0; }
+
+}  // namespace hg
+
+using namespace hg;
+
+extern "C" {
+
+int hg_version(void) { return 100; }
+
+const char* hg_last_error(void) { return g_last_error.c_str(); }
+
+int hg_pack_prisms(const double* prisms_aos, const double* density, int64_t n_prisms,
+                   double* prisms_soa, int64_t prism_stride, void* stream) {
+  if (n_prisms < 0 || prism_stride < n_prisms) return set_error(HG_ERR_INVALID, "bad sizes");
+  if (n_prisms == 0) return HG_OK;
+  if (!prisms_aos || !density || !prisms_soa) return set_error(HG_ERR_INVALID, "null pointer");
+  int threads = 256;
+  int64_t blocks = (n_prisms + threads - 1) / threads;
+  pack_prisms_kernel<<<(unsigned)blocks, threads, 0, (cudaStream_t)stream>>>(
+      prisms_aos, density, n_prisms, prisms_soa, prism_stride);
+  return cuda_check(cudaGetLastError(), "pack_prisms_kernel launch");
+}
+
+int hg_prism_forward_workspace(int64_t n_obs, int64_t n_prisms, uint32_t field_mask,
+                               size_t* bytes) {
+  if (!bytes) return set_error(HG_ERR_INVALID, "null pointer");
+  if (n_obs < 0 || n_prisms < 0 || !valid_mask(field_mask))
+    return set_error(HG_ERR_INVALID, "bad sizes or field mask");
+  *bytes = make_plan(n_obs, n_prisms, field_mask).workspace_bytes;
+  return HG_OK;
+}
+
+int hg_prism_forward(const double* obs_e, const double* obs_n, const double* obs_u, int64_t n_obs,
+                     const double* prisms_soa, int64_t prism_stride, int64_t n_prisms,
+                     uint32_t field_mask, double* out, int32_t* singular_flag, void* workspace,
+                     size_t workspace_bytes, void* stream) {
+  if (n_obs < 0 || n_prisms < 0 || prism_stride < n_prisms || !valid_mask(field_mask))
+    return set_error(HG_ERR_INVALID, "bad sizes or field mask");
+  if (n_obs > 0 && (!obs_e || !obs_n || !obs_u || !out))
+    return set_error(HG_ERR_INVALID, "null pointer");
+  if (n_prisms > 0 && !prisms_soa) return set_error(HG_ERR_INVALID, "null prisms pointer");
+  Plan plan = make_plan(n_obs, n_prisms, field_mask);
+  if (workspace && workspace_bytes < plan.workspace_bytes)
+    return set_error(HG_ERR_INVALID, "workspace too small");
+  ListSource src{prisms_soa, prism_stride};
+  return launch_forward(plan, obs_e, obs_n, obs_u, n_obs, src, n_prisms, field_mask, out,
+                        singular_flag, workspace, (cudaStream_t)stream, true);
+}
+
+int hg_layer_forward_workspace(int64_t n_obs, int64_t n_east, int64_t n_north,
+                               uint32_t field_mask, size_t* bytes) {
+  if (!bytes) return set_error(HG_ERR_INVALID, "null pointer");
+  if (n_obs < 0 || n_east < 0 || n_north < 0 || !valid_mask(field_mask))
+    return set_error(HG_ERR_INVALID, "bad sizes or field mask");
+  *bytes = make_plan(n_obs, n_east * n_north, field_mask).workspace_bytes;
+  return HG_OK;
+}
+
+int hg_layer_forward(const double* obs_e, const double* obs_n, const double* obs_u, int64_t n_obs,
+                     const double* centre_e, int64_t n_east, const double* centre_n,
+                     int64_t n_north, const double* bottom, const double* top,
+                     const double* density, double thickness_threshold, uint32_t field_mask,
+                     double* out, void* workspace, size_t workspace_bytes, void* stream) {
+  if (n_obs < 0 || n_east < 2 || n_north < 2 || !valid_mask(field_mask))
+    return set_error(HG_ERR_INVALID, "bad sizes or field mask (layer needs >= 2 x 2 prisms)");
+  if (n_obs > 0 && (!obs_e || !obs_n || !obs_u || !out))
+    return set_error(HG_ERR_INVALID, "null pointer");
+  if (!centre_e || !centre_n || !bottom || !top || !density)
+    return set_error(HG_ERR_INVALID, "null layer pointer");
+  cudaStream_t st = (cudaStream_t)stream;
+  int64_t n_prisms = n_east * n_north;
+  Plan plan = make_plan(n_obs, n_prisms, field_mask);
+  if (workspace && workspace_bytes < plan.workspace_bytes)
+    return set_error(HG_ERR_INVALID, "workspace too small");
+  LayerSource src{centre_e, centre_n, bottom, top, density, n_east, thickness_threshold};
+  return launch_forward(plan, obs_e, obs_n, obs_u, n_obs, src, n_prisms, field_mask, out, nullptr,
+                        workspace, st, false);
+}
+
+}  // extern "C"

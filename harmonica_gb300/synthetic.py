@@ -1,0 +1,74 @@
+"""
+Seeded synthetic prism layers and surveys with the sizes of the standard
+benchmark workloads (no public dataset is involved; these stand in for the
+ETOPO-based layers of harmonica's gallery, doc/gallery_src/forward/).
+
+* ``layer_topography_1e4`` : 100 x 100 prisms on a 1 km grid over
+  [0, 100 km]^2, bottoms at -30 000 m, tops a sum of 20 Gaussians (centres
+  uniform in the region, amplitudes N(0, 800 m), widths U(5, 30) km, seed 0),
+  densities U(2000, 3000) kg/m^3 (seed 1); 50 x 50 stations at 1000 m.
+* ``layer_topography_1e6`` : 1000 x 1000 prisms on a 200 m grid (200 km
+  square), bottoms at -10 000 m, Gaussian-sum tops (seed 2), densities
+  U(1800, 3100) (seed 2); 500 x 500 stations at 2000 m + N(0, 50 m) (seed 3).
+"""
+
+import numpy as np
+
+
+def gaussian_topography(easting, northing, region, n_bumps, seed):
+    rng = np.random.default_rng(seed)
+    w, e, s, n = region
+    ce = rng.uniform(w, e, n_bumps)
+    cn = rng.uniform(s, n, n_bumps)
+    amp = rng.normal(0.0, 800.0, n_bumps)
+    width = rng.uniform(5e3, 30e3, n_bumps)
+    ge, gn = np.meshgrid(easting, northing)
+    top = np.zeros_like(ge)
+    for k in range(n_bumps):
+        top += amp[k] * np.exp(-((ge - ce[k]) ** 2 + (gn - cn[k]) ** 2) / (2 * width[k] ** 2))
+    return top
+
+
+def layer_topography_1e4():
+    """Returns dict(easting, northing, top, bottom, density, coordinates)."""
+    spacing = 1000.0
+    easting = np.arange(100) * spacing + spacing / 2
+    northing = np.arange(100) * spacing + spacing / 2
+    region = (0.0, 100e3, 0.0, 100e3)
+    top = gaussian_topography(easting, northing, region, 20, seed=0)
+    bottom = np.full_like(top, -30000.0)
+    density = np.random.default_rng(1).uniform(2000, 3000, top.shape)
+    se, sn = np.meshgrid(np.linspace(0, 100e3, 50), np.linspace(0, 100e3, 50))
+    coordinates = (se.ravel(), sn.ravel(), np.full(se.size, 1000.0))
+    return dict(easting=easting, northing=northing, top=top, bottom=bottom, density=density,
+                coordinates=coordinates)
+
+
+def layer_topography_1e6(n_side=1000, n_stations_side=500):
+    """The 1e6-prism layer (or a smaller one with the same recipe)."""
+    spacing = 200e3 / n_side
+    easting = np.arange(n_side) * spacing + spacing / 2
+    northing = np.arange(n_side) * spacing + spacing / 2
+    region = (0.0, 200e3, 0.0, 200e3)
+    top = gaussian_topography(easting, northing, region, 20, seed=2)
+    bottom = np.full_like(top, -10000.0)
+    density = np.random.default_rng(2).uniform(1800, 3100, top.shape)
+    se, sn = np.meshgrid(
+        np.linspace(0, 200e3, n_stations_side), np.linspace(0, 200e3, n_stations_side)
+    )
+    up = 2000.0 + np.random.default_rng(3).normal(0.0, 50.0, se.size)
+    coordinates = (se.ravel(), sn.ravel(), up)
+    return dict(easting=easting, northing=northing, top=top, bottom=bottom, density=density,
+                coordinates=coordinates)
+
+
+def layer_to_prisms(layer):
+    """(M, 6) prism array and (M,) densities of a layer dict, row-major (northing, easting)."""
+    e, n = layer["easting"], layer["northing"]
+    he, hn = (e[1] - e[0]) / 2, (n[1] - n[0]) / 2
+    ge, gn = np.meshgrid(e, n)
+    prisms = np.column_stack(
+        [ge.ravel() - he, ge.ravel() + he, gn.ravel() - hn, gn.ravel() + hn,
+         layer["bottom"].ravel(), layer["top"].ravel()]
+    )
+    return prisms, layer["density"].ravel()

@@ -1,0 +1,112 @@
+/*
+ * harmonica_gb300 — C ABI of the GB300 (sm_103a) prism gravity forward model.
+ *
+ * Every entry point takes plain pointers and sizes; no C++ or torch types
+ * cross this boundary and no exception escapes it.  Unless stated otherwise,
+ * array arguments are DEVICE pointers owned by the caller, the work is queued
+ * asynchronously on `stream` (a cudaStream_t, NULL = legacy default stream),
+ * and the return value is HG_OK or a negative HG_ERR_* code whose message is
+ * available from hg_last_error() on the calling thread.
+ *
+ * Field codes and bit masks (harmonica FIELDS, src/harmonica/_forward/prisms/gravity.py:37-48):
+ *   0 potential  (J/kg)     bit 1<<0
+ *   1 g_e        (mGal)     bit 1<<1
+ *   2 g_n        (mGal)     bit 1<<2
+ *   3 g_z        (mGal, downward)   bit 1<<3
+ *   4 g_ee       (Eotvos)   bit 1<<4
+ *   5 g_nn       (Eotvos)   bit 1<<5
+ *   6 g_zz       (Eotvos)   bit 1<<6
+ *   7 g_en       (Eotvos)   bit 1<<7
+ *   8 g_ez       (Eotvos, easting-downward)   bit 1<<8
+ *   9 g_nz       (Eotvos, northing-downward)  bit 1<<9
+ * Outputs carry harmonica's units and signs (gravity.py:227-236).  With more
+ * than one bit set, `out` holds one row of n_obs values per requested field,
+ * in increasing field-code order.
+ */
+#ifndef HARMONICA_GB300_H
+#define HARMONICA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HG_OK 0
+#define HG_ERR_INVALID (-1)
+#define HG_ERR_CUDA (-2)
+
+#define HG_FIELD_MASK_ALL 0x3FFu
+
+/* Library version (major*10000 + minor*100 + patch). */
+int hg_version(void);
+
+/* Message of the last failed call on this thread ("" if none). */
+const char *hg_last_error(void);
+
+/*
+ * Pack an (n_prisms, 6) row-major array [w, e, s, n, b, t] and a density
+ * vector into the structure-of-arrays layout the forward kernels read:
+ * 7 rows (w, e, s, n, b, t, rho) of `prism_stride` doubles each.
+ * Replaces the host-side reshaping of harmonica's prism_gravity
+ * (np.atleast_2d / ravel, gravity.py:200-205).
+ */
+int hg_pack_prisms(const double *prisms_aos, const double *density, int64_t n_prisms,
+                   double *prisms_soa, int64_t prism_stride, void *stream);
+
+/*
+ * Bytes of device workspace hg_prism_forward needs for this problem
+ * (0 when the launch writes `out` directly).
+ */
+int hg_prism_forward_workspace(int64_t n_obs, int64_t n_prisms, uint32_t field_mask,
+                               size_t *bytes);
+
+/*
+ * All-pairs prism gravity: out[f][i] = sum over prisms j of the field f of
+ * prism j at observation point i.  Replaces harmonica's hot loop
+ * jit_prism_gravity (src/harmonica/_forward/prisms/gravity.py:489-545) with
+ * the null-prism discard of _discard_null_prisms (gravity.py:452-486) fused
+ * (prisms with w == e, s == n, b == t or rho == 0 contribute nothing) and the
+ * singular-point scan of _check_singular_points (gravity.py:239-449) fused:
+ * if `singular_flag` is not NULL, *singular_flag is OR-ed with 1 when any
+ * observation point lies on a singular edge or vertex of any prism (null
+ * prisms included) for a requested tensor field; the caller zeroes it first.
+ * Tensor values at singular points are NaN, as in the reference.
+ *   obs_e/n/u    : n_obs doubles each
+ *   prisms_soa   : 7 rows of prism_stride doubles (see hg_pack_prisms)
+ *   out          : popcount(field_mask) rows of n_obs doubles
+ *   workspace    : hg_prism_forward_workspace() bytes, or NULL to let the
+ *                  library allocate it on `stream` (cudaMallocAsync).
+ */
+int hg_prism_forward(const double *obs_e, const double *obs_n, const double *obs_u, int64_t n_obs,
+                     const double *prisms_soa, int64_t prism_stride, int64_t n_prisms,
+                     uint32_t field_mask, double *out, int32_t *singular_flag, void *workspace,
+                     size_t workspace_bytes, void *stream);
+
+/* Bytes of device workspace hg_layer_forward needs for this problem. */
+int hg_layer_forward_workspace(int64_t n_obs, int64_t n_east, int64_t n_north,
+                               uint32_t field_mask, size_t *bytes);
+
+/*
+ * Prism-layer forward.  Replaces the loop of _forward_gravity_prism_layer
+ * (src/harmonica/_forward/prisms/layer.py:522-633) behind
+ * DatasetAccessorPrismLayer.gravity (layer.py:314-433): prism boundaries are
+ * generated from the regular grid of centres +- half the spacing, and prisms
+ * with zero or NaN density, thickness below `thickness_threshold`, or NaN top
+ * or bottom are skipped (layer.py:596-607).
+ *   centre_e     : n_east easting centres (regular, n_east >= 2)
+ *   centre_n     : n_north northing centres (regular, n_north >= 2)
+ *   bottom, top, density : (n_north, n_east) row-major
+ */
+int hg_layer_forward(const double *obs_e, const double *obs_n, const double *obs_u, int64_t n_obs,
+                     const double *centre_e, int64_t n_east, const double *centre_n,
+                     int64_t n_north, const double *bottom, const double *top,
+                     const double *density, double thickness_threshold, uint32_t field_mask,
+                     double *out, void *workspace, size_t workspace_bytes, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HARMONICA_GB300_H */

@@ -1,0 +1,263 @@
+"""
+Parity of the CUDA path (through the C ABI) with the CPU oracle, and the
+behavioural tests of harmonica's own suite run on the GPU.
+
+Tolerance (FP64 forward): |gpu - oracle| <= 1e-8 |oracle| + 1e-9 max|oracle|
+per output array, unless a test states otherwise.
+"""
+
+import json
+import os
+import warnings
+
+import numpy as np
+import numpy.testing as npt
+import pytest
+
+import harmonica_gb300 as hg
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+FIELDS = hg.FIELDS
+RTOL = 1e-8
+ATOL_FRAC = 1e-9
+
+
+def assert_parity(actual, expected, rtol=RTOL, atol_frac=ATOL_FRAC, msg=""):
+    expected = np.asarray(expected)
+    finite = np.isfinite(expected)
+    atol = atol_frac * (np.max(np.abs(expected[finite])) if finite.any() else 0.0)
+    npt.assert_allclose(actual, expected, rtol=rtol, atol=atol, err_msg=msg)
+
+
+def random_problem(seed, n_prisms, n_obs, spread=5e3):
+    rng = np.random.default_rng(seed)
+    west = rng.uniform(-spread, spread * 0.8, n_prisms)
+    south = rng.uniform(-spread, spread * 0.8, n_prisms)
+    bottom = rng.uniform(-3e3, -200, n_prisms)
+    prisms = np.column_stack(
+        [
+            west,
+            west + rng.uniform(20, 1500, n_prisms),
+            south,
+            south + rng.uniform(20, 1500, n_prisms),
+            bottom,
+            bottom + rng.uniform(20, 1500, n_prisms),
+        ]
+    )
+    density = rng.uniform(-600, 600, n_prisms)
+    coords = (
+        rng.uniform(-1.2 * spread, 1.2 * spread, n_obs),
+        rng.uniform(-1.2 * spread, 1.2 * spread, n_obs),
+        rng.uniform(-500, 800, n_obs),  # some points inside/below prisms
+    )
+    return coords, prisms, density
+
+
+def test_reference_doctest_vectors(gpu_lib):
+    gold = json.load(open(os.path.join(GOLDEN, "reference_doctests.json")))
+    for case in ("single_prism", "two_prisms"):
+        c = gold[case]
+        gz = hg.prism_gravity(gold["coordinates"], c["prisms"], c["density"], field="g_z")
+        npt.assert_allclose(np.round(gz, 5), c["g_z"], rtol=0, atol=0)
+
+
+@pytest.mark.parametrize("field", FIELDS)
+def test_against_golden_choclo_fixture(gpu_lib, field):
+    """TestAgainstChoclo inputs (test/test_prism.py:161-244) vs oracle fixture."""
+    g = np.load(os.path.join(GOLDEN, "oracle_small.npz"))
+    coords = (g["choclo_e"], g["choclo_n"], g["choclo_u"])
+    result = hg.prism_gravity(coords, g["choclo_prisms"], g["choclo_density"], field=field)
+    assert_parity(result, g[f"choclo_{field}"], msg=field)
+
+
+@pytest.mark.parametrize("field", FIELDS)
+def test_random_prisms_against_oracle(gpu_lib, oracle, field):
+    coords, prisms, density = random_problem(1, 400, 300)
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        ref = oracle.prism_gravity(coords, prisms, density, field)
+        res = hg.prism_gravity(coords, prisms, density, field=field)
+    assert_parity(res, ref, msg=field)
+
+
+def test_fused_all_fields_match_single(gpu_lib):
+    coords, prisms, density = random_problem(2, 257, 190)
+    fused = hg.prism_gravity_fields(coords, prisms, density, FIELDS)
+    for f in FIELDS:
+        single = hg.prism_gravity(coords, prisms, density, field=f)
+        npt.assert_allclose(fused[f], single, rtol=1e-13, atol=1e-13 * np.max(np.abs(single)))
+
+
+def test_many_chunks_and_ragged_sizes(gpu_lib, oracle):
+    """Few points and many prisms (split across CTAs), sizes not multiples of the tiles."""
+    for n_obs, n_prisms in ((1, 1), (3, 129), (7, 5000), (129, 1), (300, 3001)):
+        coords, prisms, density = random_problem(n_obs + n_prisms, n_prisms, n_obs)
+        ref = oracle.prism_gravity(coords, prisms, density, "g_z")
+        res = hg.prism_gravity(coords, prisms, density, field="g_z")
+        assert_parity(res, ref, msg=f"{n_obs}x{n_prisms}")
+
+
+def test_empty_inputs(gpu_lib):
+    res = hg.prism_gravity((np.zeros(0), np.zeros(0), np.zeros(0)), [0, 1, 0, 1, -1, 0], 1.0,
+                           field="g_z")
+    assert res.shape == (0,)
+    # only null prisms -> zeros (gravity.py:452-486 discards them)
+    res = hg.prism_gravity(([0.0, 5.0], [0.0, 1.0], [1.0, 1.0]), [[0, 0, 0, 1, -1, 0]], [10.0],
+                           field="g_z")
+    npt.assert_array_equal(res, np.zeros(2))
+
+
+def test_output_shape_and_dtype(gpu_lib):
+    e, n = np.meshgrid(np.linspace(-100, 100, 4), np.linspace(-50, 50, 3))
+    res = hg.prism_gravity((e, n, 10.0), [-20, 20, -20, 20, -50, -10], 2000, field="g_z",
+                           dtype="float32")
+    assert res.shape == (3, 4) and res.dtype == np.float32
+
+
+def test_infinite_slab(gpu_lib):
+    """test/test_prism.py:269-297"""
+    height, thickness, density = 1.5, 10.5, 2670
+    sizes = np.logspace(3, 9, 7)
+    results = np.array(
+        [
+            hg.prism_gravity(
+                (0, 0, height), [-s / 2, s / 2, -s / 2, s / 2, height - thickness, height],
+                density, field="g_z",
+            )
+            for s in sizes
+        ]
+    )
+    analytical = 1e5 * 2 * np.pi * 6.6743e-11 * density * thickness
+    errors = np.abs(analytical - results)
+    assert (errors[1:] < errors[:-1]).all()
+    npt.assert_allclose(analytical, results[-1], rtol=1e-7)
+
+
+def test_laplace(gpu_lib):
+    """test/test_prism.py:247-266"""
+    e, n = np.meshgrid(np.linspace(-10e3, 10e3, 10), np.linspace(-10e3, 10e3, 10))
+    coords = (e, n, np.full_like(e, 300.0))
+    prisms = [[1e3, 7e3, -5e3, 2e3, -1e3, -500], [-4e3, 1e3, 4e3, 10e3, -2e3, 200]]
+    rho = [2670.0, 2900.0]
+    d = {f: hg.prism_gravity(coords, prisms, rho, field=f) for f in ("g_ee", "g_nn", "g_zz")}
+    npt.assert_allclose(d["g_ee"] + d["g_nn"], -d["g_zz"], rtol=1e-7, atol=1e-9)
+
+
+def test_null_prisms_and_disable_checks(gpu_lib):
+    """test/test_prism.py:115-158"""
+    e, n = np.meshgrid(np.linspace(-50, 50, 3), np.linspace(-50, 50, 3))
+    coords = (e, n, np.zeros_like(e))
+    prisms = [
+        [-100, 100, -200, 200, -10e3, -5e3],
+        [100, 200, 200, 300, -10e3, -4e3],
+        [30, 30, -200, 200, -10e3, -5e3],
+        [100, 200, 30, 30, -10e3, -5e3],
+        [-100, 100, -200, 200, -10e3, -10e3],
+    ]
+    density = [2600, 0, 3000, 3100, 3200]
+    npt.assert_allclose(
+        hg.prism_gravity(coords, prisms, density, field="g_z"),
+        hg.prism_gravity(coords, [prisms[0]], [density[0]], field="g_z"),
+    )
+    valid, invalid = [0, 10, 0, 10, -10, 0], [0, 10, 0, 10, 0, -10]
+    npt.assert_allclose(
+        hg.prism_gravity([0, 0, 0], invalid, 100, field="potential", disable_checks=True),
+        -hg.prism_gravity([0, 0, 0], valid, 100, field="potential"),
+    )
+
+
+def _vertices(p):
+    return tuple(c.ravel() for c in np.meshgrid(p[:2], p[2:4], p[4:6]))
+
+
+@pytest.mark.parametrize("field", ["g_ee", "g_nn", "g_zz", "g_en", "g_ez", "g_nz"])
+def test_singular_vertices(gpu_lib, field):
+    """test/test_prism.py:380-400: warning, and NaN values (gravity.py:151)."""
+    prism = np.array([-10.3, 5.4, 8.6, 14.3, -30.3, 2.4])
+    e, n, u = _vertices(prism)
+    for i in range(e.size):
+        with pytest.warns(UserWarning, match="Found observation point"):
+            v = hg.prism_gravity((e[i], n[i], u[i]), prism, [2900.0], field=field)
+        assert np.isnan(v)
+    # no warning with disable_checks, still NaN
+    with warnings.catch_warnings():
+        warnings.simplefilter("error")
+        v = hg.prism_gravity((e[0], n[0], u[0]), prism, [2900.0], field=field,
+                             disable_checks=True)
+    assert np.isnan(v)
+
+
+def test_singular_edges_and_regular_neighbours(gpu_lib, oracle):
+    """test/test_prism.py:402-502 and finiteness of the other components."""
+    prism = np.array([-10.3, 5.4, 8.6, 14.3, -30.3, 2.4])
+    ec, nc, uc = (prism[0] + prism[1]) / 2, (prism[2] + prism[3]) / 2, (prism[4] + prism[5]) / 2
+    n, u = (c.ravel() for c in np.meshgrid(prism[2:4], prism[4:6]))
+    e_edges = (np.full_like(n, ec), n, u)
+    e, u = (c.ravel() for c in np.meshgrid(prism[0:2], prism[4:6]))
+    n_edges = (e, np.full_like(e, nc), u)
+    e, n = (c.ravel() for c in np.meshgrid(prism[0:2], prism[2:4]))
+    u_edges = (e, n, np.full_like(e, uc))
+    cases = [
+        (e_edges, ("g_nn", "g_zz", "g_nz"), ("g_ee", "g_en", "g_ez")),
+        (n_edges, ("g_ee", "g_zz", "g_ez"), ("g_nn", "g_en", "g_nz")),
+        (u_edges, ("g_ee", "g_nn", "g_en"), ("g_zz", "g_ez", "g_nz")),
+    ]
+    for pts, singular, regular in cases:
+        for f in singular:
+            with pytest.warns(UserWarning, match="Found observation point"):
+                v = hg.prism_gravity(pts, prism, [2900.0], field=f)
+            assert np.all(np.isnan(v))
+        for f in regular + ("potential", "g_e", "g_n", "g_z"):
+            with warnings.catch_warnings():
+                warnings.simplefilter("error")
+                v = hg.prism_gravity(pts, prism, [2900.0], field=f)
+            assert_parity(v, oracle.prism_gravity(pts, prism, [2900.0], f), msg=f)
+
+
+def test_points_on_faces_and_edge_extensions(gpu_lib, oracle):
+    """Face planes (outside limit of diagonal tensors) and extensions of edges."""
+    prism = np.array([-10.0, 20.0, -5.0, 15.0, -40.0, -10.0])
+    pts = []
+    for e in (-10.0, 20.0, 5.0, -30.0, 40.0):
+        for n in (-5.0, 15.0, 3.0, -25.0, 35.0):
+            for u in (-40.0, -10.0, -20.0, 5.0, -60.0):
+                pts.append((e, n, u))
+    pts = np.array(pts)
+    coords = (pts[:, 0], pts[:, 1], pts[:, 2])
+    for f in FIELDS:
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            ref = oracle.prism_gravity(coords, prism, [1000.0], f)
+            res = hg.prism_gravity(coords, prism, [1000.0], field=f)
+        npt.assert_array_equal(np.isnan(res), np.isnan(ref), err_msg=f)
+        ok = np.isfinite(ref)
+        assert_parity(res[ok], ref[ok], msg=f)
+
+
+def test_determinism(gpu_lib):
+    coords, prisms, density = random_problem(3, 2000, 50)
+    a = hg.prism_gravity(coords, prisms, density, field="g_z")
+    b = hg.prism_gravity(coords, prisms, density, field="g_z")
+    npt.assert_array_equal(a, b)
+
+
+def test_distant_prisms_against_mpmath(gpu_lib, oracle):
+    """Far prisms, where the closed form cancels: the GPU result is compared
+    with 50-digit arithmetic; it is within 1e-9 at 100 prism sizes and never
+    much worse than the per-vertex FP64 sum further out."""
+    mp_check = pytest.importorskip("oracle.mp_check")
+    rng = np.random.default_rng(9)
+    for _ in range(3):
+        w, s = rng.uniform(-100, 100, 2)
+        prism = [w, w + 50, s, s + 70, -2000, -1900]
+        for dist in (5e3, 5e4):
+            point = (dist * rng.uniform(0.5, 1), dist * rng.uniform(-1, 1), 100.0)
+            for f in FIELDS:
+                ref = mp_check.prism_gravity(f, [point], [prism], [2500.0])[0]
+                ours = abs(hg.prism_gravity(point, prism, 2500.0, field=f) - ref) / abs(ref)
+                base = abs(oracle.prism_gravity(point, prism, [2500.0], f) - ref) / abs(ref)
+                if dist <= 5e3:
+                    assert ours <= 1e-9, (f, dist, ours)
+                assert ours <= max(10 * base, 1e-9), (f, dist, ours, base)
