@@ -153,30 +153,48 @@ HG_HD __forceinline__ double edge_log(AxisCase c, double a1, double a2, double r
 // b_1 < b_2, c_1 < c_2 and vertex distances r[bi][ci]:
 //   O = sum_{bi,ci} s_b s_c atan(b c / (a r)).
 // For a != 0, atan(bc/(ar)) = sign(a) arg(|a| r + i bc) with a positive real
-// part, so the two pairs (22 - 12) and (11 - 21) are each an argument
-// difference in (-pi, pi) and equal arg(c22 conj(c12)) and arg(c11 conj(c21))
-// exactly.  For a == 0 the value is the limit from outside the prism:
+// part, so each pair of vertices along b is an argument difference in
+// (-pi, pi) and equals the argument of one complex product:
+//   arg(c_2c) - arg(c_1c) = arg((|a| r_2c + i b2 c)(|a| r_1c - i b1 c))
+//     = atan2(|a| c (b2 r_1c - b1 r_2c), a^2 r_1c r_2c + b1 b2 c^2).
+// For a distant face b2 r_1c - b1 r_2c cancels; when b1, b2 have one sign it
+// is rewritten without cancellation as
+//   (b2 - b1)(b2 + b1)(a^2 + c^2) / (b2 r_1c + b1 r_2c)
+// and the positive denominator is moved into the real part (atan2 is
+// invariant under scaling both arguments by a positive number).
+// For a == 0 the value is the limit from outside the prism:
 // a -> 0+ for the lower face (upper == false), a -> 0- for the upper face.
+HG_HD __forceinline__ double pair_angle(double aa, double a2, double b1, double b2, double c,
+                                        double c2, double r1, double r2, bool same_sign) {
+  double re = a2 * r1 * r2 + b1 * b2 * c2;
+  double d;
+  if (same_sign) {
+    double den = b2 * r1 + b1 * r2;  // one sign, no cancellation
+    d = (b2 - b1) * (b2 + b1) * (a2 + c2);
+    if (den < 0.0) {
+      den = -den;
+      d = -d;
+    }
+    re *= den;
+  } else {
+    d = b2 * r1 - b1 * r2;  // b1 < 0 < b2: both terms positive
+  }
+  return atan2(aa * c * d, re);
+}
+
 HG_HD __forceinline__ double face_angle(double a, bool upper, double b1, double b2, double c1,
-                                             double c2, double r11, double r12, double r21,
-                                             double r22) {
+                                        double c2, double r11, double r12, double r21,
+                                        double r22) {
   if (is_zero(a)) {
     int s = sgn(b2) * sgn(c2) + sgn(b1) * sgn(c1) - sgn(b1) * sgn(c2) - sgn(b2) * sgn(c1);
     return (upper ? -kHalfPi : kHalfPi) * (double)s;
   }
-  double aa = fabs(a);
-  // c_bc = aa * r_bc + i * b c
-  double re22 = aa * r22, im22 = b2 * c2;
-  double re12 = aa * r12, im12 = b1 * c2;
-  double re11 = aa * r11, im11 = b1 * c1;
-  double re21 = aa * r21, im21 = b2 * c1;
-  // c22 * conj(c12)
-  double pr = re22 * re12 + im22 * im12;
-  double pi = im22 * re12 - re22 * im12;
-  // c11 * conj(c21)
-  double qr = re11 * re21 + im11 * im21;
-  double qi = im11 * re21 - re11 * im21;
-  double o = atan2(pi, pr) + atan2(qi, qr);
+  const double aa = fabs(a);
+  const double asq = a * a;
+  const bool same_sign = !(is_neg(b1) && !is_nonpos(b2));
+  // (22 - 12) + (11 - 21) = [arg c_{2,c2} - arg c_{1,c2}] - [arg c_{2,c1} - arg c_{1,c1}]
+  double o = pair_angle(aa, asq, b1, b2, c2, c2 * c2, r12, r22, same_sign) -
+             pair_angle(aa, asq, b1, b2, c1, c1 * c1, r11, r21, same_sign);
   return is_neg(a) ? -o : o;
 }
 

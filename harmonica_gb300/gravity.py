@@ -130,9 +130,7 @@ def pack_prisms(prisms, density):
 def _prepare(coordinates, prisms, density, disable_checks):
     cast = np.broadcast(*coordinates[:3])
     coords = tuple(
-        np.ascontiguousarray(
-            np.broadcast_to(np.asarray(c, dtype=np.float64), cast.shape)
-        ).ravel()
+        np.array(np.broadcast_to(np.asarray(c, dtype=np.float64), cast.shape)).ravel()
         for c in coordinates[:3]
     )
     prisms = np.atleast_2d(np.asarray(prisms, dtype=np.float64))

@@ -258,9 +258,7 @@ class DatasetAccessorPrismLayer:
         _check_regular_grid(self._obj.easting.values, self._obj.northing.values)
         cast = np.broadcast(*coordinates[:3])
         coords = tuple(
-            np.ascontiguousarray(
-                np.broadcast_to(np.asarray(c, dtype=np.float64), cast.shape)
-            ).ravel()
+            np.array(np.broadcast_to(np.asarray(c, dtype=np.float64), cast.shape)).ravel()
             for c in coordinates[:3]
         )
         thickness_threshold = 0.0 if thickness_threshold is None else thickness_threshold
