@@ -98,6 +98,20 @@ __global__ void __launch_bounds__(kThreads) forward_kernel(
   __shared__ double sh_w[kTile], sh_e[kTile], sh_s[kTile], sh_n[kTile], sh_b[kTile], sh_t[kTile],
       sh_rho[kTile];
   __shared__ int sh_null[kTile];
+  // constant tables of the FP64 elementary functions, staged once per CTA
+  __shared__ double sh_logc[lean::kLogTableSize], sh_logl[lean::kLogTableSize];
+  __shared__ double sh_th[lean::kArgTableSize], sh_cs[lean::kArgTableSize],
+      sh_sn[lean::kArgTableSize];
+  for (int t = threadIdx.x; t < lean::kLogTableSize; t += blockDim.x) {
+    sh_logc[t] = lean::kLogC[t];
+    sh_logl[t] = lean::kLogL[t];
+  }
+  for (int t = threadIdx.x; t < lean::kArgTableSize; t += blockDim.x) {
+    sh_th[t] = lean::kArgTh[t];
+    sh_cs[t] = lean::kArgCos[t];
+    sh_sn[t] = lean::kArgSin[t];
+  }
+  const Tables T{sh_logc, sh_logl, sh_th, sh_cs, sh_sn};
 
   const int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x;
   const bool active = i < n_obs;
@@ -148,17 +162,16 @@ __global__ void __launch_bounds__(kThreads) forward_kernel(
       }
       if (sh_null[p]) continue;  // uniform across the CTA
       const double rho = sh_rho[p];
-      PairTerms T;
-      pair_terms<F>(q, T);
       if (F == kAll) {
+        double v[kNumFields];
+        pair_all<true>(q, T, v);
 #pragma unroll
         for (int f = 0; f < kNumFields; f++) {
-          double v = combine(f, q, T);
-          if (is_tensor(f) && singular_for(f, q)) v = quiet_nan();
-          acc[f] = fma(rho, v, acc[f]);
+          if (is_tensor(f) && singular_for(f, q)) v[f] = quiet_nan();
+          acc[f] = fma(rho, v[f], acc[f]);
         }
       } else {
-        double v = combine(F, q, T);
+        double v = pair_field<(F < kNumFields ? F : 0), true>(q, T);
         if (is_tensor(F) && singular_for(F, q)) v = quiet_nan();
         acc[0] = fma(rho, v, acc[0]);
       }

@@ -9,10 +9,10 @@ OUT = os.path.join(HERE, "_build", "libhost_pair.so")
 
 def build():
     src = os.path.join(HERE, "host_pair.cu")
-    dep = os.path.join(os.path.dirname(os.path.dirname(HERE)), "harmonica_gb300", "csrc",
-                       "prism_math.cuh")
-    if os.path.exists(OUT) and os.path.getmtime(OUT) > max(os.path.getmtime(src),
-                                                          os.path.getmtime(dep)):
+    csrc = os.path.join(os.path.dirname(os.path.dirname(HERE)), "harmonica_gb300", "csrc")
+    deps = [src] + [os.path.join(csrc, f) for f in os.listdir(csrc)
+                    if f.endswith((".cuh", ".inc"))]
+    if os.path.exists(OUT) and os.path.getmtime(OUT) > max(os.path.getmtime(d) for d in deps):
         return OUT
     os.makedirs(os.path.dirname(OUT), exist_ok=True)
     subprocess.run(

@@ -8,25 +8,20 @@
 
 using namespace hg;
 
-template <int F>
-static double pair_value(const Rel& q) {
-  PairTerms T;
-  pair_terms<F>(q, T);
-  return combine(F, q, T);
-}
-
+template <bool LEAN>
 static double pair_any(int f, const Rel& q) {
+  const Tables T = lean::host_tables();
   switch (f) {
-    case 0: return pair_value<0>(q);
-    case 1: return pair_value<1>(q);
-    case 2: return pair_value<2>(q);
-    case 3: return pair_value<3>(q);
-    case 4: return pair_value<4>(q);
-    case 5: return pair_value<5>(q);
-    case 6: return pair_value<6>(q);
-    case 7: return pair_value<7>(q);
-    case 8: return pair_value<8>(q);
-    case 9: return pair_value<9>(q);
+    case 0: return pair_field<0, LEAN>(q, T);
+    case 1: return pair_field<1, LEAN>(q, T);
+    case 2: return pair_field<2, LEAN>(q, T);
+    case 3: return pair_field<3, LEAN>(q, T);
+    case 4: return pair_field<4, LEAN>(q, T);
+    case 5: return pair_field<5, LEAN>(q, T);
+    case 6: return pair_field<6, LEAN>(q, T);
+    case 7: return pair_field<7, LEAN>(q, T);
+    case 8: return pair_field<8, LEAN>(q, T);
+    case 9: return pair_field<9, LEAN>(q, T);
   }
   return 0.0;
 }
@@ -34,17 +29,25 @@ static double pair_any(int f, const Rel& q) {
 extern "C" {
 
 // Sum over prisms (AoS, 6 per row) for each point, harmonica units, with the
-// kernel's null-prism skip and NaN at singular points.
+// kernel's null-prism skip and NaN at singular points.  mode: 0 = lean math,
+// 1 = generic library math, 2 = lean math through the fused all-field path.
 void host_prism_gravity(int field, int64_t n_obs, const double* e, const double* n,
                         const double* u, int64_t m, const double* prisms, const double* rho,
-                        double* out) {
+                        double* out, int mode) {
   for (int64_t i = 0; i < n_obs; i++) {
     double acc = 0.0;
     for (int64_t j = 0; j < m; j++) {
       const double* p = prisms + 6 * j;
       if (p[0] == p[1] || p[2] == p[3] || p[4] == p[5] || rho[j] == 0.0) continue;
       Rel q{p[0] - e[i], p[1] - e[i], p[2] - n[i], p[3] - n[i], p[4] - u[i], p[5] - u[i]};
-      double v = pair_any(field, q);
+      double v;
+      if (mode == 2) {
+        double all[kNumFields];
+        pair_all<true>(q, lean::host_tables(), all);
+        v = all[field];
+      } else {
+        v = mode == 0 ? pair_any<true>(field, q) : pair_any<false>(field, q);
+      }
       if (field >= kGee && singular_for(field, q)) v = quiet_nan();
       acc += rho[j] * v;
     }

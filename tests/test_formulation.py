@@ -28,11 +28,11 @@ def host():
     lib = ctypes.CDLL(build_host.build())
     dp = ctypes.POINTER(ctypes.c_double)
     lib.host_prism_gravity.argtypes = [
-        ctypes.c_int, ctypes.c_int64, dp, dp, dp, ctypes.c_int64, dp, dp, dp
+        ctypes.c_int, ctypes.c_int64, dp, dp, dp, ctypes.c_int64, dp, dp, dp, ctypes.c_int
     ]
     lib.host_prism_gravity.restype = None
 
-    def run(coords, prisms, density, field):
+    def run(coords, prisms, density, field, mode=0):
         cast = np.broadcast(*coords)
         e, n, u = (
             np.ascontiguousarray(np.broadcast_to(np.asarray(c, float), cast.shape)).ravel()
@@ -43,7 +43,7 @@ def host():
         out = np.zeros(e.size)
         P = lambda a: a.ctypes.data_as(dp)  # noqa: E731
         lib.host_prism_gravity(FIELDS.index(field), e.size, P(e), P(n), P(u), p.shape[0], P(p),
-                               P(rho), P(out))
+                               P(rho), P(out), mode)
         return out.reshape(cast.shape)
 
     return run
@@ -57,8 +57,12 @@ def parity(a, b, rtol=1e-8, atol_frac=1e-9):
     npt.assert_allclose(np.asarray(a)[fin], b[fin], rtol=rtol, atol=atol)
 
 
+MODES = {"lean": 0, "libm": 1, "fused": 2}
+
+
+@pytest.mark.parametrize("mode", MODES)
 @pytest.mark.parametrize("field", FIELDS)
-def test_random_against_oracle(host, oracle, field):
+def test_random_against_oracle(host, oracle, field, mode):
     rng = np.random.default_rng(3)
     m, n = 120, 150
     w = rng.uniform(-2e3, 2e3, m)
@@ -71,11 +75,12 @@ def test_random_against_oracle(host, oracle, field):
     with warnings.catch_warnings():
         warnings.simplefilter("ignore")
         ref = oracle.prism_gravity(coords, prisms, rho, field)
-    parity(host(coords, prisms, rho, field), ref)
+    parity(host(coords, prisms, rho, field, MODES[mode]), ref)
 
 
+@pytest.mark.parametrize("mode", MODES)
 @pytest.mark.parametrize("field", FIELDS)
-def test_special_points_against_oracle(host, oracle, field):
+def test_special_points_against_oracle(host, oracle, field, mode):
     """Points on vertices, edges, faces, and on extensions of edges and faces."""
     prism = np.array([-10.0, 20.0, -5.0, 15.0, -40.0, -10.0])
     vals_e = (-10.0, 20.0, 5.0, -30.0, 40.0)
@@ -86,7 +91,7 @@ def test_special_points_against_oracle(host, oracle, field):
     with warnings.catch_warnings():
         warnings.simplefilter("ignore")
         ref = oracle.prism_gravity(coords, prism, [1000.0], field)
-    parity(host(coords, prism, [1000.0], field), ref)
+    parity(host(coords, prism, [1000.0], field, MODES[mode]), ref)
 
 
 def test_distant_prism_accuracy_vs_mpmath(host, oracle):
