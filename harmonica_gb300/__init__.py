@@ -14,12 +14,16 @@ in ``include/harmonica_gb300.h``; :func:`build` compiles them in-tree.
 """
 
 from ._native import build
+from .batch import PrismBatch, autotune, prism_gravity_batch
 from .fields import FIELDS
 from .gravity import check_prisms, prism_gravity, prism_gravity_fields
 from .layer import DatasetAccessorPrismLayer, PrismLayer, prism_layer
 
 __all__ = [
     "FIELDS",
+    "PrismBatch",
+    "autotune",
+    "prism_gravity_batch",
     "DatasetAccessorPrismLayer",
     "PrismLayer",
     "build",

@@ -26,7 +26,7 @@ HEADERS = (
 )
 
 #: translation units compiled into the library
-SOURCES = ("prism_forward.cu", "bench_probe.cu")
+SOURCES = ("prism_forward.cu", "prism_batch.cu", "bench_probe.cu")
 
 ARCH_FLAGS = ("-gencode", "arch=compute_103a,code=sm_103a")
 
@@ -104,6 +104,24 @@ def build(force=False, verbose=False):
 
 _c_double_p = ctypes.c_void_p  # device pointers travel as integers
 
+
+class HgProblem(ctypes.Structure):
+    """ctypes mirror of ``hg_problem`` (include/harmonica_gb300.h)."""
+
+    _fields_ = [
+        ("obs_e", ctypes.c_void_p),
+        ("obs_n", ctypes.c_void_p),
+        ("obs_u", ctypes.c_void_p),
+        ("n_obs", ctypes.c_int64),
+        ("prisms_soa", ctypes.c_void_p),
+        ("prism_stride", ctypes.c_int64),
+        ("n_prisms", ctypes.c_int64),
+        ("field", ctypes.c_int32),
+        ("check_singular", ctypes.c_int32),
+        ("out", ctypes.c_void_p),
+        ("singular_flag", ctypes.c_void_p),
+    ]
+
 #: ctypes prototypes of every exported symbol (must match include/harmonica_gb300.h)
 PROTOTYPES = {
     "hg_version": (ctypes.c_int, []),
@@ -123,6 +141,21 @@ PROTOTYPES = {
          ctypes.c_int64, ctypes.c_int64, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p,
          ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p],
     ),
+    "hg_batch_create": (
+        ctypes.c_int,
+        [ctypes.POINTER(HgProblem), ctypes.c_int64, ctypes.c_int64, ctypes.c_int32,
+         ctypes.POINTER(ctypes.c_void_p)],
+    ),
+    "hg_batch_workspace": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t)]),
+    "hg_batch_info": (
+        ctypes.c_int,
+        [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
+         ctypes.POINTER(ctypes.c_double)],
+    ),
+    "hg_batch_run": (
+        ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]
+    ),
+    "hg_batch_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "hg_fp64_peak_probe": (
         ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_void_p]
     ),

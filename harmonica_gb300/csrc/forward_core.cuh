@@ -1,0 +1,153 @@
+// Building blocks shared by the forward kernels (prism_forward.cu) and the
+// batched persistent kernel (prism_batch.cu): prism sources, the staging of
+// prism tiles and math tables in shared memory, and the inner loop that adds
+// the field of a range of prisms to one observation point per thread.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "prism_math.cuh"
+
+namespace hg {
+
+constexpr int kThreads = 128;  // observation points per CTA
+constexpr int kTile = 128;     // prisms staged per shared-memory tile
+constexpr int kSmCount = 152;
+
+template <int F> struct NumOut { static constexpr int value = 1; };
+template <> struct NumOut<kAll> { static constexpr int value = kNumFields; };
+
+HG_HD __forceinline__ bool is_tensor(int f) { return f >= kGee && f <= kGnz; }
+
+// ---------------------------------------------------------------------------
+// Prism sources: how a CTA loads prism p into shared memory.
+struct ListSource {
+  const double* soa;  // 7 rows (w, e, s, n, b, t, rho) of `stride` doubles
+  int64_t stride;
+  __device__ __forceinline__ void load(int64_t p, double& w, double& e, double& s, double& n,
+                                       double& b, double& t, double& rho, bool& null) const {
+    w = soa[p];
+    e = soa[stride + p];
+    s = soa[2 * stride + p];
+    n = soa[3 * stride + p];
+    b = soa[4 * stride + p];
+    t = soa[5 * stride + p];
+    rho = soa[6 * stride + p];
+    // gravity.py:475-480: zero volume or zero density
+    null = (w == e) || (s == n) || (b == t) || (rho == 0.0);
+  }
+};
+
+struct LayerSource {
+  const double* ce;
+  const double* cn;
+  const double* bottom;
+  const double* top;
+  const double* density;
+  int64_t n_east;
+  double threshold;
+  __device__ __forceinline__ void load(int64_t p, double& w, double& e, double& s, double& n,
+                                       double& b, double& t, double& rho, bool& null) const {
+    // half spacings from the first two centres, as layer.py:582-583
+    const double half_e = (ce[1] - ce[0]) / 2.0;
+    const double half_n = (cn[1] - cn[0]) / 2.0;
+    const int64_t k = p / n_east, j = p - k * n_east;
+    w = ce[j] - half_e;
+    e = ce[j] + half_e;
+    s = cn[k] - half_n;
+    n = cn[k] + half_n;
+    b = bottom[p];
+    t = top[p];
+    rho = density[p];
+    // layer.py:596-607; zero-thickness prisms add exactly zero and are skipped too
+    null = (rho == 0.0) || isnan(rho) || (t - b < threshold) || isnan(t) || isnan(b) || (b == t);
+  }
+};
+
+// ---------------------------------------------------------------------------
+struct SmemTile {
+  double w[kTile], e[kTile], s[kTile], n[kTile], b[kTile], t[kTile], rho[kTile];
+  int null[kTile];
+};
+
+struct SmemTables {
+  double logc[lean::kLogTableSize], logl[lean::kLogTableSize];
+  double th[lean::kArgTableSize], cs[lean::kArgTableSize], sn[lean::kArgTableSize];
+
+  // Copy the constant tables of lean_math.cuh; the caller synchronises.
+  __device__ __forceinline__ Tables stage() {
+    for (int t = threadIdx.x; t < lean::kLogTableSize; t += blockDim.x) {
+      logc[t] = lean::kLogC[t];
+      logl[t] = lean::kLogL[t];
+    }
+    for (int t = threadIdx.x; t < lean::kArgTableSize; t += blockDim.x) {
+      th[t] = lean::kArgTh[t];
+      cs[t] = lean::kArgCos[t];
+      sn[t] = lean::kArgSin[t];
+    }
+    return Tables{logc, logl, th, cs, sn};
+  }
+};
+
+// Adds to acc[] the field(s) F of prisms [p0, p1) of `src` at this thread's
+// point (pe, pn, pu).  Must be called by every thread of the CTA (it
+// synchronises around each shared-memory tile).  With check_singular, ORs
+// into `singular` whether the point is a singular point of any prism (null
+// prisms included, as gravity.py:207-214 scans before discarding) for the
+// tensor fields in sing_mask.  Tensor values at singular points are NaN.
+template <int F, class Source>
+__device__ __forceinline__ void accumulate(const Source& src, int64_t p0, int64_t p1, double pe,
+                                           double pn, double pu, bool active, bool check_singular,
+                                           uint32_t sing_mask, SmemTile& sh, const Tables& T,
+                                           double* acc, bool& singular) {
+  for (int64_t base = p0; base < p1; base += kTile) {
+    const int cnt = (int)min((int64_t)kTile, p1 - base);
+    __syncthreads();
+    if ((int)threadIdx.x < cnt) {
+      double w, e, s, n, b, t, rho;
+      bool null;
+      src.load(base + threadIdx.x, w, e, s, n, b, t, rho, null);
+      sh.w[threadIdx.x] = w;
+      sh.e[threadIdx.x] = e;
+      sh.s[threadIdx.x] = s;
+      sh.n[threadIdx.x] = n;
+      sh.b[threadIdx.x] = b;
+      sh.t[threadIdx.x] = t;
+      sh.rho[threadIdx.x] = rho;
+      sh.null[threadIdx.x] = null;
+    }
+    __syncthreads();
+    for (int p = 0; p < cnt; p++) {
+      Rel q;
+      q.x1 = sh.w[p] - pe;
+      q.x2 = sh.e[p] - pe;
+      q.y1 = sh.s[p] - pn;
+      q.y2 = sh.n[p] - pn;
+      q.z1 = sh.b[p] - pu;
+      q.z2 = sh.t[p] - pu;
+      if (check_singular && active) {
+#pragma unroll
+        for (int f = kGee; f <= kGnz; f++)
+          if ((sing_mask >> f) & 1u) singular |= singular_for(f, q);
+      }
+      if (sh.null[p]) continue;  // uniform across the CTA
+      const double rho = sh.rho[p];
+      if (F == kAll) {
+        double v[kNumFields];
+        pair_all<true>(q, T, v);
+#pragma unroll
+        for (int f = 0; f < kNumFields; f++) {
+          if (is_tensor(f) && singular_for(f, q)) v[f] = quiet_nan();
+          acc[f] = fma(rho, v[f], acc[f]);
+        }
+      } else {
+        double v = pair_field<(F < kNumFields ? F : 0), true>(q, T);
+        if (is_tensor(F) && singular_for(F, q)) v = quiet_nan();
+        acc[0] = fma(rho, v, acc[0]);
+      }
+    }
+  }
+}
+
+}  // namespace hg

@@ -1,0 +1,300 @@
+// Batched prism forward: many independent (points, prisms, field) problems of
+// very different sizes in ONE persistent launch.
+//
+// The host cuts every problem into work items (problem, point tile of
+// kThreads points, prism chunk) and sorts them by decreasing cost.  A
+// persistent grid of CTAs pulls items from a device counter (atomicAdd, no
+// waiting on other CTAs), so small and large problems share the GPU without
+// tail effects.  Each item writes its partial sums into its own slot of a
+// workspace and a second kernel adds each point's chunks in fixed order and
+// applies the units: results are bitwise independent of the schedule and of
+// the other problems in the batch.  hg_batch_run only issues a memset and two
+// launches on the caller's stream (no allocation, no host synchronisation),
+// so it can be captured in a CUDA graph and replayed.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/harmonica_gb300.h"
+#include "forward_core.cuh"
+
+namespace hg {
+
+int set_error(int code, const std::string& msg);
+int cuda_check(cudaError_t e, const char* what);
+
+struct ProblemDev {
+  const double* e;
+  const double* n;
+  const double* u;
+  int64_t n_obs;
+  const double* soa;
+  int64_t stride;
+  int64_t n_prisms;
+  int64_t chunk;        // prisms per work item
+  int64_t n_chunks;
+  int64_t part_offset;  // first partial (in doubles) of this problem in the workspace
+  double* out;
+  int32_t* flag;
+  int32_t field;
+  int32_t check_singular;
+};
+
+struct WorkItem {
+  int32_t problem;
+  int32_t tile;
+  int32_t chunk;
+  int32_t pad;
+};
+
+template <int F>
+__device__ __forceinline__ void run_item(const ProblemDev& P, const WorkItem& w, SmemTile& sh,
+                                         const Tables& T, double* __restrict__ part) {
+  const int64_t i = (int64_t)w.tile * kThreads + threadIdx.x;
+  const bool active = i < P.n_obs;
+  const double pe = active ? P.e[i] : 0.0;
+  const double pn = active ? P.n[i] : 0.0;
+  const double pu = active ? P.u[i] : 0.0;
+  const int64_t p0 = (int64_t)w.chunk * P.chunk;
+  const int64_t p1 = min(p0 + P.chunk, P.n_prisms);
+  double acc[1] = {0.0};
+  bool singular = false;
+  const bool check = P.check_singular && P.flag != nullptr;
+  accumulate<F>(ListSource{P.soa, P.stride}, p0, p1, pe, pn, pu, active, check, 1u << F, sh, T,
+                acc, singular);
+  if (singular) atomicOr(P.flag, 1);
+  if (active) part[P.part_offset + (int64_t)w.chunk * P.n_obs + i] = acc[0];
+}
+
+__global__ void __launch_bounds__(kThreads) batch_kernel(const ProblemDev* __restrict__ probs,
+                                                         const WorkItem* __restrict__ items,
+                                                         int64_t n_items,
+                                                         unsigned long long* __restrict__ counter,
+                                                         double* __restrict__ part) {
+  __shared__ SmemTile sh;
+  __shared__ SmemTables tabs;
+  __shared__ long long next;
+  const Tables T = tabs.stage();
+  for (;;) {
+    __syncthreads();  // everyone is done with `next` and the previous tile
+    if (threadIdx.x == 0) next = (long long)atomicAdd(counter, 1ull);
+    __syncthreads();
+    const long long it = next;
+    if (it >= n_items) break;
+    const WorkItem w = items[it];
+    const ProblemDev P = probs[w.problem];
+    switch (P.field) {  // uniform across the CTA
+      case kPotential: run_item<kPotential>(P, w, sh, T, part); break;
+      case kGe: run_item<kGe>(P, w, sh, T, part); break;
+      case kGn: run_item<kGn>(P, w, sh, T, part); break;
+      case kGz: run_item<kGz>(P, w, sh, T, part); break;
+      case kGee: run_item<kGee>(P, w, sh, T, part); break;
+      case kGnn: run_item<kGnn>(P, w, sh, T, part); break;
+      case kGzz: run_item<kGzz>(P, w, sh, T, part); break;
+      case kGen: run_item<kGen>(P, w, sh, T, part); break;
+      case kGez: run_item<kGez>(P, w, sh, T, part); break;
+      default: run_item<kGnz>(P, w, sh, T, part); break;
+    }
+  }
+}
+
+// out_p[i] = scale(field_p) * sum_c part_p[c][i], chunks in order.
+__global__ void batch_reduce_kernel(const ProblemDev* __restrict__ probs,
+                                    const double* __restrict__ part) {
+  const ProblemDev P = probs[blockIdx.y];
+  const double scale = field_scale(P.field);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < P.n_obs;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int64_t c = 0; c < P.n_chunks; c++) s += part[P.part_offset + c * P.n_obs + i];
+    P.out[i] = s * scale;
+  }
+}
+
+}  // namespace hg
+
+using namespace hg;
+
+struct hg_batch {
+  int64_t n_problems = 0;
+  int64_t n_items = 0;
+  int64_t n_ctas = 0;
+  int64_t partials = 0;  // doubles
+  double pairs = 0.0;
+  ProblemDev* d_probs = nullptr;
+  WorkItem* d_items = nullptr;
+  int device = 0;
+};
+
+namespace {
+
+constexpr size_t kCounterBytes = 256;  // counter, then the partials (256-byte aligned)
+
+int64_t round_up(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
+
+}  // namespace
+
+extern "C" {
+
+int hg_batch_create(const hg_problem* problems, int64_t n_problems, int64_t chunk_prisms,
+                    int32_t n_ctas, hg_batch** batch) {
+  if (!batch || n_problems < 0 || (n_problems > 0 && !problems))
+    return set_error(HG_ERR_INVALID, "bad arguments");
+  if (n_problems > 65535) return set_error(HG_ERR_INVALID, "at most 65535 problems per batch");
+  *batch = nullptr;
+  int device = 0;
+  int rc = cuda_check(cudaGetDevice(&device), "cudaGetDevice");
+  if (rc != HG_OK) return rc;
+  int sms = kSmCount;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  if (n_ctas <= 0) {
+    int per_sm = 0;
+    rc = cuda_check(
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel, kThreads, 0),
+        "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+    if (rc != HG_OK) return rc;
+    n_ctas = (int32_t)std::max(1, per_sm) * sms;
+  }
+  std::vector<ProblemDev> probs((size_t)n_problems);
+  int64_t total_pairs_all = 0;
+  for (int64_t p = 0; p < n_problems; p++) {
+    const hg_problem& q = problems[p];
+    if (q.n_obs < 0 || q.n_prisms < 0 || q.prism_stride < q.n_prisms || q.field < 0 ||
+        q.field >= kNumFields)
+      return set_error(HG_ERR_INVALID, "bad problem " + std::to_string(p));
+    if (q.n_obs > 0 && (!q.obs_e || !q.obs_n || !q.obs_u || !q.out))
+      return set_error(HG_ERR_INVALID, "null pointer in problem " + std::to_string(p));
+    if (q.n_prisms > 0 && !q.prisms_soa)
+      return set_error(HG_ERR_INVALID, "null prisms in problem " + std::to_string(p));
+    total_pairs_all += q.n_obs * q.n_prisms;
+  }
+  // Chunk size: enough items to keep every CTA busy ~16 times over, with
+  // chunks a multiple of the shared-memory tile.
+  int64_t chunk_default = kTile;
+  if (chunk_prisms <= 0) {
+    const double target_items = 16.0 * n_ctas;
+    const double pairs_per_item = std::max(1.0, (double)total_pairs_all / target_items);
+    chunk_default = round_up(std::max<int64_t>(kTile, (int64_t)(pairs_per_item / kThreads)), kTile);
+  }
+  std::vector<WorkItem> items;
+  std::vector<double> cost;
+  int64_t part = 0;
+  double pairs = 0.0;
+  for (int64_t p = 0; p < n_problems; p++) {
+    const hg_problem& q = problems[p];
+    ProblemDev& d = probs[(size_t)p];
+    d.e = q.obs_e;
+    d.n = q.obs_n;
+    d.u = q.obs_u;
+    d.n_obs = q.n_obs;
+    d.soa = q.prisms_soa;
+    d.stride = q.prism_stride;
+    d.n_prisms = q.n_prisms;
+    d.chunk = chunk_prisms > 0 ? round_up(chunk_prisms, kTile) : chunk_default;
+    d.n_chunks = q.n_prisms > 0 ? (q.n_prisms + d.chunk - 1) / d.chunk : 0;
+    d.part_offset = part;
+    d.out = q.out;
+    d.flag = q.singular_flag;
+    d.field = q.field;
+    d.check_singular = q.check_singular;
+    part += d.n_chunks * q.n_obs;
+    pairs += (double)q.n_obs * (double)q.n_prisms;
+    const int64_t tiles = (q.n_obs + kThreads - 1) / kThreads;
+    if (tiles > INT32_MAX || d.n_chunks > INT32_MAX || n_problems > INT32_MAX)
+      return set_error(HG_ERR_INVALID, "problem too large for the work list");
+    for (int64_t t = 0; t < tiles; t++)
+      for (int64_t c = 0; c < d.n_chunks; c++) {
+        items.push_back(WorkItem{(int32_t)p, (int32_t)t, (int32_t)c, 0});
+        const double np = (double)std::min(d.chunk, q.n_prisms - c * d.chunk);
+        cost.push_back(np);  // every item runs kThreads threads over np prisms
+      }
+  }
+  // longest items first (list scheduling), ties in creation order
+  std::vector<int64_t> order(items.size());
+  for (size_t k = 0; k < order.size(); k++) order[k] = (int64_t)k;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int64_t a, int64_t b) { return cost[(size_t)a] > cost[(size_t)b]; });
+  std::vector<WorkItem> sorted(items.size());
+  for (size_t k = 0; k < order.size(); k++) sorted[k] = items[(size_t)order[k]];
+
+  hg_batch* b = new hg_batch();
+  b->n_problems = n_problems;
+  b->n_items = (int64_t)sorted.size();
+  b->n_ctas = n_ctas;
+  b->partials = part;
+  b->pairs = pairs;
+  b->device = device;
+  if (n_problems > 0) {
+    rc = cuda_check(cudaMalloc(&b->d_probs, sizeof(ProblemDev) * probs.size()), "cudaMalloc");
+    if (rc == HG_OK)
+      rc = cuda_check(cudaMemcpy(b->d_probs, probs.data(), sizeof(ProblemDev) * probs.size(),
+                                 cudaMemcpyHostToDevice),
+                      "cudaMemcpy(problems)");
+  }
+  if (rc == HG_OK && !sorted.empty()) {
+    rc = cuda_check(cudaMalloc(&b->d_items, sizeof(WorkItem) * sorted.size()), "cudaMalloc");
+    if (rc == HG_OK)
+      rc = cuda_check(cudaMemcpy(b->d_items, sorted.data(), sizeof(WorkItem) * sorted.size(),
+                                 cudaMemcpyHostToDevice),
+                      "cudaMemcpy(items)");
+  }
+  if (rc != HG_OK) {
+    cudaFree(b->d_probs);
+    cudaFree(b->d_items);
+    delete b;
+    return rc;
+  }
+  *batch = b;
+  return HG_OK;
+}
+
+int hg_batch_workspace(const hg_batch* batch, size_t* bytes) {
+  if (!batch || !bytes) return set_error(HG_ERR_INVALID, "null pointer");
+  *bytes = kCounterBytes + sizeof(double) * (size_t)batch->partials;
+  return HG_OK;
+}
+
+int hg_batch_info(const hg_batch* batch, int64_t* n_items, int64_t* n_ctas, double* pairs) {
+  if (!batch) return set_error(HG_ERR_INVALID, "null batch");
+  if (n_items) *n_items = batch->n_items;
+  if (n_ctas) *n_ctas = batch->n_ctas;
+  if (pairs) *pairs = batch->pairs;
+  return HG_OK;
+}
+
+int hg_batch_run(const hg_batch* batch, void* workspace, size_t workspace_bytes, void* stream) {
+  if (!batch) return set_error(HG_ERR_INVALID, "null batch");
+  size_t need = 0;
+  hg_batch_workspace(batch, &need);
+  if (!workspace || workspace_bytes < need)
+    return set_error(HG_ERR_INVALID, "workspace missing or too small");
+  if (batch->n_problems == 0) return HG_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  unsigned long long* counter = static_cast<unsigned long long*>(workspace);
+  double* part = reinterpret_cast<double*>(static_cast<char*>(workspace) + kCounterBytes);
+  int rc = cuda_check(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st),
+                      "cudaMemsetAsync(counter)");
+  if (rc != HG_OK) return rc;
+  if (batch->n_items > 0) {
+    batch_kernel<<<(unsigned)batch->n_ctas, kThreads, 0, st>>>(batch->d_probs, batch->d_items,
+                                                              batch->n_items, counter, part);
+    rc = cuda_check(cudaGetLastError(), "batch_kernel launch");
+    if (rc != HG_OK) return rc;
+  }
+  dim3 grid(64, (unsigned)batch->n_problems);
+  batch_reduce_kernel<<<grid, 256, 0, st>>>(batch->d_probs, part);
+  return cuda_check(cudaGetLastError(), "batch_reduce_kernel launch");
+}
+
+int hg_batch_destroy(hg_batch* batch) {
+  if (!batch) return HG_OK;
+  cudaFree(batch->d_probs);
+  cudaFree(batch->d_items);
+  delete batch;
+  return HG_OK;
+}
+
+}  // extern "C"

@@ -17,13 +17,9 @@
 #include <string>
 
 #include "../../include/harmonica_gb300.h"
-#include "prism_math.cuh"
+#include "forward_core.cuh"
 
 namespace hg {
-
-constexpr int kThreads = 128;  // observation points per CTA
-constexpr int kTile = 128;     // prisms staged per shared-memory tile
-constexpr int kSmCount = 152;
 
 thread_local std::string g_last_error;
 
@@ -37,56 +33,6 @@ int cuda_check(cudaError_t e, const char* what) {
   return set_error(HG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-// ---------------------------------------------------------------------------
-// Prism sources: how a CTA stages prism p of the list into shared memory.
-struct ListSource {
-  const double* soa;  // 7 rows of stride
-  int64_t stride;
-  __device__ __forceinline__ void load(int64_t p, double& w, double& e, double& s, double& n,
-                                       double& b, double& t, double& rho, bool& null) const {
-    w = soa[p];
-    e = soa[stride + p];
-    s = soa[2 * stride + p];
-    n = soa[3 * stride + p];
-    b = soa[4 * stride + p];
-    t = soa[5 * stride + p];
-    rho = soa[6 * stride + p];
-    // gravity.py:475-480: zero volume or zero density
-    null = (w == e) || (s == n) || (b == t) || (rho == 0.0);
-  }
-};
-
-struct LayerSource {
-  const double* ce;
-  const double* cn;
-  const double* bottom;
-  const double* top;
-  const double* density;
-  int64_t n_east;
-  double threshold;
-  __device__ __forceinline__ void load(int64_t p, double& w, double& e, double& s, double& n,
-                                       double& b, double& t, double& rho, bool& null) const {
-    // half spacings from the first two centres, as layer.py:582-583
-    const double half_e = (ce[1] - ce[0]) / 2.0;
-    const double half_n = (cn[1] - cn[0]) / 2.0;
-    int64_t k = p / n_east, j = p - k * n_east;
-    w = ce[j] - half_e;
-    e = ce[j] + half_e;
-    s = cn[k] - half_n;
-    n = cn[k] + half_n;
-    b = bottom[p];
-    t = top[p];
-    rho = density[p];
-    // layer.py:596-607; zero-thickness prisms add exactly zero and are skipped too
-    null = (rho == 0.0) || isnan(rho) || (t - b < threshold) || isnan(t) || isnan(b) || (b == t);
-  }
-};
-
-template <int F> struct NumOut { static constexpr int value = 1; };
-template <> struct NumOut<kAll> { static constexpr int value = kNumFields; };
-
-__device__ __forceinline__ bool is_tensor(int f) { return f >= kGee && f <= kGnz; }
-
 // out_mask: for kAll, which of the ten fields are written (compact rows).
 template <int F, class Source>
 __global__ void __launch_bounds__(kThreads) forward_kernel(
@@ -95,23 +41,9 @@ __global__ void __launch_bounds__(kThreads) forward_kernel(
     double* __restrict__ dst, int64_t dst_chunk_stride, int scale_output, int check_singular,
     int32_t* __restrict__ flag) {
   constexpr int NF = NumOut<F>::value;
-  __shared__ double sh_w[kTile], sh_e[kTile], sh_s[kTile], sh_n[kTile], sh_b[kTile], sh_t[kTile],
-      sh_rho[kTile];
-  __shared__ int sh_null[kTile];
-  // constant tables of the FP64 elementary functions, staged once per CTA
-  __shared__ double sh_logc[lean::kLogTableSize], sh_logl[lean::kLogTableSize];
-  __shared__ double sh_th[lean::kArgTableSize], sh_cs[lean::kArgTableSize],
-      sh_sn[lean::kArgTableSize];
-  for (int t = threadIdx.x; t < lean::kLogTableSize; t += blockDim.x) {
-    sh_logc[t] = lean::kLogC[t];
-    sh_logl[t] = lean::kLogL[t];
-  }
-  for (int t = threadIdx.x; t < lean::kArgTableSize; t += blockDim.x) {
-    sh_th[t] = lean::kArgTh[t];
-    sh_cs[t] = lean::kArgCos[t];
-    sh_sn[t] = lean::kArgSin[t];
-  }
-  const Tables T{sh_logc, sh_logl, sh_th, sh_cs, sh_sn};
+  __shared__ SmemTile sh;
+  __shared__ SmemTables tabs;
+  const Tables T = tabs.stage();  // made visible by the first barrier in accumulate()
 
   const int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x;
   const bool active = i < n_obs;
@@ -123,60 +55,11 @@ __global__ void __launch_bounds__(kThreads) forward_kernel(
 #pragma unroll
   for (int f = 0; f < NF; f++) acc[f] = 0.0;
   bool singular_seen = false;
-
+  const uint32_t sing_mask = F == kAll ? out_mask : (1u << (F < kNumFields ? F : 0));
   const int64_t p0 = (int64_t)blockIdx.y * chunk;
   const int64_t p1 = min(p0 + chunk, n_prisms);
-  for (int64_t base = p0; base < p1; base += kTile) {
-    const int cnt = (int)min((int64_t)kTile, p1 - base);
-    __syncthreads();
-    if (threadIdx.x < cnt) {
-      double w, e, s, n, b, t, rho;
-      bool null;
-      src.load(base + threadIdx.x, w, e, s, n, b, t, rho, null);
-      sh_w[threadIdx.x] = w;
-      sh_e[threadIdx.x] = e;
-      sh_s[threadIdx.x] = s;
-      sh_n[threadIdx.x] = n;
-      sh_b[threadIdx.x] = b;
-      sh_t[threadIdx.x] = t;
-      sh_rho[threadIdx.x] = rho;
-      sh_null[threadIdx.x] = null;
-    }
-    __syncthreads();
-    for (int p = 0; p < cnt; p++) {
-      Rel q;
-      q.x1 = sh_w[p] - pe;
-      q.x2 = sh_e[p] - pe;
-      q.y1 = sh_s[p] - pn;
-      q.y2 = sh_n[p] - pn;
-      q.z1 = sh_b[p] - pu;
-      q.z2 = sh_t[p] - pu;
-      if (check_singular && active) {
-        if (F == kAll) {
-#pragma unroll
-          for (int f = kGee; f <= kGnz; f++)
-            if ((out_mask >> f) & 1u) singular_seen |= singular_for(f, q);
-        } else if (is_tensor(F)) {
-          singular_seen |= singular_for(F, q);
-        }
-      }
-      if (sh_null[p]) continue;  // uniform across the CTA
-      const double rho = sh_rho[p];
-      if (F == kAll) {
-        double v[kNumFields];
-        pair_all<true>(q, T, v);
-#pragma unroll
-        for (int f = 0; f < kNumFields; f++) {
-          if (is_tensor(f) && singular_for(f, q)) v[f] = quiet_nan();
-          acc[f] = fma(rho, v[f], acc[f]);
-        }
-      } else {
-        double v = pair_field<(F < kNumFields ? F : 0), true>(q, T);
-        if (is_tensor(F) && singular_for(F, q)) v = quiet_nan();
-        acc[0] = fma(rho, v, acc[0]);
-      }
-    }
-  }
+  accumulate<F>(src, p0, p1, pe, pn, pu, active, check_singular != 0, sing_mask, sh, T, acc,
+                singular_seen);
   if (singular_seen) atomicOr(flag, 1);
   if (!active) return;
   double* d = dst + (int64_t)blockIdx.y * dst_chunk_stride;

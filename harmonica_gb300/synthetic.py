@@ -72,3 +72,35 @@ def layer_to_prisms(layer):
          layer["bottom"].ravel(), layer["top"].ravel()]
     )
     return prisms, layer["density"].ravel()
+
+
+def batched_problems(n_problems=256, seed=4, scale=1.0):
+    """
+    The batched workload: ``n_problems`` independent problems with prism
+    counts log-uniform in [1e3, 2e5] and station counts log-uniform in
+    [1e3, 5e4] (both times ``scale``), random axis-aligned prisms with sides
+    U(50, 2000) m in a 50 km square, tops U(-5000, 1000) m and bottoms
+    top - U(50, 2000) m, densities U(-500, 500), stations uniform in the
+    prisms' bounding box at heights U(100, 3000) m; fields alternate g_z and
+    g_zz.  Returns a list of dicts (coordinates, prisms, density, field).
+    """
+    rng = np.random.default_rng(seed)
+    problems = []
+    for p in range(n_problems):
+        m = max(1, int(round(np.exp(rng.uniform(np.log(1e3), np.log(2e5))) * scale)))
+        n = max(1, int(round(np.exp(rng.uniform(np.log(1e3), np.log(5e4))) * scale)))
+        west = rng.uniform(0, 50e3, m)
+        south = rng.uniform(0, 50e3, m)
+        top = rng.uniform(-5000, 1000, m)
+        prisms = np.column_stack(
+            [west, west + rng.uniform(50, 2000, m), south, south + rng.uniform(50, 2000, m),
+             top - rng.uniform(50, 2000, m), top]
+        )
+        density = rng.uniform(-500, 500, m)
+        lo_e, hi_e = prisms[:, 0].min(), prisms[:, 1].max()
+        lo_n, hi_n = prisms[:, 2].min(), prisms[:, 3].max()
+        coordinates = (rng.uniform(lo_e, hi_e, n), rng.uniform(lo_n, hi_n, n),
+                       rng.uniform(100, 3000, n))
+        problems.append(dict(coordinates=coordinates, prisms=prisms, density=density,
+                             field="g_z" if p % 2 == 0 else "g_zz"))
+    return problems

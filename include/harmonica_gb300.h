@@ -105,6 +105,57 @@ int hg_layer_forward(const double *obs_e, const double *obs_n, const double *obs
                      const double *density, double thickness_threshold, uint32_t field_mask,
                      double *out, void *workspace, size_t workspace_bytes, void *stream);
 
+/*
+ * ---------------------------------------------------------------------------
+ * Batched forward: many independent problems (each its own points, prisms
+ * and ONE field) in one persistent launch.  Replaces a Python loop of
+ * harmonica prism_gravity calls (gravity.py:51-236), one per problem, with a
+ * single launch whose work items (problem, 128-point tile, prism chunk) are
+ * pulled from a device queue by a persistent grid; each point's chunks are
+ * added in fixed order, so every result is bitwise the same alone and in any
+ * batch.
+ */
+typedef struct hg_problem {
+  const double *obs_e;       /* n_obs (device) */
+  const double *obs_n;
+  const double *obs_u;
+  int64_t n_obs;
+  const double *prisms_soa;  /* 7 rows of prism_stride (hg_pack_prisms layout) */
+  int64_t prism_stride;
+  int64_t n_prisms;
+  int32_t field;             /* field code 0..9 */
+  int32_t check_singular;    /* 1: OR 1 into *singular_flag on a singular point */
+  double *out;               /* n_obs (device), harmonica units */
+  int32_t *singular_flag;    /* device int32 or NULL */
+} hg_problem;
+
+typedef struct hg_batch hg_batch; /* opaque plan */
+
+/*
+ * Build the work list of a batch (host work + two small device copies; the
+ * plan keeps device pointers of the problems, which must stay valid until
+ * hg_batch_destroy).  chunk_prisms <= 0 and n_ctas <= 0 choose automatically
+ * (about 16 work items per CTA; one CTA per free slot of every SM).
+ */
+int hg_batch_create(const hg_problem *problems, int64_t n_problems, int64_t chunk_prisms,
+                    int32_t n_ctas, hg_batch **batch);
+
+/* Bytes of device workspace hg_batch_run needs. */
+int hg_batch_workspace(const hg_batch *batch, size_t *bytes);
+
+/* Work items, persistent CTAs and prism-point pairs of the plan. */
+int hg_batch_info(const hg_batch *batch, int64_t *n_items, int64_t *n_ctas, double *pairs);
+
+/*
+ * Run the batch on `stream`: one memset and two launches, no allocation and
+ * no host synchronisation (capturable in a CUDA graph; replays recompute
+ * from the current contents of the problems' input buffers).
+ */
+int hg_batch_run(const hg_batch *batch, void *workspace, size_t workspace_bytes, void *stream);
+
+/* Free a plan (device work list included). */
+int hg_batch_destroy(hg_batch *batch);
+
 #ifdef __cplusplus
 }
 #endif
