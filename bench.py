@@ -59,7 +59,7 @@ def parse_args():
     p.add_argument("--cpu-sample-stations", type=int, default=32)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
-    p.add_argument("--workload", default="layer", choices=["layer", "batched"],
+    p.add_argument("--workload", default="layer", choices=["layer", "batched", "inversion"],
                    help="layer: the 1e6-prism layer (default); batched: 256 uneven "
                         "g_z/g_zz problems, one persistent graph-captured launch vs one "
                         "launch per problem")
@@ -316,6 +316,62 @@ def run_batched(args, rank, world, local):
     batch.close()
 
 
+def run_inversion(args, rank, world, local):
+    """Basement-inversion step: FP64 forward + adjoint (density, bottom) of a 200x200 layer."""
+    import torch
+
+    import harmonica_gb300 as hg
+    from harmonica_gb300 import _native, synthetic
+
+    _native.build()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    L = synthetic.basement_layer()
+    T = lambda a: torch.tensor(a, dtype=torch.float64, device=dev)  # noqa: E731
+    coords = tuple(T(c) for c in L["coordinates"])
+    ce, cn = T(L["easting"]), T(L["northing"])
+    with torch.no_grad():
+        true_gz = hg.layer_gravity_torch(coords, ce, cn, T(L["bottom"]), T(L["top"]),
+                                         T(L["density"]))
+    rng = np.random.default_rng(L["noise_seed"])
+    data = true_gz + T(rng.normal(0.0, 0.1, true_gz.numel()))
+    start = T(np.full_like(L["bottom"], -3000.0))
+
+    def step():
+        bottom = start.clone().requires_grad_(True)
+        rho = T(L["density"]).requires_grad_(True)
+        gz = hg.layer_gravity_torch(coords, ce, cn, bottom, T(L["top"]), rho)
+        loss = 0.5 * ((gz - data) ** 2).sum()
+        loss.backward()
+        return loss.detach(), bottom.grad, rho.grad
+
+    for _ in range(max(1, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record()
+    for _ in range(args.steps):
+        loss, gb, gr = step()
+    t1.record()
+    torch.cuda.synchronize()
+    step_s = t0.elapsed_time(t1) * 1e-3 / args.steps
+    pairs = coords[0].numel() * L["bottom"].size
+    if rank != 0:
+        return
+    print(json.dumps({
+        "metric": "basement inversion step (FP64 g_z forward + adjoint d/drho, d/dbottom)",
+        "value": pairs / step_s, "unit": "forward pairs/s", "ms_per_step": step_s * 1e3,
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "200x200 layer (500 m), tops 0, smooth bottoms N(-3000,800), "
+                               "contrast -400, 100x100 stations at 500 m",
+                   "pairs_per_forward": pairs, "loss": float(loss),
+                   "grad_bottom_norm": float(gb.norm()), "grad_density_norm": float(gr.norm())},
+        "gpu_launches": 4 * args.steps,
+    }))
+
+
 def main():
     args = parse_args()
     rank, world, local = dist_env()
@@ -324,6 +380,9 @@ def main():
         return
     if args.workload == "batched":
         run_batched(args, rank, world, local)
+        return
+    if args.workload == "inversion":
+        run_inversion(args, rank, world, local)
         return
 
     import torch

@@ -14,6 +14,7 @@ in ``include/harmonica_gb300.h``; :func:`build` compiles them in-tree.
 """
 
 from ._native import build
+from .adjoint import layer_gravity_torch, prism_gravity_torch
 from .batch import PrismBatch, autotune, prism_gravity_batch
 from .fields import FIELDS
 from .gravity import check_prisms, prism_gravity, prism_gravity_fields
@@ -28,6 +29,8 @@ __all__ = [
     "PrismLayer",
     "build",
     "check_prisms",
+    "layer_gravity_torch",
+    "prism_gravity_torch",
     "prism_gravity",
     "prism_gravity_fields",
     "prism_layer",

@@ -26,7 +26,7 @@ HEADERS = (
 )
 
 #: translation units compiled into the library
-SOURCES = ("prism_forward.cu", "prism_batch.cu", "bench_probe.cu")
+SOURCES = ("prism_forward.cu", "prism_batch.cu", "prism_adjoint.cu", "bench_probe.cu")
 
 ARCH_FLAGS = ("-gencode", "arch=compute_103a,code=sm_103a")
 
@@ -156,6 +156,26 @@ PROTOTYPES = {
         ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]
     ),
     "hg_batch_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "hg_prism_adjoint_workspace": (
+        ctypes.c_int, [ctypes.c_int64, ctypes.c_int64, ctypes.POINTER(ctypes.c_size_t)]
+    ),
+    "hg_prism_adjoint": (
+        ctypes.c_int,
+        [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+         ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p,
+         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p],
+    ),
+    "hg_layer_adjoint_workspace": (
+        ctypes.c_int,
+        [ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.POINTER(ctypes.c_size_t)],
+    ),
+    "hg_layer_adjoint": (
+        ctypes.c_int,
+        [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+         ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_int32, ctypes.c_void_p,
+         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p],
+    ),
     "hg_fp64_peak_probe": (
         ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_void_p]
     ),

@@ -469,4 +469,30 @@ HG_HD __forceinline__ double pair_field(const Rel& q, const Tables& T) {
   }
 }
 
+// g_z combination of one pair together with its two horizontal face angles
+// (the derivatives of the combination with respect to the bottom and top
+// coordinates: d/dz_bottom = O_bottom, d/dz_top = -O_top), for the adjoint.
+template <bool LEAN>
+HG_HD __forceinline__ double pair_gz_faces(const Rel& q, const Tables& T, double& o_bottom,
+                                           double& o_top) {
+  Geom g;
+  make_geom<LEAN>(q, g);
+  EdgeSet Ey, Ex;
+  edges_y(g, Ey);
+  edges_x(g, Ex);
+  o_bottom = face_z<LEAN>(g, 0, T);
+  o_top = face_z<LEAN>(g, 1, T);
+  double v = 0.0;
+#pragma unroll
+  for (int a = 0; a < 2; a++) {
+    const double s = a ? 1.0 : -1.0;
+    v += s * cmul(g.x[a], log_ratio2<LEAN>(Ey.num[a][1], Ey.den[a][1], Ey.num[a][0],
+                                           Ey.den[a][0], T));
+    v += s * cmul(g.y[a], log_ratio2<LEAN>(Ex.num[a][1], Ex.den[a][1], Ex.num[a][0],
+                                           Ex.den[a][0], T));
+  }
+  v -= cmul(g.z[1], o_top) - cmul(g.z[0], o_bottom);
+  return v;
+}
+
 }  // namespace hg

@@ -104,3 +104,33 @@ def batched_problems(n_problems=256, seed=4, scale=1.0):
         problems.append(dict(coordinates=coordinates, prisms=prisms, density=density,
                              field="g_z" if p % 2 == 0 else "g_zz"))
     return problems
+
+
+def basement_layer(n_side=200, spacing=500.0, seed=5, noise_seed=6, n_stations_side=100,
+                   height=500.0, contrast=-400.0):
+    """
+    The basement-inversion workload: an n_side x n_side layer of 500 m cells
+    (100 km square) with tops at 0 m and bottoms a smooth seeded surface
+    (Gaussian-filtered white noise rescaled to mean -3000 m, std 800 m), a
+    density contrast of -400 kg/m^3, and g_z data on an n x n station grid at
+    ``height`` computed elsewhere; returns the geometry and the true bottom.
+    """
+    rng = np.random.default_rng(seed)
+    noise = rng.normal(size=(n_side, n_side))
+    k = np.fft.fftfreq(n_side)
+    kx, ky = np.meshgrid(k, k)
+    sigma = 5.0  # cells
+    filt = np.exp(-2 * (np.pi * sigma) ** 2 * (kx ** 2 + ky ** 2))
+    smooth = np.real(np.fft.ifft2(np.fft.fft2(noise) * filt))
+    smooth = (smooth - smooth.mean()) / smooth.std()
+    bottom = -3000.0 + 800.0 * smooth
+    bottom = np.minimum(bottom, -10.0)  # keep bottom below the 0 m top
+    easting = np.arange(n_side) * spacing + spacing / 2
+    northing = np.arange(n_side) * spacing + spacing / 2
+    side = n_side * spacing
+    se, sn = np.meshgrid(np.linspace(0, side, n_stations_side),
+                         np.linspace(0, side, n_stations_side))
+    coordinates = (se.ravel(), sn.ravel(), np.full(se.size, height))
+    return dict(easting=easting, northing=northing, top=np.zeros_like(bottom), bottom=bottom,
+                density=np.full_like(bottom, contrast), coordinates=coordinates,
+                noise_seed=noise_seed)

@@ -156,6 +156,37 @@ int hg_batch_run(const hg_batch *batch, void *workspace, size_t workspace_bytes,
 /* Free a plan (device work list included). */
 int hg_batch_destroy(hg_batch *batch);
 
+/*
+ * ---------------------------------------------------------------------------
+ * Adjoint of the forward (new: the reference has no derivatives; it
+ * replaces assembling a gradient from repeated prism_gravity calls,
+ * gravity.py:51-236).  With weights w_i = dL/dd_i for the outputs d_i of
+ * field `field` (harmonica units):
+ *   grad_density[j] = sum_i w_i dd_i/drho_j                 (any field)
+ *   grad_bottom[j]  = sum_i w_i dd_i/dbottom_j              (g_z only)
+ *   grad_top[j]     = sum_i w_i dd_i/dtop_j                 (g_z only)
+ * Any of the three outputs may be NULL.  Null prisms (and, for the layer,
+ * the prisms its forward skips) get zero gradients.  The workspace
+ * (hg_*_adjoint_workspace bytes) is required.
+ */
+int hg_prism_adjoint_workspace(int64_t n_obs, int64_t n_prisms, size_t *bytes);
+
+int hg_prism_adjoint(const double *obs_e, const double *obs_n, const double *obs_u,
+                     const double *weights, int64_t n_obs, const double *prisms_soa,
+                     int64_t prism_stride, int64_t n_prisms, int32_t field, double *grad_density,
+                     double *grad_bottom, double *grad_top, void *workspace,
+                     size_t workspace_bytes, void *stream);
+
+int hg_layer_adjoint_workspace(int64_t n_obs, int64_t n_east, int64_t n_north, size_t *bytes);
+
+/* Layer version: gradients are (n_north, n_east) row-major like the layer grids. */
+int hg_layer_adjoint(const double *obs_e, const double *obs_n, const double *obs_u,
+                     const double *weights, int64_t n_obs, const double *centre_e, int64_t n_east,
+                     const double *centre_n, int64_t n_north, const double *bottom,
+                     const double *top, const double *density, double thickness_threshold,
+                     int32_t field, double *grad_density, double *grad_bottom, double *grad_top,
+                     void *workspace, size_t workspace_bytes, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
