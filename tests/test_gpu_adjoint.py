@@ -21,7 +21,10 @@ pytestmark = pytest.mark.gpu
 def small_basement():
     L = synthetic.basement_layer(n_side=24, spacing=500.0, n_stations_side=15)
     rng = np.random.default_rng(L["noise_seed"])
-    w = rng.normal(0.0, 0.1, L["coordinates"][0].size)  # dL/dd_i (a residual)
+    # dL/dd_i: positive weights, so that the weighted finite differences of
+    # single prisms below do not cancel (a signed residual makes the weighted
+    # sum ~100x smaller than its terms and the FD reference noisier than 1e-6)
+    w = rng.uniform(0.5, 1.5, L["coordinates"][0].size)
     return L, w
 
 
