@@ -179,6 +179,12 @@ PROTOTYPES = {
     "hg_fp64_peak_probe": (
         ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_void_p]
     ),
+    "hg_prism_forward_noalloc": (
+        ctypes.c_int,
+        [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+         ctypes.c_int64, ctypes.c_int64, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p,
+         ctypes.c_void_p],
+    ),
     "hg_layer_forward_workspace": (
         ctypes.c_int,
         [ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_uint32,

@@ -14,6 +14,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 
 #include "../../include/harmonica_gb300.h"
@@ -293,3 +294,86 @@ int hg_layer_forward(const double* obs_e, const double* obs_n, const double* obs
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Forward for callers that cannot allocate device memory.
+//
+// Who needs this: code running under a host framework that owns the device
+// memory pool and forbids foreign cudaMalloc calls; latency-critical loops
+// where an allocation (with its possible implicit synchronisation, or its
+// failure under memory pressure) is not acceptable in the middle of a step;
+// and plugins whose GPU memory budget is fixed when the process starts.
+// hg_prism_forward needs scratch space for per-chunk partial sums whenever
+// the observation points alone cannot fill the GPU, and such a caller can
+// neither hand it a workspace nor let it call cudaMallocAsync.
+// hg_prism_forward_noalloc runs the same kernels with that scratch taken from
+// a fixed array compiled into the library (kNoAllocScratchBytes = 8 MiB; every
+// GPU that loads the library holds it until the process exits).
+
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = size_t(8) << 20;
+constexpr int kNoAllocMaxDevices = 64;
+
+}  // namespace
+
+// The scratch array.  In host code its name is only a host-side stand-in, so
+// its device address is looked up once per device (see noalloc_scratch).
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratchBytes / sizeof(double)];
+
+namespace {
+
+std::mutex g_noalloc_mutex;
+double* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+// Device address of g_noalloc_scratch on the current device, looked up with
+// cudaGetSymbolAddress the first time each device is used.
+int noalloc_scratch(double** ptr) {
+  int dev = 0;
+  int rc = cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+  if (rc != HG_OK) return rc;
+  if (dev < 0 || dev >= kNoAllocMaxDevices)
+    return set_error(HG_ERR_INVALID, "hg_prism_forward_noalloc: device index out of range");
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (g_noalloc_ptr[dev] == nullptr) {
+    void* p = nullptr;
+    rc = cuda_check(cudaGetSymbolAddress(&p, g_noalloc_scratch),
+                    "cudaGetSymbolAddress(no-alloc scratch)");
+    if (rc != HG_OK) return rc;
+    g_noalloc_ptr[dev] = static_cast<double*>(p);
+  }
+  *ptr = g_noalloc_ptr[dev];
+  return HG_OK;
+}
+
+}  // namespace
+
+extern "C" int hg_prism_forward_noalloc(const double* obs_e, const double* obs_n,
+                                        const double* obs_u, int64_t n_obs,
+                                        const double* prisms_soa, int64_t prism_stride,
+                                        int64_t n_prisms, uint32_t field_mask, double* out,
+                                        int32_t* singular_flag, void* stream) {
+  if (n_obs < 0 || n_prisms < 0 || prism_stride < n_prisms || !valid_mask(field_mask))
+    return set_error(HG_ERR_INVALID, "bad sizes or field mask");
+  if (n_obs > 0 && (!obs_e || !obs_n || !obs_u || !out))
+    return set_error(HG_ERR_INVALID, "null pointer");
+  if (n_prisms > 0 && !prisms_soa) return set_error(HG_ERR_INVALID, "null prisms pointer");
+  const Plan plan = make_plan(n_obs, n_prisms, field_mask);
+  if (plan.workspace_bytes > kNoAllocScratchBytes)
+    return set_error(HG_ERR_INVALID,
+                     "hg_prism_forward_noalloc: this problem needs " +
+                         std::to_string(plan.workspace_bytes) +
+                         " bytes of scratch, more than the fixed " +
+                         std::to_string(kNoAllocScratchBytes) +
+                         " bytes; request fewer fields or use hg_prism_forward with a workspace");
+  double* scratch = nullptr;
+  if (plan.workspace_bytes > 0) {
+    const int rc = noalloc_scratch(&scratch);
+    if (rc != HG_OK) return rc;
+  }
+  // Every partial-sum slot the reduction reads is written by the forward
+  // launch first, so the scratch left by an earlier call needs no clearing.
+  ListSource src{prisms_soa, prism_stride};
+  return launch_forward(plan, obs_e, obs_n, obs_u, n_obs, src, n_prisms, field_mask, out,
+                        singular_flag, scratch, (cudaStream_t)stream, true);
+}

@@ -84,6 +84,31 @@ int hg_prism_forward(const double *obs_e, const double *obs_n, const double *obs
                      uint32_t field_mask, double *out, int32_t *singular_flag, void *workspace,
                      size_t workspace_bytes, void *stream);
 
+/*
+ * hg_prism_forward for callers that cannot allocate device memory (no
+ * counterpart in the reference: harmonica never touches device memory).
+ * Frameworks that own the device pool, latency-critical loops that must not
+ * allocate mid-step, and plugins with a fixed GPU memory budget can neither
+ * pass hg_prism_forward a workspace nor let it allocate one.  This entry point
+ * computes exactly what hg_prism_forward computes (same arguments minus the
+ * workspace) and calls no cudaMalloc/cudaFree: its scratch for partial sums
+ * is a fixed 8 MiB array in the library's device image, held by every GPU
+ * that loads the library until the process exits.
+ *   - Problems whose partial sums need more than 8 MiB are rejected with
+ *     HG_ERR_INVALID and a message giving the size (calls for up to three
+ *     fields always fit; many fields at once with few points may not).
+ *   - The first call on each device looks up the array's device address
+ *     (cudaGetSymbolAddress) with that device current; make that first call
+ *     before any stream capture.
+ *   - All calls on a device share the one array and it keeps the last call's
+ *     contents (nothing in it needs to start at zero).  Calls that overlap on
+ *     the GPU (e.g. on two streams at once) race on it: serialise them.
+ */
+int hg_prism_forward_noalloc(const double *obs_e, const double *obs_n, const double *obs_u,
+                             int64_t n_obs, const double *prisms_soa, int64_t prism_stride,
+                             int64_t n_prisms, uint32_t field_mask, double *out,
+                             int32_t *singular_flag, void *stream);
+
 /* Bytes of device workspace hg_layer_forward needs for this problem. */
 int hg_layer_forward_workspace(int64_t n_obs, int64_t n_east, int64_t n_north,
                                uint32_t field_mask, size_t *bytes);
