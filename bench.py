@@ -59,12 +59,15 @@ def parse_args():
     p.add_argument("--cpu-sample-stations", type=int, default=32)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
-    p.add_argument("--workload", default="layer", choices=["layer", "batched", "inversion"],
+    p.add_argument("--workload", default="layer", choices=["layer", "batched", "inversion", "serving"],
                    help="layer: the 1e6-prism layer (default); batched: 256 uneven "
                         "g_z/g_zz problems, one persistent graph-captured launch vs one "
                         "launch per problem")
     p.add_argument("--batch-problems", type=int, default=256)
     p.add_argument("--autotune", action="store_true")
+    p.add_argument("--arrival-seconds", type=float, default=5.0)
+    p.add_argument("--drain-seconds", type=float, default=30.0)
+    p.add_argument("--rate", type=float, default=200.0)
     return p.parse_args()
 
 
@@ -372,6 +375,85 @@ def run_inversion(args, rank, world, local):
     }))
 
 
+def run_serving(args, rank, world, local):
+    """Poisson stream of forward solves through the continuous-batching server."""
+    import torch
+
+    from harmonica_gb300 import _native
+    from harmonica_gb300.serve import PrismServer
+
+    _native.build()
+    torch.cuda.set_device(local)
+    rng = np.random.default_rng(7)
+
+    def model(m, seed):
+        r = np.random.default_rng(seed)
+        side = np.sqrt(m) * 200.0
+        west = r.uniform(0, side, m)
+        south = r.uniform(0, side, m)
+        top = r.uniform(-3000, 1000, m)
+        prisms = np.column_stack([west, west + 200.0, south, south + 200.0,
+                                  top - r.uniform(100, 5000, m), top])
+        return prisms, r.uniform(1800, 3100, m), side
+
+    # a pool of prism models (log-uniform 1e3..1e6 prisms); 30% of the
+    # requests use one of the first 8 as a resident layer
+    sizes = np.exp(rng.uniform(np.log(1e3), np.log(1e6), 24)).astype(int)
+    models = [model(int(m), 100 + k) for k, m in enumerate(sizes)]
+    srv = PrismServer(memory_budget=120e9, max_active=4096)
+    for k in range(8):
+        srv.register_layer(f"layer{k}", models[k][0], models[k][1])
+    fields = ("g_z", "potential", "g_zz")
+    # arrivals
+    t, arrivals = 0.0, []
+    while t < args.arrival_seconds:
+        t += rng.exponential(1.0 / args.rate)
+        n_st = int(np.exp(rng.uniform(np.log(1e3), np.log(2.5e5))))
+        resident = rng.uniform() < 0.3
+        k = int(rng.integers(0, 8)) if resident else int(rng.integers(8, len(models)))
+        arrivals.append((t, n_st, resident, k, fields[int(rng.integers(0, 3))],
+                         int(rng.integers(1 << 30))))
+    offered = sum(n * models[k][0].shape[0] for _, n, _, k, _, _ in arrivals)
+    futures = []
+    t0 = time.perf_counter()
+    for (ta, n_st, resident, k, field, seed) in arrivals:
+        delay = ta - (time.perf_counter() - t0)
+        if delay > 0:
+            time.sleep(delay)
+        side = models[k][2]
+        r = np.random.default_rng(seed)
+        coords = (r.uniform(0, side, n_st), r.uniform(0, side, n_st), r.uniform(100, 3000, n_st))
+        if resident:
+            f = srv.submit(coords, field, layer=f"layer{k}")
+        else:
+            f = srv.submit(coords, field, prisms=models[k][0], density=models[k][1])
+        futures.append((f, n_st * models[k][0].shape[0]))
+    deadline = t0 + args.arrival_seconds + args.drain_seconds
+    while time.perf_counter() < deadline and not all(f.done() for f, _ in futures):
+        time.sleep(0.05)
+    elapsed = time.perf_counter() - t0
+    st = srv.stats()
+    done_pairs = sum(p for f, p in futures if f.done() and f.exception() is None)
+    srv.close(drain=False, timeout=60)
+    if rank != 0:
+        return
+    print(json.dumps({
+        "metric": "served FP64 pairs/s and latency, Poisson stream of forward solves",
+        "value": done_pairs / elapsed, "unit": "pairs/s",
+        "n_gpus": world, "steps": 1, "warmup": 0, "higher_is_better": True, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": f"Poisson {args.rate}/s for {args.arrival_seconds} s, prisms "
+                               "log-U[1e3,1e6], stations log-U[1e3,2.5e5], fields "
+                               "g_z/potential/g_zz, 30% on 8 resident layers, 120 GB budget",
+                   "requests": len(arrivals), "offered_pairs": offered,
+                   "offered_pairs_per_s": offered / args.arrival_seconds,
+                   "measured_seconds": elapsed},
+        "served": {"completed": st["completed"], "pending": len(arrivals) - st["completed"],
+                   "p50_ms": st.get("p50_ms"), "p99_ms": st.get("p99_ms"),
+                   "mean_ms": st.get("mean_ms"), "rounds": st["rounds"]},
+    }))
+
+
 def main():
     args = parse_args()
     rank, world, local = dist_env()
@@ -383,6 +465,9 @@ def main():
         return
     if args.workload == "inversion":
         run_inversion(args, rank, world, local)
+        return
+    if args.workload == "serving":
+        run_serving(args, rank, world, local)
         return
 
     import torch

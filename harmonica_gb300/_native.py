@@ -105,6 +105,27 @@ def build(force=False, verbose=False):
 _c_double_p = ctypes.c_void_p  # device pointers travel as integers
 
 
+class HgProblemPlan(ctypes.Structure):
+    """ctypes mirror of ``hg_problem_plan`` (include/harmonica_gb300.h)."""
+
+    _fields_ = [
+        ("obs_e", ctypes.c_void_p),
+        ("obs_n", ctypes.c_void_p),
+        ("obs_u", ctypes.c_void_p),
+        ("n_obs", ctypes.c_int64),
+        ("prisms_soa", ctypes.c_void_p),
+        ("prism_stride", ctypes.c_int64),
+        ("n_prisms", ctypes.c_int64),
+        ("chunk", ctypes.c_int64),
+        ("n_chunks", ctypes.c_int64),
+        ("partials", ctypes.c_void_p),
+        ("out", ctypes.c_void_p),
+        ("singular_flag", ctypes.c_void_p),
+        ("field", ctypes.c_int32),
+        ("check_singular", ctypes.c_int32),
+    ]
+
+
 class HgProblem(ctypes.Structure):
     """ctypes mirror of ``hg_problem`` (include/harmonica_gb300.h)."""
 
@@ -175,6 +196,14 @@ PROTOTYPES = {
          ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_int32, ctypes.c_void_p,
          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p],
+    ),
+    "hg_round_run": (
+        ctypes.c_int,
+        [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p,
+         ctypes.c_void_p],
+    ),
+    "hg_round_reduce": (
+        ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]
     ),
     "hg_fp64_peak_probe": (
         ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_void_p]

@@ -298,3 +298,113 @@ int hg_batch_destroy(hg_batch* batch) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Rounds for continuous batching: explicit problem table and item list.
+namespace hg {
+namespace {
+
+template <int F>
+__device__ __forceinline__ void run_plan_item(const hg_problem_plan& P, const hg_work_item& w,
+                                              SmemTile& sh, const Tables& T) {
+  const int64_t i = (int64_t)w.tile * kThreads + threadIdx.x;
+  const bool active = i < P.n_obs;
+  const double pe = active ? P.obs_e[i] : 0.0;
+  const double pn = active ? P.obs_n[i] : 0.0;
+  const double pu = active ? P.obs_u[i] : 0.0;
+  const int64_t p0 = (int64_t)w.chunk * P.chunk;
+  const int64_t p1 = min(p0 + P.chunk, P.n_prisms);
+  double acc[1] = {0.0};
+  bool singular = false;
+  const bool check = P.check_singular && P.singular_flag != nullptr;
+  accumulate<F>(ListSource{P.prisms_soa, P.prism_stride}, p0, p1, pe, pn, pu, active, check,
+                1u << F, sh, T, acc, singular);
+  if (singular) atomicOr(P.singular_flag, 1);
+  if (active) P.partials[(int64_t)w.chunk * P.n_obs + i] = acc[0];
+}
+
+__global__ void __launch_bounds__(kThreads) round_kernel(const hg_problem_plan* __restrict__ probs,
+                                                         const hg_work_item* __restrict__ items,
+                                                         int64_t n_items,
+                                                         unsigned long long* __restrict__ counter) {
+  __shared__ SmemTile sh;
+  __shared__ SmemTables tabs;
+  __shared__ long long next;
+  const Tables T = tabs.stage();
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) next = (long long)atomicAdd(counter, 1ull);
+    __syncthreads();
+    const long long it = next;
+    if (it >= n_items) break;
+    const hg_work_item w = items[it];
+    const hg_problem_plan P = probs[w.problem];
+    switch (P.field) {  // uniform across the CTA
+      case kPotential: run_plan_item<kPotential>(P, w, sh, T); break;
+      case kGe: run_plan_item<kGe>(P, w, sh, T); break;
+      case kGn: run_plan_item<kGn>(P, w, sh, T); break;
+      case kGz: run_plan_item<kGz>(P, w, sh, T); break;
+      case kGee: run_plan_item<kGee>(P, w, sh, T); break;
+      case kGnn: run_plan_item<kGnn>(P, w, sh, T); break;
+      case kGzz: run_plan_item<kGzz>(P, w, sh, T); break;
+      case kGen: run_plan_item<kGen>(P, w, sh, T); break;
+      case kGez: run_plan_item<kGez>(P, w, sh, T); break;
+      default: run_plan_item<kGnz>(P, w, sh, T); break;
+    }
+  }
+}
+
+__global__ void round_reduce_kernel(const hg_problem_plan* __restrict__ probs,
+                                    const int32_t* __restrict__ ids) {
+  const hg_problem_plan P = probs[ids[blockIdx.y]];
+  const double scale = field_scale(P.field);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < P.n_obs;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int64_t c = 0; c < P.n_chunks; c++) s += P.partials[c * P.n_obs + i];
+    P.out[i] = s * scale;
+  }
+}
+
+}  // namespace
+}  // namespace hg
+
+extern "C" {
+
+int hg_round_run(const hg_problem_plan* problems, const hg_work_item* items, int64_t n_items,
+                 int32_t n_ctas, void* counter, void* stream) {
+  if (n_items < 0 || !counter || (n_items > 0 && (!problems || !items)))
+    return set_error(HG_ERR_INVALID, "bad arguments");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (n_items == 0) return HG_OK;
+  if (n_ctas <= 0) {
+    int device = 0, sms = kSmCount, per_sm = 0;
+    int rc = cuda_check(cudaGetDevice(&device), "cudaGetDevice");
+    if (rc != HG_OK) return rc;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    rc = cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, round_kernel,
+                                                                  kThreads, 0),
+                    "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+    if (rc != HG_OK) return rc;
+    n_ctas = (int32_t)std::max(1, per_sm) * sms;
+  }
+  int rc = cuda_check(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st),
+                      "cudaMemsetAsync(counter)");
+  if (rc != HG_OK) return rc;
+  const int64_t ctas = std::min<int64_t>(n_ctas, n_items);
+  round_kernel<<<(unsigned)ctas, kThreads, 0, st>>>(problems, items, n_items,
+                                                    static_cast<unsigned long long*>(counter));
+  return cuda_check(cudaGetLastError(), "round_kernel launch");
+}
+
+int hg_round_reduce(const hg_problem_plan* problems, const int32_t* problem_ids, int64_t n_ids,
+                    void* stream) {
+  if (n_ids < 0 || n_ids > 65535 || (n_ids > 0 && (!problems || !problem_ids)))
+    return set_error(HG_ERR_INVALID, "bad arguments (at most 65535 problems per reduce)");
+  if (n_ids == 0) return HG_OK;
+  dim3 grid(64, (unsigned)n_ids);
+  round_reduce_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(problems, problem_ids);
+  return cuda_check(cudaGetLastError(), "round_reduce_kernel launch");
+}
+
+}  // extern "C"

@@ -1,0 +1,441 @@
+"""
+Serving loop with continuous batching for prism forward solves on one GPU.
+
+Requests (observation points + a prism layer or prism list + one field)
+arrive at any time through :meth:`PrismServer.submit` and get a
+``concurrent.futures.Future``.  A scheduler thread:
+
+* **admits** queued requests in arrival order while their device memory
+  (points, output, partial sums, and the prisms unless they are a resident
+  layer) fits the memory budget, copying their inputs on a copy stream while
+  the GPU computes;
+* keeps **resident layers** (:meth:`register_layer`) on the device so repeated
+  requests against the same model skip the upload; idle layers are evicted
+  least-recently-used when memory is needed;
+* launches **rounds**: each round is one persistent launch (``hg_round_run``)
+  over work items (request, 128-point tile, prism chunk) taken from every
+  admitted request, shortest remaining work first, up to a per-round budget
+  of point-prism pairs, so requests that arrive while others are on the GPU
+  join the next round instead of waiting for the earlier ones to finish;
+* finishes requests with ``hg_round_reduce`` (each point's chunks added in
+  fixed order), copies results to pinned host memory and resolves the
+  futures, recording arrival-to-result latency.
+
+Work items of a request are cut with a chunk size that depends only on that
+request, and its chunks are reduced in fixed order, so a result is bitwise
+the same whether the request ran alone or mixed with others.
+
+This replaces calling ``harmonica.prism_gravity``
+(``src/harmonica/_forward/prisms/gravity.py:51-236``) once per request.
+"""
+
+import collections
+import ctypes
+import queue
+import threading
+import time
+from concurrent.futures import Future
+
+import numpy as np
+
+from . import _native
+from .fields import FIELD_CODES, TENSOR_FIELDS
+from .gravity import _prepare, pack_prisms
+
+KTHREADS = 128  # points per work item (the kernels' tile)
+
+
+def chunk_for(n_prisms, max_chunk=2048):
+    """Prism chunk of a request: a function of the request alone."""
+    return max(128, min(max_chunk, ((n_prisms + 127) // 128) * 128))
+
+
+class _Layer:
+    __slots__ = ("key", "soa", "n_prisms", "bytes", "users", "last_used")
+
+    def __init__(self, key, soa, n_prisms):
+        self.key = key
+        self.soa = soa
+        self.n_prisms = n_prisms
+        self.bytes = soa.numel() * 8
+        self.users = 0
+        self.last_used = time.perf_counter()
+
+
+class _Request:
+    def __init__(self, rid, coords, field, layer_key, prisms, density, check_singular):
+        self.id = rid
+        self.coords = coords
+        self.field = field
+        self.layer_key = layer_key
+        self.prisms = prisms
+        self.density = density
+        self.check_singular = check_singular
+        self.future = Future()
+        self.t_submit = time.perf_counter()
+        self.t_done = None
+        self.slot = -1
+        self.layer = None
+        self.tensors = []
+        self.bytes = 0
+        self.n_obs = coords[0].size
+        self.n_prisms = prisms.shape[0] if prisms is not None else None
+        self.next_item = 0
+        self.n_items = 0
+        self.chunk = 0
+        self.n_chunks = 0
+        self.pinned_out = None
+        self.shape = None
+
+
+class PrismServer:
+    """
+    Continuous-batching server for prism forward solves on one GPU.
+
+    Parameters
+    ----------
+    memory_budget : float
+        Device bytes the server may hold for admitted requests and resident
+        layers (admission stops when the next request would not fit).
+    round_pairs : float
+        Target point-prism pairs per round (a round is one persistent launch).
+    max_active : int
+        Size of the device problem table (admitted requests at once).
+    chunk : int
+        Largest prism chunk of a work item.
+    """
+
+    def __init__(self, device=None, memory_budget=120e9, round_pairs=4e8, max_active=1024,
+                 chunk=2048, n_ctas=0, rounds_in_flight=2):
+        import torch
+
+        from .gravity import _device
+
+        self.torch = torch
+        self.dev = _device(device)
+        self.lib = _native.lib()
+        self.budget = float(memory_budget)
+        self.used = 0.0
+        self.round_pairs = float(round_pairs)
+        self.max_active = int(max_active)
+        self.max_chunk = int(chunk)
+        self.n_ctas = int(n_ctas)
+        self.rounds_in_flight = int(rounds_in_flight)
+        self.layers = collections.OrderedDict()
+        self.inbox = queue.Queue()
+        self.pending = collections.deque()
+        self.active = {}
+        self.free_slots = list(range(self.max_active - 1, -1, -1))
+        self.in_flight = collections.deque()
+        self.completed = []
+        self.errors = []
+        self.rounds = 0
+        self.pairs_done = 0.0
+        self._ids = 0
+        self._lock = threading.Lock()
+        self._stop = threading.Event()
+        with torch.cuda.device(self.dev):
+            self.compute = torch.cuda.Stream(self.dev)
+            self.copy = torch.cuda.Stream(self.dev)
+            self.table_dev = torch.empty(self.max_active * ctypes.sizeof(_native.HgProblemPlan),
+                                         dtype=torch.uint8, device=self.dev)
+            self.counter = torch.zeros(1, dtype=torch.int64, device=self.dev)
+            self.flags = torch.zeros(self.max_active, dtype=torch.int32, device=self.dev)
+        self.table = (_native.HgProblemPlan * self.max_active)()
+        self._ring = [self._pinned_round_buffers() for _ in range(self.rounds_in_flight + 2)]
+        self._ring_next = 0
+        self.thread = threading.Thread(target=self._run, name="prism-server", daemon=True)
+        self.thread.start()
+
+    # ------------------------------------------------------------------ api
+    def register_layer(self, key, prisms, density):
+        """Keep a prism model resident (evictable when idle); returns its bytes."""
+        torch = self.torch
+        _, _, p_np, d_np = _prepare(([0.0], [0.0], [0.0]), prisms, density, False)
+        with torch.cuda.device(self.dev), torch.cuda.stream(self.copy):
+            pr = torch.from_numpy(np.ascontiguousarray(p_np)).to(self.dev, non_blocking=False)
+            rho = torch.from_numpy(np.ascontiguousarray(d_np)).to(self.dev, non_blocking=False)
+            soa = pack_prisms(pr, rho)
+            self.copy.synchronize()
+        layer = _Layer(key, soa, p_np.shape[0])
+        with self._lock:
+            self.layers[key] = layer
+            self.used += layer.bytes
+        return layer.bytes
+
+    def submit(self, coordinates, field, layer=None, prisms=None, density=None,
+               check_singular=False):
+        """Queue one forward solve; returns a Future of the result array."""
+        if field not in FIELD_CODES:
+            raise ValueError(f"Gravitational field {field} not recognized")
+        cast, coords, p_np, d_np = _prepare(
+            coordinates,
+            prisms if prisms is not None else np.zeros((0, 6)),
+            density if density is not None else np.zeros(0),
+            prisms is None,
+        )
+        if layer is None and prisms is None:
+            raise ValueError("submit needs a registered layer key or prisms and density")
+        with self._lock:
+            rid = self._ids
+            self._ids += 1
+        req = _Request(rid, coords, field, layer, p_np if layer is None else None,
+                       d_np if layer is None else None,
+                       check_singular and field in TENSOR_FIELDS)
+        req.shape = cast.shape
+        self.inbox.put(req)
+        return req.future
+
+    def close(self, drain=True, timeout=None):
+        """Stop the scheduler (after finishing queued work if ``drain``)."""
+        self._drain = drain
+        self._stop.set()
+        self.thread.join(timeout)
+
+    def stats(self):
+        lat = np.array([r.t_done - r.t_submit for r in self.completed])
+        out = {"completed": len(self.completed), "rounds": self.rounds,
+               "pairs_done": self.pairs_done, "errors": len(self.errors)}
+        if lat.size:
+            out.update(p50_ms=float(np.percentile(lat, 50) * 1e3),
+                       p99_ms=float(np.percentile(lat, 99) * 1e3),
+                       mean_ms=float(lat.mean() * 1e3))
+        return out
+
+    # ----------------------------------------------------------- internals
+    def _pinned_round_buffers(self):
+        torch = self.torch
+        return {
+            "table": torch.empty(self.max_active * ctypes.sizeof(_native.HgProblemPlan),
+                                 dtype=torch.uint8, pin_memory=True),
+            "items": torch.empty(0, dtype=torch.int32, pin_memory=True),
+            "ids": torch.empty(0, dtype=torch.int32, pin_memory=True),
+            "event": None,
+        }
+
+    def _request_bytes(self, req, layer):
+        chunk = chunk_for(layer.n_prisms if layer else req.n_prisms, self.max_chunk)
+        n_prisms = layer.n_prisms if layer else req.n_prisms
+        n_chunks = max(1, -(-n_prisms // chunk))
+        b = 8 * req.n_obs * (3 + 1 + n_chunks)
+        if layer is None:
+            b += 8 * 7 * max(req.n_prisms, 1) + 8 * 7 * max(req.n_prisms, 1)
+        return b, chunk, n_chunks
+
+    def _evict_for(self, need):
+        for key in list(self.layers):
+            if self.used + need <= self.budget:
+                return True
+            layer = self.layers[key]
+            if layer.users == 0:
+                del self.layers[key]
+                self.used -= layer.bytes
+        return self.used + need <= self.budget
+
+    def _admit(self):
+        with self._lock:
+            self._admit_locked()
+
+    def _admit_locked(self):
+        torch = self.torch
+        admitted = False
+        while self.pending and self.free_slots:
+            req = self.pending[0]
+            layer = None
+            if req.layer_key is not None:
+                layer = self.layers.get(req.layer_key)
+                if layer is None:
+                    self.pending.popleft()
+                    req.future.set_exception(KeyError(f"layer {req.layer_key!r} not registered"))
+                    continue
+            need, chunk, n_chunks = self._request_bytes(req, layer)
+            if need > self.budget:
+                self.pending.popleft()
+                req.future.set_exception(MemoryError(
+                    f"request needs {need} device bytes, above the server budget"))
+                continue
+            if self.used + need > self.budget and not self._evict_for(need):
+                break  # wait for memory to free up (arrival order is kept)
+            self.pending.popleft()
+            with torch.cuda.device(self.dev), torch.cuda.stream(self.copy):
+                e, n, u = (torch.from_numpy(c).pin_memory().to(self.dev, non_blocking=True)
+                           for c in req.coords)
+                if layer is None:
+                    pr = torch.from_numpy(np.ascontiguousarray(req.prisms)).to(self.dev)
+                    rho = torch.from_numpy(np.ascontiguousarray(req.density)).to(self.dev)
+                    soa = pack_prisms(pr, rho) if req.n_prisms else torch.zeros(
+                        (7, 1), dtype=torch.float64, device=self.dev)
+                    n_prisms = req.n_prisms
+                    req.tensors += [pr, rho]
+                else:
+                    soa = layer.soa
+                    n_prisms = layer.n_prisms
+                    layer.users += 1
+                    layer.last_used = time.perf_counter()
+                    self.layers.move_to_end(layer.key)
+                out = torch.empty(max(req.n_obs, 1), dtype=torch.float64, device=self.dev)
+                part = torch.empty(max(req.n_obs * n_chunks, 1), dtype=torch.float64,
+                                   device=self.dev)
+            req.tensors += [e, n, u, soa, out, part]
+            req.layer = layer
+            req.bytes = need
+            self.used += need
+            if n_prisms == 0 or req.n_obs == 0:
+                # nothing to sum: zeros (gravity.py:202 starts from np.zeros)
+                req.t_done = time.perf_counter()
+                if layer is not None:
+                    layer.users -= 1
+                self.used -= need
+                req.tensors = []
+                self.completed.append(req)
+                req.future.set_result(np.zeros(req.shape))
+                continue
+            req.chunk = chunk
+            req.n_chunks = -(-n_prisms // chunk) if n_prisms else 0
+            req.n_items = -(-req.n_obs // KTHREADS) * req.n_chunks
+            req.slot = self.free_slots.pop()
+            req.pinned_out = torch.empty(max(req.n_obs, 1), dtype=torch.float64, pin_memory=True)
+            p = self.table[req.slot]
+            p.obs_e, p.obs_n, p.obs_u = e.data_ptr(), n.data_ptr(), u.data_ptr()
+            p.n_obs = req.n_obs
+            p.prisms_soa = soa.data_ptr()
+            p.prism_stride = soa.shape[1]
+            p.n_prisms = n_prisms
+            p.chunk = chunk
+            p.n_chunks = req.n_chunks
+            p.partials = part.data_ptr()
+            p.out = out.data_ptr()
+            p.singular_flag = self.flags[req.slot:].data_ptr()
+            p.field = FIELD_CODES[req.field]
+            p.check_singular = int(req.check_singular)
+            self.active[req.id] = req
+            admitted = True
+        if admitted:
+            self._copy_event = self.torch.cuda.Event()
+            self._copy_event.record(self.copy)
+
+    def _plan_round(self):
+        """Items for the next round: shortest remaining work first."""
+        reqs = [r for r in self.active.values() if r.next_item < r.n_items]
+        if not reqs:
+            return None, []
+        reqs.sort(key=lambda r: (r.n_items - r.next_item) * r.chunk)
+        budget = self.round_pairs
+        parts, finishing = [], []
+        for r in reqs:
+            if budget <= 0:
+                break
+            per_item = KTHREADS * r.chunk
+            take = int(min(r.n_items - r.next_item, max(1, budget // per_item)))
+            k = np.arange(r.next_item, r.next_item + take, dtype=np.int64)
+            items = np.empty((take, 4), dtype=np.int32)
+            items[:, 0] = r.slot
+            items[:, 1] = k // r.n_chunks  # tile
+            items[:, 2] = k % r.n_chunks   # chunk
+            items[:, 3] = 0
+            parts.append(items)
+            r.next_item += take
+            budget -= take * per_item
+            if r.next_item == r.n_items:
+                finishing.append(r)
+        return np.concatenate(parts), finishing
+
+    def _launch_round(self, items, finishing):
+        torch = self.torch
+        buf = self._ring[self._ring_next]
+        self._ring_next = (self._ring_next + 1) % len(self._ring)
+        if buf["event"] is not None:
+            buf["event"].synchronize()  # the previous use of this buffer has been consumed
+        ctypes.memmove(buf["table"].data_ptr(), ctypes.addressof(self.table),
+                       ctypes.sizeof(self.table))
+        if buf["items"].numel() < items.size:
+            buf["items"] = torch.empty(items.size * 2, dtype=torch.int32, pin_memory=True)
+        buf["items"][: items.size].copy_(torch.from_numpy(items.ravel()))
+        ids = np.array([r.slot for r in finishing], dtype=np.int32)
+        if buf["ids"].numel() < ids.size:
+            buf["ids"] = torch.empty(max(ids.size * 2, 16), dtype=torch.int32, pin_memory=True)
+        if ids.size:
+            buf["ids"][: ids.size].copy_(torch.from_numpy(ids))
+        with torch.cuda.device(self.dev), torch.cuda.stream(self.compute):
+            if getattr(self, "_copy_event", None) is not None:
+                self.compute.wait_event(self._copy_event)
+            self.table_dev.copy_(buf["table"], non_blocking=True)
+            items_dev = buf["items"][: items.size].to(self.dev, non_blocking=True)
+            stream = self.compute.cuda_stream
+            _native.check(self.lib.hg_round_run(self.table_dev.data_ptr(), items_dev.data_ptr(),
+                                                items.shape[0], self.n_ctas,
+                                                self.counter.data_ptr(), stream))
+            if ids.size:
+                ids_dev = buf["ids"][: ids.size].to(self.dev, non_blocking=True)
+                _native.check(self.lib.hg_round_reduce(self.table_dev.data_ptr(),
+                                                       ids_dev.data_ptr(), ids.size, stream))
+                for r in finishing:
+                    out = r.tensors[-2]
+                    r.pinned_out[: r.n_obs].copy_(out[: r.n_obs], non_blocking=True)
+            ev = torch.cuda.Event()
+            ev.record(self.compute)
+        buf["event"] = ev
+        self.in_flight.append((ev, finishing, items, 0.0))
+        self.rounds += 1
+
+    def _retire(self, block=False):
+        while self.in_flight:
+            ev, finishing, items, _ = self.in_flight[0]
+            if not block and not ev.query():
+                return
+            ev.synchronize()
+            self.in_flight.popleft()
+            block = False
+            now = time.perf_counter()
+            flags = None
+            if any(r.check_singular for r in finishing):
+                with self.torch.cuda.stream(self.compute):
+                    flags = self.flags.cpu().numpy()
+            for r in finishing:
+                result = r.pinned_out[: r.n_obs].numpy().copy().reshape(r.shape)
+                r.t_done = now
+                self.pairs_done += float(r.n_obs) * float(
+                    r.layer.n_prisms if r.layer else r.n_prisms)
+                if flags is not None and flags[r.slot]:
+                    r.future.singular = True
+                with self._lock:
+                    self._release(r)
+                self.completed.append(r)
+                r.future.set_result(result)
+
+    def _release(self, r):
+        self.active.pop(r.id, None)
+        if r.layer is not None:
+            r.layer.users -= 1
+        self.used -= r.bytes
+        with self.torch.cuda.stream(self.compute):
+            self.flags[r.slot:r.slot + 1].zero_()
+        self.free_slots.append(r.slot)
+        r.tensors = []
+
+    def _run(self):
+        try:
+            while True:
+                idle = not self.pending and not self.active and not self.in_flight
+                if self._stop.is_set() and (idle or not getattr(self, "_drain", True)):
+                    break
+                try:
+                    req = self.inbox.get(timeout=0.002 if not idle else 0.05)
+                    self.pending.append(req)
+                    while True:
+                        self.pending.append(self.inbox.get_nowait())
+                except queue.Empty:
+                    pass
+                self._admit()
+                if len(self.in_flight) < self.rounds_in_flight:
+                    items, finishing = self._plan_round()
+                    if items is not None:
+                        self._launch_round(items, finishing)
+                        continue
+                self._retire(block=len(self.in_flight) >= self.rounds_in_flight)
+        except Exception as exc:  # noqa: BLE001 - fail every waiting request
+            self.errors.append(exc)
+            for r in list(self.active.values()) + list(self.pending):
+                if not r.future.done():
+                    r.future.set_exception(exc)
+            raise

@@ -183,6 +183,53 @@ int hg_batch_destroy(hg_batch *batch);
 
 /*
  * ---------------------------------------------------------------------------
+ * Rounds for continuous batching (a serving loop admits requests while
+ * earlier ones are on the GPU and launches a round of work items from many
+ * requests at a time).  The caller keeps, in device memory, a table of
+ * hg_problem_plan entries and, per round, a list of hg_work_item; every
+ * item (problem, 128-point tile, prism chunk) writes its partial sums to
+ * problem.partials[chunk * n_obs + point].  hg_round_reduce then adds the
+ * chunks of finished problems in fixed order into problem.out, so a result
+ * does not depend on which rounds or neighbours its items ran with.
+ */
+typedef struct hg_problem_plan {
+  const double *obs_e;       /* n_obs (device) */
+  const double *obs_n;
+  const double *obs_u;
+  int64_t n_obs;
+  const double *prisms_soa;  /* 7 rows of prism_stride */
+  int64_t prism_stride;
+  int64_t n_prisms;
+  int64_t chunk;             /* prisms per work item (multiple of 128) */
+  int64_t n_chunks;          /* ceil(n_prisms / chunk) */
+  double *partials;          /* n_chunks * n_obs doubles (device) */
+  double *out;               /* n_obs doubles (device), harmonica units */
+  int32_t *singular_flag;    /* device int32 or NULL */
+  int32_t field;             /* field code 0..9 */
+  int32_t check_singular;
+} hg_problem_plan;
+
+typedef struct hg_work_item {
+  int32_t problem;  /* index into the problem table */
+  int32_t tile;     /* 128-point tile */
+  int32_t chunk;    /* prism chunk */
+  int32_t pad;
+} hg_work_item;
+
+/*
+ * Run n_items items (device array) over the problem table (device array)
+ * with n_ctas persistent CTAs (<= 0: one per free slot of every SM).
+ * `counter` is 8 bytes of device memory the call zeroes and uses.
+ */
+int hg_round_run(const hg_problem_plan *problems, const hg_work_item *items, int64_t n_items,
+                 int32_t n_ctas, void *counter, void *stream);
+
+/* out = units * sum over chunks of partials, for the listed problems (device int32 ids). */
+int hg_round_reduce(const hg_problem_plan *problems, const int32_t *problem_ids, int64_t n_ids,
+                    void *stream);
+
+/*
+ * ---------------------------------------------------------------------------
  * Adjoint of the forward (new: the reference has no derivatives; it
  * replaces assembling a gradient from repeated prism_gravity calls,
  * gravity.py:51-236).  With weights w_i = dL/dd_i for the outputs d_i of
