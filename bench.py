@@ -59,6 +59,8 @@ def parse_args():
     p.add_argument("--cpu-sample-stations", type=int, default=32)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-all-fields", action="store_true")
+    p.add_argument("--all-fields-stations", type=int, default=1000)
     p.add_argument("--workload", default="layer", choices=["layer", "batched", "inversion", "serving"],
                    help="layer: the 1e6-prism layer (default); batched: 256 uneven "
                         "g_z/g_zz problems, one persistent graph-captured launch vs one "
@@ -585,6 +587,27 @@ def main():
         e2e = {"value": e2e_pairs / e2e_time, "unit": "pairs/s", "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": 8 * B}
 
+    # all ten fields fused on the same layer (one launch computes every field)
+    all_fields = None
+    if not args.no_all_fields:
+        nb = min(args.all_fields_stations, n_total)
+        lo = rank * nb % n_total
+        layer_forward_device(de[lo:lo + nb], dn[lo:lo + nb], du[lo:lo + nb], ce, cn, bt, tp, rho,
+                             0x3FF, 0.0)
+        torch.cuda.synchronize()
+        a0 = torch.cuda.Event(enable_timing=True)
+        a1 = torch.cuda.Event(enable_timing=True)
+        a0.record()
+        layer_forward_device(de[lo:lo + nb], dn[lo:lo + nb], du[lo:lo + nb], ce, cn, bt, tp, rho,
+                             0x3FF, 0.0)
+        a1.record()
+        torch.cuda.synchronize()
+        sec = a0.elapsed_time(a1) * 1e-3
+        all_fields = {"value": nb * n_prisms / sec, "unit": "pairs/s (all 10 fields per pair)",
+                      "field_values_per_s": 10 * nb * n_prisms / sec,
+                      "sample": f"{nb} stations x all 1e6 prisms, one fused launch",
+                      "ms": sec * 1e3}
+
     base = None
     if rank == 0 and not args.no_cpu_baseline:
         rate, dt, sample_pairs = cpu_baseline(layer, coords, args.cpu_sample_stations,
@@ -630,6 +653,7 @@ def main():
             "peak_source": "measured live: hg_fp64_peak_probe (FP64 FMA chains)",
         },
         "cpu_baseline": base,
+        "all_fields": all_fields,
         "e2e": e2e,
         "gpu_launches": launches_per_step * args.steps,
         "clocks": clocks,

@@ -231,7 +231,9 @@ HG_HD __forceinline__ double lm_log(double x, const Tables& T) {
 }
 
 // Argument of (pr + i pi) on the 2*pi branch nearest `est` (an FP32
-// estimate of the wanted angle, within ~1e-3 of it).
+// estimate of the wanted angle, within ~1e-3 of it).  The table rotation and
+// the quarter-turn assembly are skipped for small angles (the common case for
+// distant faces).
 HG_HD __forceinline__ double lm_arg_near(double pr, double pi, float est, const Tables& T) {
   const int q = round_to_int(est * 0.636619772f);  // quarter turns
   const float rem = fmaf((float)(-q), 1.57079637f, est);
@@ -241,10 +243,12 @@ HG_HD __forceinline__ double lm_arg_near(double pr, double pi, float est, const 
   const int qm = q & 3;
   const double r0 = qm == 0 ? pr : (qm == 1 ? pi : (qm == 2 ? -pr : -pi));
   const double i0 = qm == 0 ? pi : (qm == 1 ? -pr : (qm == 2 ? -pi : pr));
-  // rotate by -th_j
-  const double C = T.cs[j + kArgTableHalf], S = T.sn[j + kArgTableHalf];
-  const double re = fma(i0, S, r0 * C);
-  const double im = fma(-r0, S, i0 * C);
+  double re = r0, im = i0;
+  if (j != 0) {  // rotate by -th_j
+    const double C = T.cs[j + kArgTableHalf], S = T.sn[j + kArgTableHalf];
+    re = fma(i0, S, r0 * C);
+    im = fma(-r0, S, i0 * C);
+  }
   double delta;
   const double u = lm_div(im, re);
   const float uf = d2f_trunc(u);
@@ -256,8 +260,68 @@ HG_HD __forceinline__ double lm_arg_near(double pr, double pi, float est, const 
   } else {
     delta = atan2(im, re);  // estimate too far off: generic path
   }
+  if (q == 0) return j == 0 ? delta : T.th[j + kArgTableHalf] + delta;
   const double qd = int_to_double(q);
   return fma(qd, kPio2Hi, T.th[j + kArgTableHalf]) + fma(qd, kPio2Lo, delta);
+}
+
+// ln((p1 p2) / (q1 q2)) for positive normal arguments, without forming the
+// quotient: the FP32 estimate of the mantissa ratio selects the table entry
+// c_k ~ 1/g_k and the binary exponent E, then
+//   t = (p1 p2 c_k 2^-E - q1 q2) / (q1 q2)   (numerator by one FMA)
+// and ln = E ln2 - ln c_k + log1p(t).  When the quotient is within half a
+// table step of 1 (c_k = 1, E = 0) the numerator is the exact FMA
+// p1 p2 - q1 q2 and the table/exponent terms vanish: the log of a ratio near
+// 1 keeps its full relative accuracy.  ONE_FACTOR skips the products
+// (p2 = q2 = 1).  Other inputs take the generic path.
+template <bool ONE_FACTOR>
+HG_HD __forceinline__ double lm_log_quot(double p1, double p2, double q1, double q2,
+                                         const Tables& T) {
+  const long long b1 = d2ll(p1), b3 = d2ll(q1);
+  const long long b2 = ONE_FACTOR ? 0x3ff0000000000000LL : d2ll(p2);
+  const long long b4 = ONE_FACTOR ? 0x3ff0000000000000LL : d2ll(q2);
+  const int e1 = (int)((b1 >> 52) & 0x7ff), e2 = (int)((b2 >> 52) & 0x7ff);
+  const int e3 = (int)((b3 >> 52) & 0x7ff), e4 = (int)((b4 >> 52) & 0x7ff);
+  const double d = ONE_FACTOR ? q1 : q1 * q2;
+  const long long bd = d2ll(d);
+  const int ed = (int)((bd >> 52) & 0x7ff);
+  const bool ok = b1 > 0 && b2 > 0 && b3 > 0 && b4 > 0 && e1 != 0 && e2 != 0 && e3 != 0 &&
+                  e4 != 0 && e1 != 0x7ff && e2 != 0x7ff && e3 != 0x7ff && e4 != 0x7ff &&
+                  ed != 0 && ed < 0x7fe;
+  if (!ok) return log((ONE_FACTOR ? p1 : p1 * p2) / d);
+  const auto mant = [](long long b) { return u2f(0x3f800000u | (unsigned)((b >> 29) & 0x7fffff)); };
+  float rf = ONE_FACTOR ? mant(b1) * rcp_approx(mant(b3))
+                        : (mant(b1) * mant(b2)) * rcp_approx(mant(b3) * mant(b4));
+  int E = (e1 + e2) - (e3 + e4);
+#pragma unroll
+  for (int s = 0; s < 2; s++) {
+    if (rf >= 1.5f) { rf *= 0.5f; E += 1; }
+    if (rf < 0.75f) { rf *= 2.0f; E -= 1; }
+  }
+  int k = round_to_int((rf - 0.75f) * 256.0f);
+  k = k < 0 ? 0 : (k > kLogTableSize - 1 ? kLogTableSize - 1 : k);
+  const bool near1 = (E == 0) && (k == 64);
+  if (!near1 && (E > 1000 || E < -1000)) return log((ONE_FACTOR ? p1 : p1 * p2) / d);
+  // 1/d: FP32 seed and one Newton step (~2^-44; t is small, so ample)
+  double r = f2d_scaled(rcp_approx(mant(bd)), -(ed - 1023));
+  r = fma(r, fma(-d, r, 1.0), r);
+  double num;
+  if (near1) {
+    num = ONE_FACTOR ? p1 - d : fma(p1, p2, -d);
+  } else {
+    const double cp = ll2d(d2ll(T.logc[k]) - ((long long)E << 52));  // c_k 2^-E, exact
+    num = fma(ONE_FACTOR ? p1 : p1 * p2, cp, -d);
+  }
+  const double t = num * r;
+  const float tf = d2f_trunc(t);
+  const float r2 = fmaf(tf, fmaf(tf, fmaf(tf, -0.125f, 0.142857143f), -0.166666672f), 0.2f);
+  double a = fma(t, f2d_scaled(r2, 0), -0.25);
+  a = fma(t, a, 1.0 / 3.0);
+  a = fma(t, a, -0.5);
+  const double p = fma(t * t, a, t);  // log1p(t)
+  if (near1) return p;
+  const double edd = int_to_double(E);
+  return fma(edd, kLn2Hi, T.logl[k]) + fma(edd, kLn2Lo, p);
 }
 
 // FP32 angle of (re + i im) for doubles of any magnitude (joint scaling by a

@@ -139,6 +139,7 @@ HG_HD __forceinline__ bool singular_for(int f, const Rel& q) {
 struct Geom {
   double x[2], y[2], z[2];
   double x2[2], y2[2], z2[2];
+  double xz2[2][2];   // x_i^2 + z_k^2 (also the squared distance from y-edges)
   double r[2][2][2];  // r[i][j][k]
 };
 
@@ -156,11 +157,13 @@ HG_HD __forceinline__ void make_geom(const Rel& q, Geom& g) {
 #pragma unroll
   for (int i = 0; i < 2; i++)
 #pragma unroll
-    for (int j = 0; j < 2; j++) {
-      const double xy = g.x2[i] + g.y2[j];
+    for (int k = 0; k < 2; k++) g.xz2[i][k] = g.x2[i] + g.z2[k];
 #pragma unroll
-      for (int k = 0; k < 2; k++) g.r[i][j][k] = Math<LEAN>::sqrt_(xy + g.z2[k]);
-    }
+  for (int i = 0; i < 2; i++)
+#pragma unroll
+    for (int j = 0; j < 2; j++)
+#pragma unroll
+      for (int k = 0; k < 2; k++) g.r[i][j][k] = Math<LEAN>::sqrt_(g.xz2[i][k] + g.y2[j]);
 }
 
 // ---------------------------------------------------------------------------
@@ -221,7 +224,7 @@ HG_HD __forceinline__ void edges_y(const Geom& g, EdgeSet& E) {
   for (int i = 0; i < 2; i++)
 #pragma unroll
     for (int k = 0; k < 2; k++)
-      edge_ratio(c, g.y[0], g.y[1], g.r[i][0][k], g.r[i][1][k], g.x2[i] + g.z2[k], E.num[i][k],
+      edge_ratio(c, g.y[0], g.y[1], g.r[i][0][k], g.r[i][1][k], g.xz2[i][k], E.num[i][k],
                  E.den[i][k]);
 }
 // edges along z at (x_i, y_j)
@@ -239,11 +242,20 @@ HG_HD __forceinline__ void edges_z(const Geom& g, EdgeSet& E) {
 template <bool LEAN>
 HG_HD __forceinline__ double log_ratio2(double na, double da, double nb, double db,
                                         const Tables& T) {
-  return Math<LEAN>::log_(Math<LEAN>::div_(na * db, da * nb), T);
+  if (LEAN) return lean::lm_log_quot<false>(na, db, da, nb, T);
+  return log((na * db) / (da * nb));
 }
 template <bool LEAN>
 HG_HD __forceinline__ double log_ratio1(double n, double d, const Tables& T) {
-  return Math<LEAN>::log_(Math<LEAN>::div_(n, d), T);
+  if (LEAN) return lean::lm_log_quot<true>(n, 1.0, d, 1.0, T);
+  return log(n / d);
+}
+// ln((p1 p2) / (q1 q2))
+template <bool LEAN>
+HG_HD __forceinline__ double log_quot(double p1, double p2, double q1, double q2,
+                                      const Tables& T) {
+  if (LEAN) return lean::lm_log_quot<false>(p1, p2, q1, q2, T);
+  return log((p1 * p2) / (q1 * q2));
 }
 
 // ---------------------------------------------------------------------------
@@ -463,9 +475,8 @@ HG_HD __forceinline__ double pair_field(const Rel& q, const Tables& T) {
     if (F == kGen) edges_z(g, E);
     if (F == kGez) edges_y(g, E);
     if (F == kGnz) edges_x(g, E);
-    const double n = (E.num[1][1] * E.num[0][0]) * (E.den[0][1] * E.den[1][0]);
-    const double d = (E.den[1][1] * E.den[0][0]) * (E.num[0][1] * E.num[1][0]);
-    return log_ratio1<LEAN>(n, d, T);
+    return log_quot<LEAN>(E.num[1][1] * E.num[0][0], E.den[0][1] * E.den[1][0],
+                          E.den[1][1] * E.den[0][0], E.num[0][1] * E.num[1][0], T);
   }
 }
 
