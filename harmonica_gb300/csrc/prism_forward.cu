@@ -34,9 +34,18 @@ int cuda_check(cudaError_t e, const char* what) {
   return set_error(HG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
+// Resident CTAs per SM the register allocation must allow (FP64-pipe bound
+// code hides its latency with more warps; the fused all-field kernel needs
+// more registers).
+#ifndef HG_FWD_MIN_BLOCKS
+#define HG_FWD_MIN_BLOCKS 4
+#endif
+template <int F> struct MinBlocks { static constexpr int value = HG_FWD_MIN_BLOCKS; };
+template <> struct MinBlocks<kAll> { static constexpr int value = 3; };
+
 // out_mask: for kAll, which of the ten fields are written (compact rows).
 template <int F, class Source>
-__global__ void __launch_bounds__(kThreads) forward_kernel(
+__global__ void __launch_bounds__(kThreads, MinBlocks<F>::value) forward_kernel(
     const double* __restrict__ oe, const double* __restrict__ on, const double* __restrict__ ou,
     int64_t n_obs, Source src, int64_t n_prisms, int64_t chunk, uint32_t out_mask,
     double* __restrict__ dst, int64_t dst_chunk_stride, int scale_output, int check_singular,
