@@ -61,7 +61,7 @@ def parse_args():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-all-fields", action="store_true")
     p.add_argument("--all-fields-stations", type=int, default=1000)
-    p.add_argument("--workload", default="layer", choices=["layer", "batched", "inversion", "serving"],
+    p.add_argument("--workload", default="layer", choices=["layer", "batched", "inversion", "serving", "points"],
                    help="layer: the 1e6-prism layer (default); batched: 256 uneven "
                         "g_z/g_zz problems, one persistent graph-captured launch vs one "
                         "launch per problem")
@@ -456,6 +456,61 @@ def run_serving(args, rank, world, local):
     }))
 
 
+def run_points(args, rank, world, local):
+    """Point masses (Cartesian g_z): 1e6 masses under the 500 x 500 survey."""
+    import torch
+
+    from harmonica_gb300 import _native, synthetic
+    from harmonica_gb300.gravity import _ptr
+
+    _native.build()
+    lib = _native.lib()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    L = synthetic.layer_topography_1e6()
+    prisms, density = synthetic.layer_to_prisms(L)
+    # one point mass per prism, at its centre, with its mass
+    pe = 0.5 * (prisms[:, 0] + prisms[:, 1])
+    pn = 0.5 * (prisms[:, 2] + prisms[:, 3])
+    pu = 0.5 * (prisms[:, 4] + prisms[:, 5])
+    vol = (prisms[:, 1] - prisms[:, 0]) * (prisms[:, 3] - prisms[:, 2]) * (prisms[:, 5] - prisms[:, 4])
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).to(dev)  # noqa: E731
+    p = [T(pe), T(pn), T(pu), T(vol * density)]
+    c = [T(x) for x in L["coordinates"]]
+    B = 20000
+    out = torch.empty(B, dtype=torch.float64, device=dev)
+    ws = _native.ctypes.c_size_t(0)
+    _native.check(lib.hg_point_forward_workspace(B, pe.size, _native.ctypes.byref(ws)))
+    work = torch.empty(max(1, ws.value // 8), dtype=torch.float64, device=dev)
+
+    def step(s):
+        lo = (s * B) % (c[0].numel() - B)
+        _native.check(lib.hg_point_forward(
+            _ptr(c[0][lo:]), _ptr(c[1][lo:]), _ptr(c[2][lo:]), B, _ptr(p[0]), _ptr(p[1]),
+            _ptr(p[2]), _ptr(p[3]), pe.size, 0, 3, _ptr(out), _ptr(work), ws.value,
+            torch.cuda.current_stream().cuda_stream))
+
+    for s in range(args.warmup):
+        step(s)
+    torch.cuda.synchronize()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record()
+    for s in range(args.steps):
+        step(args.warmup + s)
+    b.record()
+    torch.cuda.synchronize()
+    sec = a.elapsed_time(b) * 1e-3 / args.steps
+    if rank == 0:
+        print(json.dumps({"metric": "FP64 g_z point-mass pairs/s (Cartesian)",
+                          "value": B * pe.size / sec, "unit": "pairs/s", "ms_per_step": sec * 1e3,
+                          "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                          "dtype": "f64", "data": "synthetic",
+                          "config": {"workload": "1e6 point masses (prism centres of the 1e6 "
+                                                 "layer), 20000 stations per step"},
+                          "gpu_launches": 2 * args.steps}))
+
+
 def main():
     args = parse_args()
     rank, world, local = dist_env()
@@ -470,6 +525,9 @@ def main():
         return
     if args.workload == "serving":
         run_serving(args, rank, world, local)
+        return
+    if args.workload == "points":
+        run_points(args, rank, world, local)
         return
 
     import torch

@@ -174,6 +174,22 @@ HG_HD __forceinline__ double lm_sqrt(double x) {
   return fma(r, h, s);
 }
 
+// 1 / sqrt(x): FP32 seed of the mantissa and two Newton steps
+// y <- y (1.5 - (x/2) y^2); other inputs take the generic path.
+HG_HD __forceinline__ double lm_rsqrt(double x) {
+  const long long b = d2ll(x);
+  const int ef = (int)((b >> 52) & 0x7ff);
+  if (b <= 0 || ef == 0 || ef == 0x7ff) return 1.0 / sqrt(x);
+  const int e = ef - 1023;
+  const int odd = e & 1;
+  const int k = (e - odd) / 2;
+  const float mf = u2f(((unsigned)(127 + odd) << 23) | (unsigned)((b >> 29) & 0x7fffff));
+  double y = f2d_scaled(rsqrt_approx(mf), -k);
+  const double hx = 0.5 * x;
+  y = y * fma(-hx, y * y, 1.5);
+  return y * fma(-hx, y * y, 1.5);
+}
+
 // n / d for d > 0 (other d fall back to the IEEE division).
 HG_HD __forceinline__ double lm_div(double n, double d) {
   const long long b = d2ll(d);

@@ -1,0 +1,206 @@
+// Point-mass gravity: all-pairs sum over observation points x point masses
+// (harmonica src/harmonica/_forward/point.py, point_mass_cartesian :357-398
+// and point_mass_spherical :400-450).  Same work decomposition as the prism
+// kernels: one thread per observation point, point masses staged in shared
+// memory, prism-chunk partials replaced by point-chunk partials reduced in
+// fixed order.  FP64, with the FP32-seeded reciprocal square root.
+//
+// Cartesian kernels (choclo.point, from V = G m / l): with d = P - Q,
+//   potential  G m / l;   g_a = -G m d_a / l^3;
+//   g_ab = G m (3 d_a d_b - delta_ab l^2) / l^5.
+// Spherical (longitude, latitude in degrees, radius): potential G m / l and
+// the upward component -G m (r - r_p cos psi) / l^3 with
+//   cos psi = sin phi_p sin phi + cos phi_p cos phi cos(lambda_p - lambda),
+//   l = sqrt((r - r_p)^2 + 2 r r_p (1 - cos psi))      (utils.py:164-201).
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "../../include/harmonica_gb300.h"
+#include "forward_core.cuh"
+
+namespace hg {
+
+int set_error(int code, const std::string& msg);
+int cuda_check(cudaError_t e, const char* what);
+
+namespace {
+
+struct PointTile {
+  double a[kTile], b[kTile], c[kTile], d[kTile], m[kTile];
+};
+
+constexpr double kDeg = 3.141592653589793 / 180.0;
+
+template <int F>
+__device__ __forceinline__ double point_cart(double dx, double dy, double dz) {
+  const double l2 = fma(dx, dx, fma(dy, dy, dz * dz));
+  const double inv = lean::lm_rsqrt(l2);
+  if (F == kPotential) return inv;
+  const double inv3 = (inv * inv) * inv;
+  if (F == kGe) return -dx * inv3;
+  if (F == kGn) return -dy * inv3;
+  if (F == kGz) return -dz * inv3;
+  const double inv5 = inv3 * (inv * inv);
+  if (F == kGee) return fma(3.0 * dx, dx, -l2) * inv5;
+  if (F == kGnn) return fma(3.0 * dy, dy, -l2) * inv5;
+  if (F == kGzz) return fma(3.0 * dz, dz, -l2) * inv5;
+  if (F == kGen) return 3.0 * dx * dy * inv5;
+  if (F == kGez) return 3.0 * dx * dz * inv5;
+  return 3.0 * dy * dz * inv5;  // kGnz
+}
+
+// SPH: 0 Cartesian (coordinates e, n, u), 1 spherical (lon, lat, r in degrees/m)
+template <int F, int SPH>
+__global__ void __launch_bounds__(kThreads) point_kernel(
+    const double* __restrict__ c1, const double* __restrict__ c2, const double* __restrict__ c3,
+    int64_t n_obs, const double* __restrict__ p1, const double* __restrict__ p2,
+    const double* __restrict__ p3, const double* __restrict__ mass, int64_t n_points,
+    int64_t chunk, double* __restrict__ dst, int64_t dst_chunk_stride, int scale_output) {
+  __shared__ PointTile sh;
+  const int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x;
+  const bool active = i < n_obs;
+  double x1 = active ? c1[i] : 0.0, x2 = active ? c2[i] : 0.0, x3 = active ? c3[i] : 1.0;
+  double cphi = 0.0, sphi = 0.0;
+  if (SPH) {
+    x1 *= kDeg;
+    sincos(x2 * kDeg, &sphi, &cphi);
+  }
+  double acc = 0.0;
+  const int64_t q0 = (int64_t)blockIdx.y * chunk;
+  const int64_t q1 = min(q0 + chunk, n_points);
+  for (int64_t base = q0; base < q1; base += kTile) {
+    const int cnt = (int)min((int64_t)kTile, q1 - base);
+    __syncthreads();
+    if ((int)threadIdx.x < cnt) {
+      const int64_t j = base + threadIdx.x;
+      if (SPH) {
+        double sp, cp;
+        sincos(p2[j] * kDeg, &sp, &cp);
+        sh.a[threadIdx.x] = p1[j] * kDeg;
+        sh.b[threadIdx.x] = cp;
+        sh.c[threadIdx.x] = sp;
+        sh.d[threadIdx.x] = p3[j];
+      } else {
+        sh.a[threadIdx.x] = p1[j];
+        sh.b[threadIdx.x] = p2[j];
+        sh.c[threadIdx.x] = p3[j];
+      }
+      sh.m[threadIdx.x] = mass[j];
+    }
+    __syncthreads();
+    for (int k = 0; k < cnt; k++) {
+      double v;
+      if (SPH) {
+        const double coslambda = cos(sh.a[k] - x1);
+        const double cospsi = sh.c[k] * sphi + sh.b[k] * cphi * coslambda;
+        const double rp = sh.d[k];
+        const double dr = x3 - rp;
+        const double l2 = dr * dr + 2.0 * x3 * rp * (1.0 - cospsi);
+        const double inv = lean::lm_rsqrt(l2);
+        v = F == kPotential ? inv : -(x3 - rp * cospsi) * ((inv * inv) * inv);
+      } else {
+        v = point_cart<F>(x1 - sh.a[k], x2 - sh.b[k], x3 - sh.c[k]);
+      }
+      acc = fma(sh.m[k], v, acc);
+    }
+  }
+  if (!active) return;
+  dst[(int64_t)blockIdx.y * dst_chunk_stride + i] = scale_output ? acc * field_scale(F) : acc;
+}
+
+__global__ void point_reduce_kernel(const double* __restrict__ part, int64_t n_chunks,
+                                    int64_t n_obs, double scale, double* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_obs) return;
+  double s = 0.0;
+  for (int64_t c = 0; c < n_chunks; c++) s += part[c * n_obs + i];
+  out[i] = s * scale;
+}
+
+struct PointPlan {
+  int64_t tiles, n_chunks, chunk;
+  size_t bytes;
+};
+
+PointPlan point_plan(int64_t n_obs, int64_t n_points) {
+  PointPlan p;
+  p.tiles = (n_obs + kThreads - 1) / kThreads;
+  const int64_t target = (int64_t)kSmCount * 8;
+  int64_t pt = (n_points + kTile - 1) / kTile;
+  if (pt < 1) pt = 1;
+  int64_t want = (target + (p.tiles > 0 ? p.tiles : 1) - 1) / (p.tiles > 0 ? p.tiles : 1);
+  want = want < 1 ? 1 : (want > pt ? pt : want);
+  if (want > 65535) want = 65535;
+  p.chunk = ((pt + want - 1) / want) * kTile;
+  p.n_chunks = n_points > 0 ? (n_points + p.chunk - 1) / p.chunk : 1;
+  p.bytes = p.n_chunks > 1 ? (size_t)p.n_chunks * (size_t)n_obs * sizeof(double) : 0;
+  return p;
+}
+
+template <int SPH>
+int launch_point(int field, const double* c1, const double* c2, const double* c3, int64_t n_obs,
+                 const double* p1, const double* p2, const double* p3, const double* m,
+                 int64_t n_points, double* out, void* ws, size_t ws_bytes, cudaStream_t st) {
+  const PointPlan plan = point_plan(n_obs, n_points);
+  if (n_obs == 0) return HG_OK;
+  if (n_points == 0)
+    return cuda_check(cudaMemsetAsync(out, 0, sizeof(double) * n_obs, st), "cudaMemsetAsync");
+  const bool direct = plan.n_chunks == 1;
+  if (!direct && (!ws || ws_bytes < plan.bytes))
+    return set_error(HG_ERR_INVALID, "workspace missing or too small");
+  double* dst = direct ? out : static_cast<double*>(ws);
+  dim3 grid((unsigned)plan.tiles, (unsigned)plan.n_chunks);
+  switch (field) {
+#define HG_PT(FF)                                                                              \
+  case FF:                                                                                     \
+    point_kernel<FF, SPH><<<grid, kThreads, 0, st>>>(c1, c2, c3, n_obs, p1, p2, p3, m,        \
+                                                      n_points, plan.chunk, dst, n_obs,        \
+                                                      direct ? 1 : 0);                         \
+    break;
+    HG_PT(0) HG_PT(1) HG_PT(2) HG_PT(3) HG_PT(4) HG_PT(5) HG_PT(6) HG_PT(7) HG_PT(8) HG_PT(9)
+#undef HG_PT
+    default: return set_error(HG_ERR_INVALID, "bad field");
+  }
+  int rc = cuda_check(cudaGetLastError(), "point_kernel launch");
+  if (rc != HG_OK || direct) return rc;
+  point_reduce_kernel<<<(unsigned)((n_obs + 255) / 256), 256, 0, st>>>(
+      dst, plan.n_chunks, n_obs, field_scale(field), out);
+  return cuda_check(cudaGetLastError(), "point_reduce_kernel launch");
+}
+
+}  // namespace
+}  // namespace hg
+
+using namespace hg;
+
+extern "C" {
+
+int hg_point_forward_workspace(int64_t n_obs, int64_t n_points, size_t* bytes) {
+  if (!bytes || n_obs < 0 || n_points < 0) return set_error(HG_ERR_INVALID, "bad arguments");
+  *bytes = point_plan(n_obs, n_points).bytes;
+  return HG_OK;
+}
+
+int hg_point_forward(const double* obs_1, const double* obs_2, const double* obs_3,
+                     int64_t n_obs, const double* pts_1, const double* pts_2,
+                     const double* pts_3, const double* masses, int64_t n_points,
+                     int32_t spherical, int32_t field, double* out, void* workspace,
+                     size_t workspace_bytes, void* stream) {
+  if (n_obs < 0 || n_points < 0 || field < 0 || field >= kNumFields)
+    return set_error(HG_ERR_INVALID, "bad sizes or field");
+  if (spherical && field != kPotential && field != kGz)
+    return set_error(HG_ERR_INVALID, "spherical point masses: potential and g_z only");
+  if (n_obs > 0 && (!obs_1 || !obs_2 || !obs_3 || !out))
+    return set_error(HG_ERR_INVALID, "null pointer");
+  if (n_points > 0 && (!pts_1 || !pts_2 || !pts_3 || !masses))
+    return set_error(HG_ERR_INVALID, "null points pointer");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (spherical)
+    return launch_point<1>(field, obs_1, obs_2, obs_3, n_obs, pts_1, pts_2, pts_3, masses,
+                           n_points, out, workspace, workspace_bytes, st);
+  return launch_point<0>(field, obs_1, obs_2, obs_3, n_obs, pts_1, pts_2, pts_3, masses,
+                         n_points, out, workspace, workspace_bytes, st);
+}
+
+}  // extern "C"

@@ -259,6 +259,22 @@ int hg_layer_adjoint(const double *obs_e, const double *obs_n, const double *obs
                      int32_t field, double *grad_density, double *grad_bottom, double *grad_top,
                      void *workspace, size_t workspace_bytes, void *stream);
 
+/*
+ * ---------------------------------------------------------------------------
+ * Point masses.  Replaces the loops point_mass_cartesian / point_mass_spherical
+ * (src/harmonica/_forward/point.py:357-450) behind point_gravity (:30-268).
+ * spherical = 0: obs/pts are easting, northing, upward (m), any field code;
+ * spherical = 1: longitude, latitude (degrees), radius (m), potential or g_z.
+ * masses in kg; out in harmonica units (g_z downward, mGal, Eotvos).
+ */
+int hg_point_forward_workspace(int64_t n_obs, int64_t n_points, size_t *bytes);
+
+int hg_point_forward(const double *obs_1, const double *obs_2, const double *obs_3,
+                     int64_t n_obs, const double *pts_1, const double *pts_2,
+                     const double *pts_3, const double *masses, int64_t n_points,
+                     int32_t spherical, int32_t field, double *out, void *workspace,
+                     size_t workspace_bytes, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -245,3 +245,68 @@ int oracle_any_singular(int field, int64_t n_obs, const double *easting, const d
                 return 1;
     return 0;
 }
+
+/* ------------------------------------------------------------------------
+ * Point masses (harmonica src/harmonica/_forward/point.py:357-450): the
+ * all-pairs loops of point_mass_cartesian and point_mass_spherical with the
+ * kernels written from the formulas of the point_gravity docstring
+ * (point.py:125-224): V = G m / l, g = grad V, tensor = grad grad V
+ * (choclo.point kernels, SI, upward z; sign/units applied by the caller).
+ * Field codes as for prisms.  Spherical: coordinates are longitude (deg),
+ * latitude (deg), radius (m); fields 0 (potential) and 3 (g_z) only, the
+ * distance is point.py's distance_spherical_core (utils.py:164-201).
+ */
+static double point_kernel_cart(int field, double e, double n, double u, double ep, double np,
+                                double up)
+{
+    double dx = e - ep, dy = n - np, dz = u - up;
+    double l = sqrt(dx * dx + dy * dy + dz * dz);
+    double l3 = l * l * l, l5 = l3 * l * l;
+    switch (field) {
+    case 0: return ORACLE_G / l;
+    case 1: return -ORACLE_G * dx / l3;
+    case 2: return -ORACLE_G * dy / l3;
+    case 3: return -ORACLE_G * dz / l3;
+    case 4: return ORACLE_G * (3.0 * dx * dx - l * l) / l5;
+    case 5: return ORACLE_G * (3.0 * dy * dy - l * l) / l5;
+    case 6: return ORACLE_G * (3.0 * dz * dz - l * l) / l5;
+    case 7: return ORACLE_G * 3.0 * dx * dy / l5;
+    case 8: return ORACLE_G * 3.0 * dx * dz / l5;
+    case 9: return ORACLE_G * 3.0 * dy * dz / l5;
+    default: return NAN;
+    }
+}
+
+void oracle_point_gravity(int field, int spherical, int64_t n_obs, const double *c1,
+                          const double *c2, const double *c3, int64_t n_points, const double *p1,
+                          const double *p2, const double *p3, const double *masses, double *out,
+                          int n_threads)
+{
+    const double deg = 3.141592653589793 / 180.0;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 16) num_threads(n_threads > 0 ? n_threads : 1)
+#endif
+    for (int64_t i = 0; i < n_obs; i++) {
+        double acc = out[i];
+        if (!spherical) {
+            for (int64_t j = 0; j < n_points; j++)
+                acc += masses[j] * point_kernel_cart(field, c1[i], c2[i], c3[i], p1[j], p2[j],
+                                                     p3[j]);
+        } else {
+            double lon = c1[i] * deg, lat = c2[i] * deg, r = c3[i];
+            double cphi = cos(lat), sphi = sin(lat);
+            for (int64_t j = 0; j < n_points; j++) {
+                double lonp = p1[j] * deg, latp = p2[j] * deg, rp = p3[j];
+                double cphip = cos(latp), sphip = sin(latp);
+                double coslambda = cos(lonp - lon);
+                double cospsi = sphip * sphi + cphip * cphi * coslambda;
+                double dist = sqrt((r - rp) * (r - rp) + 2.0 * r * rp * (1.0 - cospsi));
+                double k = field == 0 ? ORACLE_G / dist
+                                      : -ORACLE_G * (r - rp * cospsi) / (dist * dist * dist);
+                acc += masses[j] * k;
+            }
+        }
+        out[i] = acc;
+    }
+    (void)n_threads;
+}

@@ -78,6 +78,10 @@ def _load():
     ]
     lib.oracle_any_singular.restype = ctypes.c_int
     lib.oracle_any_singular.argtypes = [ctypes.c_int, i64, dp, dp, dp, i64, dp]
+    lib.oracle_point_gravity.restype = None
+    lib.oracle_point_gravity.argtypes = [
+        ctypes.c_int, ctypes.c_int, i64, dp, dp, dp, i64, dp, dp, dp, dp, dp, ctypes.c_int
+    ]
     lib.oracle_is_singular.restype = ctypes.c_int
     lib.oracle_is_singular.argtypes = [
         ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, dp
@@ -247,3 +251,49 @@ def layer_gravity(
     )
     scale_result(out, field)
     return out.reshape(cast.shape)
+
+
+POINT_FIELDS = {
+    "cartesian": {"potential": 0, "g_e": 1, "g_n": 2, "g_z": 3, "g_ee": 4, "g_nn": 5, "g_zz": 6,
+                  "g_en": 7, "g_ez": 8, "g_nz": 9, "g_ne": 7, "g_ze": 8, "g_zn": 9},
+    "spherical": {"potential": 0, "g_z": 3, "g_n": None, "g_e": None},
+}
+
+
+def point_gravity(coordinates, points, masses, field, coordinate_system="cartesian",
+                  parallel=True, dtype="float64", n_threads=None):
+    """Oracle restatement of harmonica.point_gravity (point.py:30-268)."""
+    if coordinate_system not in ("cartesian", "spherical"):
+        raise ValueError(f"Coordinate system {coordinate_system} not recognized.")
+    cast = np.broadcast(*coordinates[:3])
+    coords = tuple(
+        _f64(np.broadcast_to(np.asarray(c, dtype=np.float64), cast.shape)).ravel()
+        for c in coordinates[:3]
+    )
+    pts = tuple(_f64(np.atleast_1d(np.asarray(p, dtype=np.float64)).ravel()) for p in points[:3])
+    masses = _f64(np.atleast_1d(np.asarray(masses, dtype=np.float64)).ravel())
+    if masses.size != pts[0].size:
+        raise ValueError(
+            f"Number of elements in masses ({masses.size}) "
+            + f"mismatch the number of points ({pts[0].size})"
+        )
+    table = POINT_FIELDS[coordinate_system]
+    if field not in table:
+        raise ValueError(f"Gravitational field '{field}' not recognized")
+    if table[field] is None:
+        raise NotImplementedError
+    code = table[field]
+    out = np.zeros(cast.size)
+    lib = _load()
+    threads = (n_threads or default_threads()) if parallel else 1
+    lib.oracle_point_gravity(code, int(coordinate_system == "spherical"), out.size,
+                             _ptr(coords[0]), _ptr(coords[1]), _ptr(coords[2]), masses.size,
+                             _ptr(pts[0]), _ptr(pts[1]), _ptr(pts[2]), _ptr(masses), _ptr(out),
+                             threads)
+    if field in ("g_z", "g_ez", "g_ze", "g_nz", "g_zn"):
+        out *= -1
+    if field in ("g_e", "g_n", "g_z"):
+        out *= 1e5
+    if field in ("g_ee", "g_nn", "g_zz", "g_en", "g_ez", "g_nz", "g_ne", "g_ze", "g_zn"):
+        out *= 1e9
+    return out.astype(dtype).reshape(cast.shape)

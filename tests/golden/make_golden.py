@@ -10,7 +10,9 @@ Generate the golden fixtures in this directory.
    The inputs are those of the doctests; the expected outputs are parsed from
    the ``print`` results in the reference file, so the fixture is the
    reference's own output.
-2. ``oracle_small.npz``: outputs of the CPU oracle (oracle/prism_oracle.c) for
+2. ``reference_point_potential.npz``: the reference's point-mass potential
+   samples (test/data/sample_point_gravity.csv).
+3. ``oracle_small.npz``: outputs of the CPU oracle (oracle/prism_oracle.c) for
    the TestAgainstChoclo fixture of the reference tests
    (test/test_prism.py:161-190) for all ten fields, and for a small seeded
    prism layer, kept as regression vectors for the oracle and the GPU path.
@@ -92,11 +94,22 @@ def small_layer():
     return easting, northing, bottom, top, density, (ge.ravel(), gn.ravel(), gu.ravel())
 
 
+def point_sample(ref_root):
+    """The reference's own point-mass potential samples (test/data/sample_point_gravity.csv:
+    a 5000 kg mass at the origin, used by test/test_point_gravity.py:131-154)."""
+    data = np.loadtxt(os.path.join(ref_root, "test", "data", "sample_point_gravity.csv"),
+                      delimiter=",")
+    np.savez(os.path.join(HERE, "reference_point_potential.npz"), easting=data[:, 0],
+             northing=data[:, 1], upward=data[:, 2], potential=data[:, 3],
+             point=np.zeros(3), mass=np.array([5000.0]))
+
+
 def main():
     ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     if os.path.isdir(ref_root):
         with open(os.path.join(HERE, "reference_doctests.json"), "w") as f:
             json.dump(parse_doctests(ref_root), f, indent=1)
+        point_sample(ref_root)
     coords, prisms, densities = choclo_fixture()
     arrays = {
         "choclo_e": coords[0],

@@ -61,7 +61,7 @@ extern "C" {
 
 // Elementwise evaluation of the lean FP64 functions for the CPU tests.
 // kind: 0 sqrt(a), 1 a / b, 2 log(a), 3 log((a b) / (c d)), 4 log(a / c),
-//       5 arg(a + i b) on the branch nearest the float estimate c.
+//       5 arg(a + i b) on the branch nearest the float estimate c, 6 1/sqrt(a).
 void host_lean(int kind, int64_t n, const double* a, const double* b, const double* c,
                const double* d, double* out) {
   const Tables T = lean::host_tables();
@@ -72,7 +72,8 @@ void host_lean(int kind, int64_t n, const double* a, const double* b, const doub
       case 2: out[i] = lean::lm_log(a[i], T); break;
       case 3: out[i] = lean::lm_log_quot<false>(a[i], b[i], c[i], d[i], T); break;
       case 4: out[i] = lean::lm_log_quot<true>(a[i], 1.0, c[i], 1.0, T); break;
-      default: out[i] = lean::lm_arg_near(a[i], b[i], (float)c[i], T); break;
+      case 5: out[i] = lean::lm_arg_near(a[i], b[i], (float)c[i], T); break;
+      default: out[i] = lean::lm_rsqrt(a[i]); break;
     }
   }
 }

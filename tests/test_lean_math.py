@@ -46,6 +46,7 @@ def test_sqrt_div_log(lean):
     assert ulps(lean(0, x), np.sqrt(x)).max() <= 1.0
     assert ulps(lean(1, y, x), y / x).max() <= 1.0
     assert ulps(lean(2, x), np.log(x)).max() <= 1.0
+    assert ulps(lean(6, x), 1.0 / np.sqrt(x)).max() <= 2.0
     near = 1 + rng.uniform(-1e-3, 1e-3, 100_000)
     rel = np.abs(lean(2, near) - np.log(near)) / np.abs(np.log(near))
     assert rel.max() < 1e-15
