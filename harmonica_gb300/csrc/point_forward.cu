@@ -8,6 +8,8 @@
 // Cartesian kernels (choclo.point, from V = G m / l): with d = P - Q,
 //   potential  G m / l;   g_a = -G m d_a / l^3;
 //   g_ab = G m (3 d_a d_b - delta_ab l^2) / l^5.
+// The kernel returns them divided by G m and, for the first derivatives, by
+// -G m, the convention of field_scale() shared with the prism kernels.
 // Spherical (longitude, latitude in degrees, radius): potential G m / l and
 // the upward component -G m (r - r_p cos psi) / l^3 with
 //   cos psi = sin phi_p sin phi + cos phi_p cos phi cos(lambda_p - lambda),
@@ -38,9 +40,11 @@ __device__ __forceinline__ double point_cart(double dx, double dy, double dz) {
   const double inv = lean::lm_rsqrt(l2);
   if (F == kPotential) return inv;
   const double inv3 = (inv * inv) * inv;
-  if (F == kGe) return -dx * inv3;
-  if (F == kGn) return -dy * inv3;
-  if (F == kGz) return -dz * inv3;
+  // first derivatives carry the sign convention of the prism combinations
+  // (field_scale applies -G for them): +d / l^3 here is -g_a / (G m)
+  if (F == kGe) return dx * inv3;
+  if (F == kGn) return dy * inv3;
+  if (F == kGz) return dz * inv3;
   const double inv5 = inv3 * (inv * inv);
   if (F == kGee) return fma(3.0 * dx, dx, -l2) * inv5;
   if (F == kGnn) return fma(3.0 * dy, dy, -l2) * inv5;
@@ -98,7 +102,7 @@ __global__ void __launch_bounds__(kThreads) point_kernel(
         const double dr = x3 - rp;
         const double l2 = dr * dr + 2.0 * x3 * rp * (1.0 - cospsi);
         const double inv = lean::lm_rsqrt(l2);
-        v = F == kPotential ? inv : -(x3 - rp * cospsi) * ((inv * inv) * inv);
+        v = F == kPotential ? inv : (x3 - rp * cospsi) * ((inv * inv) * inv);
       } else {
         v = point_cart<F>(x1 - sh.a[k], x2 - sh.b[k], x3 - sh.c[k]);
       }
