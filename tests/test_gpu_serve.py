@@ -36,7 +36,7 @@ def test_results_match_drop_in(gpu_lib):
     srv.close()
     for p, r in zip(probs, res):
         ref = hg.prism_gravity(p["coordinates"], p["prisms"], p["density"], field=p["field"])
-        npt.assert_allclose(r, ref, rtol=1e-12, atol=1e-12 * np.abs(ref).max())
+        npt.assert_allclose(r, ref, rtol=1e-10, atol=1e-11 * np.abs(ref).max())
     st = srv.stats()
     assert st["completed"] == len(probs) and st["rounds"] > 1 and "p99_ms" in st
 
@@ -70,7 +70,7 @@ def test_resident_layer_and_admission_budget(gpu_lib):
     res = [f.result(timeout=120) for f in futs]
     ref = hg.prism_gravity(coords, prisms, density, field="g_z")
     for k, r in enumerate(res):
-        npt.assert_allclose(r, ref[k::4], rtol=1e-12, atol=1e-12 * np.abs(ref).max())
+        npt.assert_allclose(r, ref[k::4], rtol=1e-10, atol=1e-11 * np.abs(ref).max())
     # a request that can never fit is rejected, the server keeps going
     big = (np.zeros(200_000), np.zeros(200_000), np.ones(200_000))
     with pytest.raises(MemoryError):
