@@ -61,7 +61,7 @@ def parse_args():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-all-fields", action="store_true")
     p.add_argument("--all-fields-stations", type=int, default=1000)
-    p.add_argument("--workload", default="layer", choices=["layer", "batched", "inversion", "serving", "points"],
+    p.add_argument("--workload", default="layer", choices=["layer", "batched", "inversion", "serving", "points", "magnetic"],
                    help="layer: the 1e6-prism layer (default); batched: 256 uneven "
                         "g_z/g_zz problems, one persistent graph-captured launch vs one "
                         "launch per problem")
@@ -511,6 +511,62 @@ def run_points(args, rank, world, local):
                           "gpu_launches": 2 * args.steps}))
 
 
+def run_magnetic(args, rank, world, local):
+    """Prism magnetics (b_e, b_n, b_u together) on the 1e6-prism layer."""
+    import torch
+
+    from harmonica_gb300 import _native, synthetic
+    from harmonica_gb300.gravity import _ptr
+
+    _native.build()
+    lib = _native.lib()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    L = synthetic.layer_topography_1e6()
+    prisms, _ = synthetic.layer_to_prisms(L)
+    rng = np.random.default_rng(8)
+    mag = [rng.uniform(-1, 1, prisms.shape[0]) for _ in range(3)]
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).to(dev)  # noqa: E731
+    m = prisms.shape[0]
+    soa = torch.empty((9, m), dtype=torch.float64, device=dev)
+    aos, me, mn, mu = T(prisms), T(mag[0]), T(mag[1]), T(mag[2])
+    stream = torch.cuda.current_stream().cuda_stream
+    _native.check(lib.hg_pack_prisms_magnetic(_ptr(aos), _ptr(me), _ptr(mn), _ptr(mu), m,
+                                              _ptr(soa), m, stream))
+    c = [T(x) for x in L["coordinates"]]
+    B = 1000
+    out = torch.empty((3, B), dtype=torch.float64, device=dev)
+    ws = _native.ctypes.c_size_t(0)
+    _native.check(lib.hg_prism_magnetic_workspace(B, m, 3, _native.ctypes.byref(ws)))
+    work = torch.empty(max(1, ws.value // 8), dtype=torch.float64, device=dev)
+
+    def step(s):
+        lo = (s * B) % (c[0].numel() - B)
+        _native.check(lib.hg_prism_magnetic(_ptr(c[0][lo:]), _ptr(c[1][lo:]), _ptr(c[2][lo:]),
+                                            B, _ptr(soa), m, m, 3, _ptr(out), _ptr(work),
+                                            ws.value, torch.cuda.current_stream().cuda_stream))
+
+    for s in range(args.warmup):
+        step(s)
+    torch.cuda.synchronize()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record()
+    for s in range(args.steps):
+        step(args.warmup + s)
+    b.record()
+    torch.cuda.synchronize()
+    sec = a.elapsed_time(b) * 1e-3 / args.steps
+    if rank == 0:
+        print(json.dumps({"metric": "FP64 prism magnetic pairs/s (b_e, b_n, b_u per pair)",
+                          "value": B * m / sec, "unit": "pairs/s", "ms_per_step": sec * 1e3,
+                          "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                          "dtype": "f64", "data": "synthetic",
+                          "config": {"workload": "1e6-prism layer, magnetization U(-1,1) A/m, "
+                                                 "1000 stations per step"},
+                          "gpu_launches": 2 * args.steps}))
+
+
 def main():
     args = parse_args()
     rank, world, local = dist_env()
@@ -528,6 +584,9 @@ def main():
         return
     if args.workload == "points":
         run_points(args, rank, world, local)
+        return
+    if args.workload == "magnetic":
+        run_magnetic(args, rank, world, local)
         return
 
     import torch

@@ -19,6 +19,7 @@ from .batch import PrismBatch, autotune, prism_gravity_batch
 from .fields import FIELDS
 from .gravity import check_prisms, prism_gravity, prism_gravity_fields
 from .layer import DatasetAccessorPrismLayer, PrismLayer, prism_layer
+from .magnetic import prism_magnetic
 from .point import point_gravity
 
 __all__ = [
@@ -36,4 +37,5 @@ __all__ = [
     "prism_gravity_fields",
     "prism_layer",
     "point_gravity",
+    "prism_magnetic",
 ]

@@ -27,7 +27,8 @@ HEADERS = (
 
 #: translation units compiled into the library
 SOURCES = (
-    "prism_forward.cu", "prism_batch.cu", "prism_adjoint.cu", "point_forward.cu", "bench_probe.cu"
+    "prism_forward.cu", "prism_batch.cu", "prism_adjoint.cu", "point_forward.cu",
+    "prism_magnetic.cu", "bench_probe.cu",
 )
 
 ARCH_FLAGS = ("-gencode", "arch=compute_103a,code=sm_103a")
@@ -206,6 +207,21 @@ PROTOTYPES = {
     ),
     "hg_round_reduce": (
         ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]
+    ),
+    "hg_pack_prisms_magnetic": (
+        ctypes.c_int,
+        [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+         ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p],
+    ),
+    "hg_prism_magnetic_workspace": (
+        ctypes.c_int,
+        [ctypes.c_int64, ctypes.c_int64, ctypes.c_int32, ctypes.POINTER(ctypes.c_size_t)],
+    ),
+    "hg_prism_magnetic": (
+        ctypes.c_int,
+        [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+         ctypes.c_int64, ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+         ctypes.c_size_t, ctypes.c_void_p],
     ),
     "hg_point_forward_workspace": (
         ctypes.c_int, [ctypes.c_int64, ctypes.c_int64, ctypes.POINTER(ctypes.c_size_t)]

@@ -480,6 +480,29 @@ HG_HD __forceinline__ double pair_field(const Rel& q, const Tables& T) {
   }
 }
 
+// The six gradient-tensor combinations of one pair (the second derivatives
+// of the unit-density potential kernel, order ee, nn, uu, en, eu, nu with
+// upward u), for the magnetic field b = mu0/(4 pi) T M.  Singular points are
+// not masked here (the caller decides).
+template <bool LEAN>
+HG_HD __forceinline__ void pair_tensor6(const Rel& q, const Tables& T, double t[6]) {
+  Geom g;
+  make_geom<LEAN>(q, g);
+  t[0] = -(face_x<LEAN>(g, 1, T) - face_x<LEAN>(g, 0, T));
+  t[1] = -(face_y<LEAN>(g, 1, T) - face_y<LEAN>(g, 0, T));
+  t[2] = -(face_z<LEAN>(g, 1, T) - face_z<LEAN>(g, 0, T));
+  EdgeSet E;
+  edges_z(g, E);
+  t[3] = log_quot<LEAN>(E.num[1][1] * E.num[0][0], E.den[0][1] * E.den[1][0],
+                        E.den[1][1] * E.den[0][0], E.num[0][1] * E.num[1][0], T);
+  edges_y(g, E);
+  t[4] = log_quot<LEAN>(E.num[1][1] * E.num[0][0], E.den[0][1] * E.den[1][0],
+                        E.den[1][1] * E.den[0][0], E.num[0][1] * E.num[1][0], T);
+  edges_x(g, E);
+  t[5] = log_quot<LEAN>(E.num[1][1] * E.num[0][0], E.den[0][1] * E.den[1][0],
+                        E.den[1][1] * E.den[0][0], E.num[0][1] * E.num[1][0], T);
+}
+
 // g_z combination of one pair together with its two horizontal face angles
 // (the derivatives of the combination with respect to the bottom and top
 // coordinates: d/dz_bottom = O_bottom, d/dz_top = -O_top), for the adjoint.

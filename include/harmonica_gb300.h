@@ -261,6 +261,30 @@ int hg_layer_adjoint(const double *obs_e, const double *obs_n, const double *obs
 
 /*
  * ---------------------------------------------------------------------------
+ * Magnetic field of uniformly magnetized prisms.  Replaces the loops of
+ * _jit_prism_magnetic_field / _jit_prism_magnetic_component
+ * (src/harmonica/_forward/prisms/magnetic.py:275-400) behind prism_magnetic
+ * (:28-136): b = mu0/(4 pi) T M with T the unit-density gradient-tensor
+ * kernel, in nT.  Prisms with zero volume or zero magnetization are skipped
+ * (magnetic.py:410-440).
+ *   hg_pack_prisms_magnetic: (n, 6) [w, e, s, n, b, t] + 3 magnetization
+ *     vectors (A/m) -> 9 rows of prism_stride (w, e, s, n, b, t, m_e, m_n, m_u)
+ *   component: 0 b_e, 1 b_n, 2 b_u, 3 all three (out = 3 rows of n_obs)
+ */
+int hg_pack_prisms_magnetic(const double *prisms_aos, const double *mag_e, const double *mag_n,
+                            const double *mag_u, int64_t n_prisms, double *soa,
+                            int64_t prism_stride, void *stream);
+
+int hg_prism_magnetic_workspace(int64_t n_obs, int64_t n_prisms, int32_t component,
+                                size_t *bytes);
+
+int hg_prism_magnetic(const double *obs_e, const double *obs_n, const double *obs_u,
+                      int64_t n_obs, const double *prisms_soa, int64_t prism_stride,
+                      int64_t n_prisms, int32_t component, double *out, void *workspace,
+                      size_t workspace_bytes, void *stream);
+
+/*
+ * ---------------------------------------------------------------------------
  * Point masses.  Replaces the loops point_mass_cartesian / point_mass_spherical
  * (src/harmonica/_forward/point.py:357-450) behind point_gravity (:30-268).
  * spherical = 0: obs/pts are easting, northing, upward (m), any field code;

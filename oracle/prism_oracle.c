@@ -310,3 +310,52 @@ void oracle_point_gravity(int field, int spherical, int64_t n_obs, const double 
     }
     (void)n_threads;
 }
+
+/* ------------------------------------------------------------------------
+ * Magnetic prisms (harmonica src/harmonica/_forward/prisms/magnetic.py:275-400,
+ * loops over points (parallel) and prisms (sequential)).  choclo's
+ * magnetic_field kernel is restated from magnetostatics: outside the prism
+ * b = mu0/(4 pi) T M with T_ab the unit-density gradient-tensor 8-vertex sums
+ * of this file (vertex_term fields 4..9).  SI (tesla); the caller scales to nT.
+ */
+static double tensor_kernel(int field, double e, double n, double u, const double *p)
+{
+    double xs[2] = {p[0] - e, p[1] - e}, ys[2] = {p[2] - n, p[3] - n}, zs[2] = {p[4] - u, p[5] - u};
+    double sum = 0.0;
+    for (int i = 0; i < 2; i++)
+        for (int j = 0; j < 2; j++)
+            for (int k = 0; k < 2; k++) {
+                double sign = ((i + j + k) % 2 == 1) ? 1.0 : -1.0;
+                sum += sign * vertex_term(field, xs[i], ys[j], zs[k], i, j, k);
+            }
+    return sum;
+}
+
+void oracle_prism_magnetic(int64_t n_obs, const double *easting, const double *northing,
+                           const double *upward, int64_t n_prisms, const double *prisms,
+                           const double *me, const double *mn, const double *mu, double *be,
+                           double *bn, double *bu, int n_threads)
+{
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 16) num_threads(n_threads > 0 ? n_threads : 1)
+#endif
+    for (int64_t i = 0; i < n_obs; i++) {
+        double se = 0.0, sn = 0.0, su = 0.0;
+        for (int64_t j = 0; j < n_prisms; j++) {
+            const double *p = prisms + 6 * j;
+            double tee = tensor_kernel(4, easting[i], northing[i], upward[i], p);
+            double tnn = tensor_kernel(5, easting[i], northing[i], upward[i], p);
+            double tuu = tensor_kernel(6, easting[i], northing[i], upward[i], p);
+            double ten = tensor_kernel(7, easting[i], northing[i], upward[i], p);
+            double teu = tensor_kernel(8, easting[i], northing[i], upward[i], p);
+            double tnu = tensor_kernel(9, easting[i], northing[i], upward[i], p);
+            se += 1e-7 * (tee * me[j] + ten * mn[j] + teu * mu[j]);
+            sn += 1e-7 * (ten * me[j] + tnn * mn[j] + tnu * mu[j]);
+            su += 1e-7 * (teu * me[j] + tnu * mn[j] + tuu * mu[j]);
+        }
+        be[i] += se;
+        bn[i] += sn;
+        bu[i] += su;
+    }
+    (void)n_threads;
+}

@@ -82,6 +82,10 @@ def _load():
     lib.oracle_point_gravity.argtypes = [
         ctypes.c_int, ctypes.c_int, i64, dp, dp, dp, i64, dp, dp, dp, dp, dp, ctypes.c_int
     ]
+    lib.oracle_prism_magnetic.restype = None
+    lib.oracle_prism_magnetic.argtypes = [
+        i64, dp, dp, dp, i64, dp, dp, dp, dp, dp, dp, dp, ctypes.c_int
+    ]
     lib.oracle_is_singular.restype = ctypes.c_int
     lib.oracle_is_singular.argtypes = [
         ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, dp
@@ -297,3 +301,49 @@ def point_gravity(coordinates, points, masses, field, coordinate_system="cartesi
     if field in ("g_ee", "g_nn", "g_zz", "g_en", "g_ez", "g_nz", "g_ne", "g_ze", "g_zn"):
         out *= 1e9
     return out.astype(dtype).reshape(cast.shape)
+
+
+MAGNETIC_FIELDS = ("b", "b_e", "b_n", "b_u")
+
+
+def prism_magnetic(coordinates, prisms, magnetization, field, parallel=True, dtype=np.float64,
+                   disable_checks=False, n_threads=None):
+    """Oracle restatement of harmonica.prism_magnetic (magnetic.py:28-136), nT."""
+    if field not in MAGNETIC_FIELDS:
+        raise ValueError(
+            f"Invalid field '{field}'. Please choose one of '{','.join(MAGNETIC_FIELDS)}'."
+        )
+    cast = np.broadcast(*coordinates[:3])
+    coords = tuple(
+        _f64(np.broadcast_to(np.asarray(c, dtype=np.float64), cast.shape)).ravel()
+        for c in coordinates[:3]
+    )
+    prisms = np.atleast_2d(np.asarray(prisms, dtype=np.float64))
+    mag = tuple(_f64(np.atleast_1d(np.asarray(m, dtype=np.float64)).ravel())
+                for m in magnetization)
+    if not disable_checks:
+        if len(mag) != 3:
+            raise ValueError(
+                f"Invalid magnetization vectors with '{len(mag)}' elements. "
+                + "Magnetization vectors should have only 3 elements."
+            )
+        if mag[0].size != prisms.shape[0]:
+            raise ValueError(
+                f"Number of magnetization vectors ({mag[0].size}) "
+                + f"mismatch the number of prisms ({prisms.shape[0]})"
+            )
+        check_prisms(prisms)
+    w, e, s, n, b, t = (prisms[:, k] for k in range(6))
+    keep = ~((w == e) | (s == n) | (b == t) | ((mag[0] == 0) & (mag[1] == 0) & (mag[2] == 0)))
+    prisms = _f64(prisms[keep])
+    mag = tuple(_f64(m[keep]) for m in mag)
+    out = [np.zeros(cast.size) for _ in range(3)]
+    lib = _load()
+    threads = (n_threads or default_threads()) if parallel else 1
+    lib.oracle_prism_magnetic(cast.size, _ptr(coords[0]), _ptr(coords[1]), _ptr(coords[2]),
+                              prisms.shape[0], _ptr(prisms), _ptr(mag[0]), _ptr(mag[1]),
+                              _ptr(mag[2]), _ptr(out[0]), _ptr(out[1]), _ptr(out[2]), threads)
+    out = [(o * 1e9).astype(dtype).reshape(cast.shape) for o in out]
+    if field == "b":
+        return tuple(out)
+    return out[{"b_e": 0, "b_n": 1, "b_u": 2}[field]]

@@ -1,0 +1,47 @@
+"""
+Prism magnetics without a GPU: argument errors of the drop-in
+(test/test_prism_magnetic.py:29-225) and the oracle's physics pins (far-field
+dipole limit, b = mu0/(4 pi) T M consistent with the gravity tensor).
+"""
+
+import numpy as np
+import numpy.testing as npt
+import pytest
+
+import harmonica_gb300 as hg
+
+
+def test_errors():
+    with pytest.raises(ValueError, match="Invalid field"):
+        hg.prism_magnetic([0, 0, 0], [-1, 1, -1, 1, -2, -1], ([1.0], [1.0], [1.0]), "Bx")
+    prisms = [[-1, 1, -1, 1, -2, -1], [-1, 1, -1, 1, -4, -3]]
+    with pytest.raises(ValueError, match="Invalid magnetization vectors with '2' elements"):
+        hg.prism_magnetic([0, 0, 0], prisms, ([1.0, 1.0], [1.0, 1.0]), "b")
+    with pytest.raises(ValueError, match=r"Number of magnetization vectors \(3\) mismatch"):
+        hg.prism_magnetic([0, 0, 0], prisms, ([1.0] * 3, [1.0] * 3, [1.0] * 3), "b")
+    with pytest.raises(ValueError, match="The bottom boundary can't be greater than the top one"):
+        hg.prism_magnetic([0, 0, 0], [-1, 1, -1, 1, -1, -2], ([1.0], [1.0], [1.0]), "b_u")
+
+
+def test_oracle_far_field_dipole(oracle):
+    prism = [-1, 1, -1, 1, -1001, -999]
+    M = np.array([1.0, 2.0, 3.0])
+    rng = np.random.default_rng(0)
+    for _ in range(5):
+        pt = rng.uniform(-500, 500, 3)
+        r = pt - np.array([0.0, 0.0, -1000.0])
+        R = np.linalg.norm(r)
+        m = M * 8.0
+        dip = 1e-7 * (3 * r * np.dot(m, r) / R ** 5 - m / R ** 3) * 1e9
+        b = np.array(oracle.prism_magnetic(tuple([x] for x in pt), prism, tuple([x] for x in M),
+                                           "b")).ravel()
+        npt.assert_allclose(b, dip, rtol=1e-4)
+
+
+def test_oracle_tensor_relation(oracle):
+    """b_u of an upward magnetization equals mu0/(4 pi) * g_zz / (G rho) (outside)."""
+    prism = [-100, 120, -80, 60, -500, -200]
+    coords = ([10.0, 300.0], [-20.0, 50.0], [100.0, 30.0])
+    bu = oracle.prism_magnetic(coords, prism, ([0.0], [0.0], [2.0]), "b_u")
+    gzz = oracle.prism_gravity(coords, prism, [1.0], "g_zz")  # Eotvos for rho = 1
+    npt.assert_allclose(bu, 1e-7 * 2.0 * gzz / 6.6743e-11, rtol=1e-12)
