@@ -73,7 +73,8 @@ struct SmemTile {
 
 struct SmemTables {
   double logc[lean::kLogTableSize], logl[lean::kLogTableSize];
-  double th[lean::kArgTableSize], cs[lean::kArgTableSize], sn[lean::kArgTableSize];
+  double th[lean::kArgTableSize];
+  float csf[2 * lean::kArgTableSize], snf[2 * lean::kArgTableSize];
 
   // Copy the constant tables of lean_math.cuh; the caller synchronises.
   __device__ __forceinline__ Tables stage() {
@@ -81,12 +82,12 @@ struct SmemTables {
       logc[t] = lean::kLogC[t];
       logl[t] = lean::kLogL[t];
     }
-    for (int t = threadIdx.x; t < lean::kArgTableSize; t += blockDim.x) {
-      th[t] = lean::kArgTh[t];
-      cs[t] = lean::kArgCos[t];
-      sn[t] = lean::kArgSin[t];
+    for (int t = threadIdx.x; t < lean::kArgTableSize; t += blockDim.x) th[t] = lean::kArgTh[t];
+    for (int t = threadIdx.x; t < 2 * lean::kArgTableSize; t += blockDim.x) {
+      csf[t] = lean::kArgCosF[t];
+      snf[t] = lean::kArgSinF[t];
     }
-    return Tables{logc, logl, th, cs, sn};
+    return Tables{logc, logl, th, csf, snf};
   }
 };
 

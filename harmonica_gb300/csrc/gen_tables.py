@@ -9,7 +9,10 @@ functions in lean_math.cuh, correctly rounded with mpmath.
   so logarithms of arguments near 1 have no table error.
 * argument table: TH[j] = double(j * pi / 128), j = -32..32 (one quadrant
   split in 64 steps), with COS[j], SIN[j] the correctly rounded cosine and
-  sine of the double TH[j].
+  sine of the double TH[j]; COSF/SINF hold the same cosine and sine as
+  float pairs (hi = nearest float, lo = nearest float to the remainder),
+  interleaved hi, lo.
+* kThirdHi/kThirdLo: 1/3 as a float pair.
 
 Run:  python harmonica_gb300/csrc/gen_tables.py   (writes next to this file)
 """
@@ -25,6 +28,16 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 
 def d(x):
     return float(x).hex()
+
+
+def fl(x):
+    return float(x).hex() + "f"
+
+
+def f32pair(x):
+    hi = np.float32(float(x))
+    lo = np.float32(float(x - mp.mpf(float(hi))))
+    return float(hi), float(lo)
 
 
 def main():
@@ -64,6 +77,16 @@ def main():
         lines.append(f"HG_TABLE_QUAL double {name}[kArgTableSize] = {{")
         lines += [f"    {d(v)}," for v in vals]
         lines.append("};")
+    for name, vals in (("kArgCosF", co), ("kArgSinF", si)):
+        lines.append(f"HG_TABLE_QUAL float {name}[2 * kArgTableSize] = {{")
+        for t, v in zip(th, vals):
+            exact = mp.cos(mp.mpf(t)) if name == "kArgCosF" else mp.sin(mp.mpf(t))
+            hi, lo = f32pair(exact)
+            lines.append(f"    {fl(hi)}, {fl(lo)},")
+        lines.append("};")
+    hi, lo = f32pair(mp.mpf(1) / 3)
+    lines.append(f"constexpr float kThirdHi = {fl(hi)};")
+    lines.append(f"constexpr float kThirdLo = {fl(lo)};")
     # constants split in a high part with 40 significant bits (so that an
     # integer of up to 13 bits times the high part is exact) and a low part
     for name, val in (("Ln2", mp.log(2)), ("Pio2", mp.pi / 2)):

@@ -4,11 +4,12 @@
 // FP32 pipe 128 and the integer pipe 64, so a double-precision log or
 // arctangent from a generic library (tens of FP64 instructions each) dominates
 // the prism kernels.  The functions below do every step that does not need 53
-// bits -- exponent/mantissa splitting, table indexing, seeds, the high-order
-// terms of series -- with integer and FP32 instructions, and keep only the
-// final refinement in FP64:
+// bits -- exponent/mantissa splitting, table indexing, seeds, quotients and
+// series on float pairs (two floats, ~46 bits) -- with integer and FP32
+// instructions, and keep only the final refinement or assembly in FP64:
 //
-//   lm_sqrt   FP32 rsqrt seed of the mantissa, two Newton steps     5 FP64 ops
+//   lm_sqrt   float-pair square root of the mantissa, one FP64 Newton step
+//                                                                  3 FP64 ops
 //   lm_div    FP32 reciprocal seed, one Newton step, one residual    5 FP64 ops
 //   lm_log    table-driven logarithm after P. T. P. Tang, "Table-driven
 //             implementation of the logarithm function in IEEE
@@ -16,10 +17,14 @@
 //             x = 2^e m, m in [0.75, 1.5); t = m c_k - 1 with c_k ~ 1/g_k
 //             from a 193-entry grid; ln x = e ln2 + (-ln c_k) + log1p(t),
 //             log1p by its Taylor series to t^8 (terms t^5.. in FP32)   ~10 FP64 ops
+//   lm_log_quot  the same reduction for ln((p1 p2)/(q1 q2)) with the exact
+//             FMA numerator near 1 and t, log1p(t) on float pairs
+//                                       4 FP64 ops near 1, 7 otherwise
 //   lm_arg_near  argument of a complex number, unwrapped to the 2*pi branch
 //             nearest an FP32 estimate: exact rotation by quarter turns,
-//             rotation by a tabulated angle (cos/sin correctly rounded),
-//             then arctan(u) = u - u^3/3 + (u^5/5 - u^7/7 in FP32)     ~17 FP64 ops
+//             rotation by a tabulated angle, quotient and
+//             arctan(u) = u - u^3/3 + u^5/5 - u^7/7 on float pairs
+//                                       1 FP64 op for small angles, <= 4 otherwise
 //
 // Inputs outside the fast path (zero, negative, subnormal, inf, NaN) fall
 // back to the generic functions, so special values behave like the library.
@@ -154,7 +159,132 @@ HG_HD __forceinline__ double int_to_double(int e) {
   return ll2d(0x4338000000000000LL + (long long)e) - 6755399441055744.0;
 }
 
+// int -> double without an FP64 instruction (exact for |e| < 2^24).
+HG_HD __forceinline__ double small_int_to_double(int e) { return f2d_scaled((float)e, 0); }
+
 // ---------------------------------------------------------------------------
+// Float pairs: a value held as h + l in two floats (about 46 significant
+// bits), computed on the FP32 pipe.  Built from the error-free
+// transformations two-sum (D. E. Knuth, TAOCP vol. 2, sec. 4.2.2) and the
+// exact product by fused multiply-add (the FMA form of T. J. Dekker, "A
+// floating-point technique for extending the available precision", Numer.
+// Math. 18, 1971).  The device versions use the round-to-nearest intrinsics
+// so that the compiler never contracts or reassociates them.
+struct F2 {
+  float h, l;
+};
+
+HG_HD __forceinline__ float fadd(float a, float b) {
+#ifdef __CUDA_ARCH__
+  return __fadd_rn(a, b);
+#else
+  return a + b;
+#endif
+}
+HG_HD __forceinline__ float fsub(float a, float b) {
+#ifdef __CUDA_ARCH__
+  return __fsub_rn(a, b);
+#else
+  return a - b;
+#endif
+}
+HG_HD __forceinline__ float fmul(float a, float b) {
+#ifdef __CUDA_ARCH__
+  return __fmul_rn(a, b);
+#else
+  return a * b;
+#endif
+}
+HG_HD __forceinline__ float ffma(float a, float b, float c) {
+#ifdef __CUDA_ARCH__
+  return __fmaf_rn(a, b, c);
+#else
+  return std::fmaf(a, b, c);
+#endif
+}
+HG_HD __forceinline__ float u32_to_f32(unsigned u) {
+#ifdef __CUDA_ARCH__
+  return __uint2float_rn(u);
+#else
+  return (float)u;
+#endif
+}
+
+// a + b = s.h + s.l exactly, any order of magnitude
+HG_HD __forceinline__ F2 two_sum(float a, float b) {
+  const float s = fadd(a, b);
+  const float bb = fsub(s, a);
+  return F2{s, fadd(fsub(a, fsub(s, bb)), fsub(b, bb))};
+}
+// a + b = s.h + s.l exactly, for |a| >= |b| (or a == 0)
+HG_HD __forceinline__ F2 quick_two_sum(float a, float b) {
+  const float s = fadd(a, b);
+  return F2{s, fsub(b, fsub(s, a))};
+}
+// a b = p.h + p.l exactly (no underflow)
+HG_HD __forceinline__ F2 two_prod(float a, float b) {
+  const float p = fmul(a, b);
+  return F2{p, ffma(a, b, -p)};
+}
+// products and sums of pairs, relative error ~2^-44 (sums without heavy
+// cancellation; with cancellation the error stays ~2^-46 of the operands)
+HG_HD __forceinline__ F2 f2_mul(F2 a, F2 b) {
+  const F2 p = two_prod(a.h, b.h);
+  return quick_two_sum(p.h, ffma(a.h, b.l, ffma(a.l, b.h, p.l)));
+}
+HG_HD __forceinline__ F2 f2_add(F2 a, F2 b) {
+  const F2 s = two_sum(a.h, b.h);
+  return quick_two_sum(s.h, fadd(s.l, fadd(a.l, b.l)));
+}
+HG_HD __forceinline__ F2 f2_neg(F2 a) { return F2{-a.h, -a.l}; }
+
+// a / b for b > 0: FP32 reciprocal refined to float accuracy, the quotient
+// rounded to a float and one correction from the exact-by-FMA residual.
+HG_HD __forceinline__ F2 f2_div(F2 a, F2 b) {
+  float y = rcp_approx(b.h);
+  y = ffma(y, ffma(-b.h, y, 1.0f), y);
+  const float qh = fmul(a.h, y);
+  float r = ffma(-qh, b.h, a.h);
+  r = fadd(r, a.l);
+  r = ffma(-qh, b.l, r);
+  return F2{qh, fmul(r, y)};
+}
+
+// The significand of a normal double (bits b) as a pair in [1, 2):
+// h = the leading 24 bits, l = the other 29 bits (rounded to a float).
+HG_HD __forceinline__ F2 mant_f2(long long b) {
+  const float h = u2f(0x3f800000u | (unsigned)((b >> 29) & 0x7fffff));
+  const float l = fmul(u32_to_f32((unsigned)(b & 0x1fffffff)), 0x1p-52f);
+  return F2{h, l};
+}
+
+// 2^k as a float, for -126 <= k <= 127
+HG_HD __forceinline__ float pow2f(int k) { return u2f((unsigned)(127 + k) << 23); }
+
+// Signed value of the double with bits b times 2^(1023 - top) as a pair,
+// where top >= the double's biased exponent ef: sign * mant * 2^(ef - top).
+// Zero and subnormal inputs and results below 2^-120 give 0.
+HG_HD __forceinline__ F2 scaled_f2(long long b, int top) {
+  const int ef = (int)((b >> 52) & 0x7ff);
+  const int k = ef - top;
+  F2 m = mant_f2(b);
+  const float sc = pow2f(k < -120 ? -120 : k);
+  m.h = fmul(m.h, sc);
+  m.l = fmul(m.l, sc);
+  if (b < 0) m = f2_neg(m);
+  return (ef == 0 || k < -120) ? F2{0.0f, 0.0f} : m;
+}
+
+// The pair as a double times 2^k (one FP64 add).
+HG_HD __forceinline__ double f2_to_double(F2 a, int k) {
+  return f2d_scaled(a.h, k) + f2d_scaled(a.l, k);
+}
+
+// ---------------------------------------------------------------------------
+// sqrt(x): x = 4^k m with m in [1, 4) held as a float pair; sqrt(m) to
+// ~2^-43 from an FP32 rsqrt seed and one FP32 Newton correction of the pair
+// residual, converted to a double (one FP64 add), then one FP64 Newton step
+// s + (x - s^2) / (2 s) (two FMAs).
 HG_HD __forceinline__ double lm_sqrt(double x) {
   const long long b = d2ll(x);
   const int ef = (int)((b >> 52) & 0x7ff);
@@ -162,16 +292,16 @@ HG_HD __forceinline__ double lm_sqrt(double x) {
   const int e = ef - 1023;
   const int odd = e & 1;
   const int k = (e - odd) / 2;
-  // mantissa in [1, 4): exponent 0 or 1
-  const float mf = u2f(((unsigned)(127 + odd) << 23) | (unsigned)((b >> 29) & 0x7fffff));
-  const float yf = rsqrt_approx(mf);
-  const double y = f2d_scaled(yf, -k);      // ~ 1/sqrt(x), rel. err ~2^-22
-  const double h = f2d_scaled(yf, -k - 1);  // y / 2
-  double s = x * y;
-  double r = fma(-s, s, x);
-  s = fma(r, h, s);  // ~2^-44
-  r = fma(-s, s, x);
-  return fma(r, h, s);
+  const float mh = u2f(((unsigned)(127 + odd) << 23) | (unsigned)((b >> 29) & 0x7fffff));
+  const float ml =
+      fmul(u32_to_f32((unsigned)(b & 0x1fffffff)), odd ? 0x1p-51f : 0x1p-52f);
+  const float y = rsqrt_approx(mh);  // ~1/sqrt(m), 2^-22
+  const float sh = fmul(mh, y);
+  const float hy = fmul(0.5f, y);
+  const float res = fadd(ffma(-sh, sh, mh), ml);  // m - sh^2
+  const double s = f2_to_double(F2{sh, fmul(res, hy)}, k);
+  const double r = fma(-s, s, x);
+  return fma(r, f2d_scaled(hy, -k), s);
 }
 
 // 1 / sqrt(x): FP32 seed of the mantissa and two Newton steps
@@ -209,8 +339,8 @@ struct Tables {
   const double* logc;
   const double* logl;
   const double* th;
-  const double* cs;
-  const double* sn;
+  const float* csf;  // cos(th_j) as float pairs (hi, lo)
+  const float* snf;  // sin(th_j) as float pairs
 };
 
 // Host view of the tables (the device kernels stage them in shared memory).
@@ -218,7 +348,7 @@ inline Tables host_tables() {
 #ifdef __CUDA_ARCH__
   return Tables{nullptr, nullptr, nullptr, nullptr, nullptr};
 #else
-  return Tables{kLogC, kLogL, kArgTh, kArgCos, kArgSin};
+  return Tables{kLogC, kLogL, kArgTh, kArgCosF, kArgSinF};
 #endif
 }
 
@@ -246,39 +376,79 @@ HG_HD __forceinline__ double lm_log(double x, const Tables& T) {
   return fma(ed, kLn2Hi, T.logl[k]) + fma(ed, kLn2Lo, p);
 }
 
-// Argument of (pr + i pi) on the 2*pi branch nearest `est` (an FP32
-// estimate of the wanted angle, within ~1e-3 of it).  The table rotation and
-// the quarter-turn assembly are skipped for small angles (the common case for
-// distant faces).
-HG_HD __forceinline__ double lm_arg_near(double pr, double pi, float est, const Tables& T) {
-  const int q = round_to_int(est * 0.636619772f);  // quarter turns
+// Argument of a complex number on the 2*pi branch nearest `est` (an FP32
+// estimate of the wanted angle, within ~1e-3 of it).  The vector is rotated
+// by -q pi/2 exactly (q = nearest quarter turn of est) and, as a float pair,
+// by -th_j (th_j = j pi/128 nearest the remainder); the residual angle
+// (|u| <= ~tan(pi/256)) is arctan(u), u = im/re, by
+//   u + u^3 (-1/3 + u^2/5 - u^4/7)
+// with u, u^3 and 1/3 as float pairs and the tail in FP32 (~2^-46 absolute).
+// FP64 work: one add to form the double, plus th_j and q pi/2 when nonzero.
+HG_HD __forceinline__ void arg_plan(float est, int& q, int& j) {
+  q = round_to_int(est * 0.636619772f);  // quarter turns
   const float rem = fmaf((float)(-q), 1.57079637f, est);
-  int j = round_to_int(rem * 40.7436654f);  // 128 / pi
+  j = round_to_int(rem * 40.7436654f);  // 128 / pi
   j = j < -kArgTableHalf ? -kArgTableHalf : (j > kArgTableHalf ? kArgTableHalf : j);
-  // rotate by -q pi/2 exactly
-  const int qm = q & 3;
-  const double r0 = qm == 0 ? pr : (qm == 1 ? pi : (qm == 2 ? -pr : -pi));
-  const double i0 = qm == 0 ? pi : (qm == 1 ? -pr : (qm == 2 ? -pi : pr));
-  double re = r0, im = i0;
+}
+
+// (re, im): the vector already rotated by -q pi/2, as float pairs of
+// magnitude ~1 (any common scale).
+HG_HD __forceinline__ double arg_core(F2 re, F2 im, int q, int j, const Tables& T) {
+  const F2 re0 = re, im0 = im;
   if (j != 0) {  // rotate by -th_j
-    const double C = T.cs[j + kArgTableHalf], S = T.sn[j + kArgTableHalf];
-    re = fma(i0, S, r0 * C);
-    im = fma(-r0, S, i0 * C);
+    const int jj = 2 * (j + kArgTableHalf);
+    const F2 C{T.csf[jj], T.csf[jj + 1]}, S{T.snf[jj], T.snf[jj + 1]};
+    const F2 r2 = f2_add(f2_mul(re, C), f2_mul(im, S));
+    im = f2_add(f2_mul(im, C), f2_neg(f2_mul(re, S)));
+    re = r2;
   }
+  const F2 u = f2_div(im, re);
   double delta;
-  const double u = lm_div(im, re);
-  const float uf = d2f_trunc(u);
-  if (fabsf(uf) < 0.02f && d2ll(re) > 0) {
-    const float u2f_ = uf * uf;
-    const float tail = u2f_ * fmaf(u2f_, -0.142857143f, 0.2f);  // u^2/5 - u^4/7
-    const double u3 = (u * u) * u;
-    delta = fma(u3, f2d_scaled(tail, 0) - 1.0 / 3.0, u);
+  if (re.h > 0.0f && fabsf(u.h) < 0.02f) {
+    F2 s2 = two_prod(u.h, u.h);
+    s2.l = ffma(2.0f * u.h, u.l, s2.l);  // u^2
+    F2 w = two_prod(s2.h, u.h);
+    w.l = ffma(s2.h, u.l, ffma(s2.l, u.h, w.l));  // u^3
+    const float tail = fmul(s2.h, ffma(s2.h, -0.142857143f, 0.2f));  // u^2/5 - u^4/7
+    F2 c = two_prod(w.h, -kThirdHi);
+    c.l = ffma(w.h, fsub(tail, kThirdLo), ffma(w.l, -kThirdHi, c.l));  // u^3 (-1/3 + tail)
+    F2 a = quick_two_sum(u.h, c.h);
+    a.l = fadd(a.l, fadd(u.l, c.l));
+    delta = f2_to_double(a, 0);
   } else {
-    delta = atan2(im, re);  // estimate too far off: generic path
+    // estimate too far off or non-finite input: generic path on the
+    // quarter-turn-rotated vector
+    delta = atan2(f2_to_double(im0, 0), f2_to_double(re0, 0));
+    j = 0;
   }
   if (q == 0) return j == 0 ? delta : T.th[j + kArgTableHalf] + delta;
-  const double qd = int_to_double(q);
+  const double qd = small_int_to_double(q);
   return fma(qd, kPio2Hi, T.th[j + kArgTableHalf]) + fma(qd, kPio2Lo, delta);
+}
+
+HG_HD __forceinline__ double lm_arg_near(double pr, double pi, float est, const Tables& T) {
+  int q, j;
+  arg_plan(est, q, j);
+  // rotate by -q pi/2 exactly: (r0, i0) as the bits of +-pr / +-pi
+  const int qm = q & 3;
+  const long long bpr = d2ll(pr), bpi = d2ll(pi);
+  const long long kSign = (long long)0x8000000000000000ULL;
+  const long long br = qm == 0 ? bpr : (qm == 1 ? bpi : (qm == 2 ? bpr ^ kSign : bpi ^ kSign));
+  const long long bi = qm == 0 ? bpi : (qm == 1 ? bpr ^ kSign : (qm == 2 ? bpi ^ kSign : bpr));
+  const int er = (int)((br >> 52) & 0x7ff), ei = (int)((bi >> 52) & 0x7ff);
+  if (er == 0x7ff || ei == 0x7ff) return atan2(pi, pr);
+  const int top = (er > ei ? er : ei);
+  return arg_core(scaled_f2(br, top), scaled_f2(bi, top), q, j, T);
+}
+
+// The same for a vector given as float pairs (finite, magnitude ~1).
+HG_HD __forceinline__ double lm_arg_near_f2(F2 pr, F2 pi, float est, const Tables& T) {
+  int q, j;
+  arg_plan(est, q, j);
+  const int qm = q & 3;
+  const F2 r0 = qm == 0 ? pr : (qm == 1 ? pi : (qm == 2 ? f2_neg(pr) : f2_neg(pi)));
+  const F2 i0 = qm == 0 ? pi : (qm == 1 ? f2_neg(pr) : (qm == 2 ? f2_neg(pi) : pr));
+  return arg_core(r0, i0, q, j, T);
 }
 
 // ln((p1 p2) / (q1 q2)) for positive normal arguments, without forming the
@@ -288,8 +458,13 @@ HG_HD __forceinline__ double lm_arg_near(double pr, double pi, float est, const 
 // and ln = E ln2 - ln c_k + log1p(t).  When the quotient is within half a
 // table step of 1 (c_k = 1, E = 0) the numerator is the exact FMA
 // p1 p2 - q1 q2 and the table/exponent terms vanish: the log of a ratio near
-// 1 keeps its full relative accuracy.  ONE_FACTOR skips the products
-// (p2 = q2 = 1).  Other inputs take the generic path.
+// 1 keeps its relative accuracy.  The division and log1p run on float pairs
+// (t to ~2^-44 relative, |t| <= 2^-8.5):
+//   log1p(t) = t - t^2/2 + t^3 (1/3 - t/4 + t^2/5 - t^3/6)
+// with t, t^2, t^3 and 1/3 as pairs and the tail in FP32.  FP64 work: the
+// products and the numerator FMA, one add to form the double, and three
+// more for the table and exponent terms away from 1.  ONE_FACTOR skips the
+// products (p2 = q2 = 1).  Other inputs take the generic path.
 template <bool ONE_FACTOR>
 HG_HD __forceinline__ double lm_log_quot(double p1, double p2, double q1, double q2,
                                          const Tables& T) {
@@ -318,25 +493,34 @@ HG_HD __forceinline__ double lm_log_quot(double p1, double p2, double q1, double
   k = k < 0 ? 0 : (k > kLogTableSize - 1 ? kLogTableSize - 1 : k);
   const bool near1 = (E == 0) && (k == 64);
   if (!near1 && (E > 1000 || E < -1000)) return log((ONE_FACTOR ? p1 : p1 * p2) / d);
-  // 1/d: FP32 seed and one Newton step (~2^-44; t is small, so ample)
-  double r = f2d_scaled(rcp_approx(mant(bd)), -(ed - 1023));
-  r = fma(r, fma(-d, r, 1.0), r);
-  double num;
-  if (near1) {
-    num = ONE_FACTOR ? p1 - d : fma(p1, p2, -d);
-  } else {
-    const double cp = ll2d(d2ll(T.logc[k]) - ((long long)E << 52));  // c_k 2^-E, exact
-    num = fma(ONE_FACTOR ? p1 : p1 * p2, cp, -d);
-  }
-  const double t = num * r;
-  const float tf = d2f_trunc(t);
-  const float r2 = fmaf(tf, fmaf(tf, fmaf(tf, -0.125f, 0.142857143f), -0.166666672f), 0.2f);
-  double a = fma(t, f2d_scaled(r2, 0), -0.25);
-  a = fma(t, a, 1.0 / 3.0);
-  a = fma(t, a, -0.5);
-  const double p = fma(t * t, a, t);  // log1p(t)
+  // numerator p1 p2 c_k 2^-E - q1 q2, exact when c_k 2^-E = 1
+  const double cp = near1 ? 1.0 : ll2d(d2ll(T.logc[k]) - ((long long)E << 52));
+  const double num = ONE_FACTOR ? fma(p1, cp, -d) : fma(p1, p2 * cp, -d);
+  const long long bn = d2ll(num);
+  const int en = (int)((bn >> 52) & 0x7ff);
+  if (en == 0x7ff || (en == 0 && (bn << 1) != 0)) return log((ONE_FACTOR ? p1 : p1 * p2) / d);
+  // t = num / d: significands divided as pairs, scaled by 2^(en - ed)
+  F2 t = f2_div(mant_f2(bn), mant_f2(bd));
+  const int sc = en - ed;
+  const float scale = pow2f(sc < -120 ? -120 : (sc > 0 ? 0 : sc));
+  t.h = fmul(t.h, scale);
+  t.l = fmul(t.l, scale);
+  if (bn < 0) t = f2_neg(t);
+  if (en == 0 || sc < -120) t = F2{0.0f, 0.0f};  // |t| < 2^-120 counts as 0
+  F2 s2 = two_prod(t.h, t.h);
+  s2.l = ffma(2.0f * t.h, t.l, s2.l);  // t^2
+  F2 w = two_prod(s2.h, t.h);
+  w.l = ffma(s2.h, t.l, ffma(s2.l, t.h, w.l));  // t^3
+  const float tail = fmul(t.h, ffma(t.h, ffma(t.h, -0.166666672f, 0.2f), -0.25f));
+  F2 c = two_prod(w.h, kThirdHi);
+  c.l = ffma(w.h, fadd(tail, kThirdLo), ffma(w.l, kThirdHi, c.l));  // t^3 (1/3 + tail)
+  F2 v = quick_two_sum(fmul(-0.5f, s2.h), c.h);
+  v.l = fadd(v.l, ffma(-0.5f, s2.l, c.l));
+  F2 lp = quick_two_sum(t.h, v.h);
+  lp.l = fadd(lp.l, fadd(t.l, v.l));
+  const double p = f2_to_double(lp, 0);  // log1p(t)
   if (near1) return p;
-  const double edd = int_to_double(E);
+  const double edd = small_int_to_double(E);
   return fma(edd, kLn2Hi, T.logl[k]) + fma(edd, kLn2Lo, p);
 }
 

@@ -88,6 +88,10 @@ HG_HD __forceinline__ int sgn(double v) {
 
 // Multiply a log/angle by a coefficient, with the limit 0 * (singular) = 0.
 HG_HD __forceinline__ double cmul(double coef, double v) { return is_zero(coef) ? 0.0 : coef * v; }
+// acc + coef * v with the same limit (one FMA)
+HG_HD __forceinline__ double cfma(double coef, double v, double acc) {
+  return fma(coef, is_zero(coef) ? 0.0 : v, acc);
+}
 
 template <bool LEAN> struct Math;
 template <> struct Math<true> {
@@ -189,16 +193,16 @@ HG_HD __forceinline__ AxisCase axis_case(double a1, double a2) {
   return c;
 }
 
+// Ratio terms of one edge before the straddle case: num = hi + r_hi and
+// den = |lo| + r_lo (lo + r_lo, or r_lo - lo when lo < 0).
 HG_HD __forceinline__ void edge_ratio(AxisCase c, double a1, double a2, double r1, double r2,
-                                      double rho2, double& num, double& den) {
+                                      double& num, double& den) {
   const double lo = c.reflect ? -a2 : a1;
   const double hi = c.reflect ? -a1 : a2;
   const double rlo = c.reflect ? r2 : r1;
   const double rhi = c.reflect ? r1 : r2;
-  const double t = fabs(lo) + rlo;  // lo + rlo, or rlo - lo when lo < 0
-  const double h = hi + rhi;
-  num = c.straddle ? h * t : h;
-  den = c.straddle ? rho2 : t;
+  den = fabs(lo) + rlo;
+  num = hi + rhi;
 }
 
 // The 4 edges parallel to one axis, indexed [p][s] by the other two axes in
@@ -207,6 +211,19 @@ struct EdgeSet {
   double num[2][2], den[2][2];
 };
 
+// Straddle case of an axis (the point projects inside its edges):
+// num / den = (hi + r_hi)(r_lo - lo) / rho2.  Taken as a branch: the point
+// straddles few prisms, so most warps skip these products.
+HG_HD __forceinline__ void straddle_fix(EdgeSet& E, const double rho2[2][2]) {
+#pragma unroll
+  for (int p = 0; p < 2; p++)
+#pragma unroll
+    for (int s = 0; s < 2; s++) {
+      E.num[p][s] *= E.den[p][s];
+      E.den[p][s] = rho2[p][s];
+    }
+}
+
 // edges along x at (y_j, z_k)
 HG_HD __forceinline__ void edges_x(const Geom& g, EdgeSet& E) {
   const AxisCase c = axis_case(g.x[0], g.x[1]);
@@ -214,8 +231,15 @@ HG_HD __forceinline__ void edges_x(const Geom& g, EdgeSet& E) {
   for (int j = 0; j < 2; j++)
 #pragma unroll
     for (int k = 0; k < 2; k++)
-      edge_ratio(c, g.x[0], g.x[1], g.r[0][j][k], g.r[1][j][k], g.y2[j] + g.z2[k], E.num[j][k],
-                 E.den[j][k]);
+      edge_ratio(c, g.x[0], g.x[1], g.r[0][j][k], g.r[1][j][k], E.num[j][k], E.den[j][k]);
+  if (c.straddle) {
+    double rho2[2][2];
+#pragma unroll
+    for (int j = 0; j < 2; j++)
+#pragma unroll
+      for (int k = 0; k < 2; k++) rho2[j][k] = g.y2[j] + g.z2[k];
+    straddle_fix(E, rho2);
+  }
 }
 // edges along y at (x_i, z_k)
 HG_HD __forceinline__ void edges_y(const Geom& g, EdgeSet& E) {
@@ -224,8 +248,8 @@ HG_HD __forceinline__ void edges_y(const Geom& g, EdgeSet& E) {
   for (int i = 0; i < 2; i++)
 #pragma unroll
     for (int k = 0; k < 2; k++)
-      edge_ratio(c, g.y[0], g.y[1], g.r[i][0][k], g.r[i][1][k], g.xz2[i][k], E.num[i][k],
-                 E.den[i][k]);
+      edge_ratio(c, g.y[0], g.y[1], g.r[i][0][k], g.r[i][1][k], E.num[i][k], E.den[i][k]);
+  if (c.straddle) straddle_fix(E, g.xz2);
 }
 // edges along z at (x_i, y_j)
 HG_HD __forceinline__ void edges_z(const Geom& g, EdgeSet& E) {
@@ -234,8 +258,15 @@ HG_HD __forceinline__ void edges_z(const Geom& g, EdgeSet& E) {
   for (int i = 0; i < 2; i++)
 #pragma unroll
     for (int j = 0; j < 2; j++)
-      edge_ratio(c, g.z[0], g.z[1], g.r[i][j][0], g.r[i][j][1], g.x2[i] + g.y2[j], E.num[i][j],
-                 E.den[i][j]);
+      edge_ratio(c, g.z[0], g.z[1], g.r[i][j][0], g.r[i][j][1], E.num[i][j], E.den[i][j]);
+  if (c.straddle) {
+    double rho2[2][2];
+#pragma unroll
+    for (int i = 0; i < 2; i++)
+#pragma unroll
+      for (int j = 0; j < 2; j++) rho2[i][j] = g.x2[i] + g.y2[j];
+    straddle_fix(E, rho2);
+  }
 }
 
 // ln(R_a / R_b) with R = num / den: the difference of two edge logs as one log.
@@ -295,6 +326,91 @@ HG_HD __forceinline__ void pair_complex(double aa, double asq, double b1, double
   im = aa * c * d;
 }
 
+// Scales the complex number (re, im) by a power of two so that its larger
+// component is in [1, 2) (zero stays zero).
+HG_HD __forceinline__ void normalize_f2c(lean::F2& re, lean::F2& im) {
+  using namespace lean;
+  const int er = (int)((f2u(re.h) >> 23) & 0xffu), ei = (int)((f2u(im.h) >> 23) & 0xffu);
+  const int e = er > ei ? er : ei;
+  const float sc = u2f((unsigned)(254 - (e > 253 ? 253 : e)) << 23);  // 2^(127 - e)
+  re.h = fmul(re.h, sc);
+  re.l = fmul(re.l, sc);
+  im.h = fmul(im.h, sc);
+  im.l = fmul(im.l, sc);
+}
+
+// The same pair products on float pairs, for lengths scaled by a power of
+// two so that every product stays in the float range; bdq = bdiff (a^2+c^2).
+HG_HD __forceinline__ void pair_complex_f2(lean::F2 aa, lean::F2 asq, lean::F2 b1, lean::F2 b2,
+                                           lean::F2 c, lean::F2 csq, lean::F2 r1, lean::F2 r2,
+                                           bool same_sign, lean::F2 bdq, lean::F2& re,
+                                           lean::F2& im) {
+  using namespace lean;
+  re = f2_add(f2_mul(asq, f2_mul(r1, r2)), f2_mul(f2_mul(b1, b2), csq));
+  // same sign: den = b2 r1 + b1 r2 (one sign); straddle: d = b2 r1 - b1 r2
+  F2 x = f2_add(f2_mul(b2, r1), f2_mul(same_sign ? b1 : f2_neg(b1), r2));
+  F2 d = x;
+  if (same_sign) {
+    d = bdq;
+    if (x.h < 0.0f) {
+      x = f2_neg(x);
+      d = f2_neg(d);
+    }
+    re = f2_mul(re, x);
+  }
+  im = f2_mul(f2_mul(aa, c), d);
+}
+
+// Face angle on float pairs: every length is scaled by 2^-s, s the exponent
+// of the largest vertex distance of the face (the distances bound all
+// coordinates).  Returns false (and leaves o) when a nonzero coordinate or the
+// face width is below 2^-16 of that scale: then a product of up to six
+// scaled lengths could leave the normal float range, and the caller takes the
+// FP64 path (a point within ~1e-5 face sizes of an edge line or face plane).
+// A and B are each scaled by a power of two before the product A conj(B).
+HG_HD __forceinline__ bool face_angle_f2(double a, double b1, double b2, double c1, double c2,
+                                         double r11, double r12, double r21, double r22,
+                                         bool same_sign, double bdiff, const Tables& T,
+                                         double& o) {
+  using namespace lean;
+  const auto ex = [](double v) { return (int)((d2ll(v) >> 52) & 0x7ff); };
+  int top = ex(r11);
+  top = max(top, ex(r12));
+  top = max(top, ex(r21));
+  top = max(top, ex(r22));
+  const int lim = top - 16;
+  const auto small = [&](double v) { return !is_zero(v) && ex(v) < lim; };
+  if (small(a) || small(b1) || small(b2) || small(c1) || small(c2) || top >= 0x7fe ||
+      (same_sign && ex(bdiff) < 2 * lim - 1023))
+    return false;
+  const F2 fa = scaled_f2(d2ll(fabs(a)), top);
+  const F2 fb1 = scaled_f2(d2ll(b1), top), fb2 = scaled_f2(d2ll(b2), top);
+  const F2 fc1 = scaled_f2(d2ll(c1), top), fc2 = scaled_f2(d2ll(c2), top);
+  F2 asq = two_prod(fa.h, fa.h);
+  asq.l = ffma(2.0f * fa.h, fa.l, asq.l);
+  F2 c1sq = two_prod(fc1.h, fc1.h), c2sq = two_prod(fc2.h, fc2.h);
+  c1sq.l = ffma(2.0f * fc1.h, fc1.l, c1sq.l);
+  c2sq.l = ffma(2.0f * fc2.h, fc2.l, c2sq.l);
+  F2 bdq1{0.0f, 0.0f}, bdq2{0.0f, 0.0f};
+  if (same_sign) {
+    const F2 fbd = scaled_f2(d2ll(bdiff), 2 * top - 1023);
+    bdq1 = f2_mul(fbd, f2_add(asq, c1sq));
+    bdq2 = f2_mul(fbd, f2_add(asq, c2sq));
+  }
+  F2 ar, ai, br, bi;
+  pair_complex_f2(fa, asq, fb1, fb2, fc2, c2sq, scaled_f2(d2ll(r12), top),
+                  scaled_f2(d2ll(r22), top), same_sign, bdq2, ar, ai);
+  pair_complex_f2(fa, asq, fb1, fb2, fc1, c1sq, scaled_f2(d2ll(r11), top),
+                  scaled_f2(d2ll(r21), top), same_sign, bdq1, br, bi);
+  normalize_f2c(ar, ai);
+  normalize_f2c(br, bi);
+  const float est = atan2_f32(ai.h, ar.h) - atan2_f32(bi.h, br.h);
+  const F2 pr = f2_add(f2_mul(ar, br), f2_mul(ai, bi));
+  const F2 pim = f2_add(f2_mul(ai, br), f2_neg(f2_mul(ar, bi)));
+  o = lm_arg_near_f2(pr, pim, est, T);
+  return true;
+}
+
 template <bool LEAN>
 HG_HD __forceinline__ double face_angle(double a, bool upper, double b1, double b2, double c1,
                                         double c2, double r11, double r12, double r21, double r22,
@@ -303,15 +419,17 @@ HG_HD __forceinline__ double face_angle(double a, bool upper, double b1, double 
     int s = sgn(b2) * sgn(c2) + sgn(b1) * sgn(c1) - sgn(b1) * sgn(c2) - sgn(b2) * sgn(c1);
     return (upper ? -kHalfPi : kHalfPi) * (double)s;
   }
-  const double aa = fabs(a);
-  const double asq = a * a;
   const bool same_sign = !(is_neg(b1) && !is_nonpos(b2));
   const double bdiff = (b2 - b1) * (b2 + b1);
+  double o;
+  if (LEAN && face_angle_f2(a, b1, b2, c1, c2, r11, r12, r21, r22, same_sign, bdiff, T, o))
+    return is_neg(a) ? -o : o;
+  const double aa = fabs(a);
+  const double asq = a * a;
   // O = [arg c_{2,c2} - arg c_{1,c2}] - [arg c_{2,c1} - arg c_{1,c1}] = arg A - arg B
   double ar, ai, br, bi;
   pair_complex(aa, asq, b1, b2, c2, c2 * c2, r12, r22, same_sign, bdiff, ar, ai);
   pair_complex(aa, asq, b1, b2, c1, c1 * c1, r11, r21, same_sign, bdiff, br, bi);
-  double o;
   if (LEAN) {
     const float est = lean::arg_f32(ar, ai) - lean::arg_f32(br, bi);
     const double pr = fma(ar, br, ai * bi);
@@ -369,26 +487,34 @@ HG_HD __forceinline__ void pair_all(const Rel& q, const Tables& T, double out[kN
     Oy[a] = face_y<LEAN>(g, a, T);
     Oz[a] = face_z<LEAN>(g, a, T);
   }
-  const double s[2] = {-1.0, 1.0};
   double pot = 0.0, ge = 0.0, gn = 0.0, gz = 0.0;
 #pragma unroll
   for (int a = 0; a < 2; a++)
 #pragma unroll
     for (int b = 0; b < 2; b++) {
-      const double sab = s[a] * s[b];
-      // Lx[j][k], Ly[i][k], Lz[i][j]
-      pot += sab * (cmul(g.x[a] * g.y[b], Lz[a][b]) + cmul(g.y[a] * g.z[b], Lx[a][b]) +
-                    cmul(g.z[b] * g.x[a], Ly[a][b]));
-      ge += sab * (cmul(g.y[b], Lz[a][b]) + cmul(g.z[b], Ly[a][b]));
-      gn += sab * (cmul(g.z[b], Lx[a][b]) + cmul(g.x[a], Lz[a][b]));
-      gz += sab * (cmul(g.x[a], Ly[a][b]) + cmul(g.y[a], Lx[a][b]));
+      // s_a s_b times the coefficient; Lx[j][k], Ly[i][k], Lz[i][j]
+      const bool pos = a == b;
+      const double xa = pos ? g.x[a] : -g.x[a], ya = pos ? g.y[a] : -g.y[a];
+      pot = cfma(xa * g.y[b], Lz[a][b], pot);
+      pot = cfma(ya * g.z[b], Lx[a][b], pot);
+      pot = cfma(xa * g.z[b], Ly[a][b], pot);
+      ge = cfma(pos ? g.y[b] : -g.y[b], Lz[a][b], ge);
+      ge = cfma(pos ? g.z[b] : -g.z[b], Ly[a][b], ge);
+      gn = cfma(pos ? g.z[b] : -g.z[b], Lx[a][b], gn);
+      gn = cfma(xa, Lz[a][b], gn);
+      gz = cfma(xa, Ly[a][b], gz);
+      gz = cfma(ya, Lx[a][b], gz);
     }
 #pragma unroll
   for (int a = 0; a < 2; a++) {
-    pot -= 0.5 * s[a] * (cmul(g.x2[a], Ox[a]) + cmul(g.y2[a], Oy[a]) + cmul(g.z2[a], Oz[a]));
-    ge -= s[a] * cmul(g.x[a], Ox[a]);
-    gn -= s[a] * cmul(g.y[a], Oy[a]);
-    gz -= s[a] * cmul(g.z[a], Oz[a]);
+    // -s_a (pot: -s_a / 2)
+    const double m = a ? -1.0 : 1.0;
+    pot = cfma(0.5 * m * g.x2[a], Ox[a], pot);
+    pot = cfma(0.5 * m * g.y2[a], Oy[a], pot);
+    pot = cfma(0.5 * m * g.z2[a], Oz[a], pot);
+    ge = cfma(a ? -g.x[a] : g.x[a], Ox[a], ge);
+    gn = cfma(a ? -g.y[a] : g.y[a], Oy[a], gn);
+    gz = cfma(a ? -g.z[a] : g.z[a], Oz[a], gz);
   }
   out[kPotential] = pot;
   out[kGe] = ge;
@@ -421,12 +547,13 @@ HG_HD __forceinline__ double pair_field(const Rel& q, const Tables& T) {
     double v = 0.0;
 #pragma unroll
     for (int a = 0; a < 2; a++) {
-      const double s = a ? 1.0 : -1.0;
-      v += s * cmul(g.x[a], log_ratio2<LEAN>(Ey.num[a][1], Ey.den[a][1], Ey.num[a][0],
-                                             Ey.den[a][0], T));
-      v += s * cmul(g.y[a], log_ratio2<LEAN>(Ex.num[a][1], Ex.den[a][1], Ex.num[a][0],
-                                             Ex.den[a][0], T));
-      v -= s * cmul(g.z[a], face_z<LEAN>(g, a, T));
+      const double sx = a ? g.x[a] : -g.x[a], sy = a ? g.y[a] : -g.y[a];
+      const double sz = a ? -g.z[a] : g.z[a];
+      v = cfma(sx, log_ratio2<LEAN>(Ey.num[a][1], Ey.den[a][1], Ey.num[a][0], Ey.den[a][0], T),
+               v);
+      v = cfma(sy, log_ratio2<LEAN>(Ex.num[a][1], Ex.den[a][1], Ex.num[a][0], Ex.den[a][0], T),
+               v);
+      v = cfma(sz, face_z<LEAN>(g, a, T), v);
     }
     return v;
   } else if (F == kGe) {
@@ -438,12 +565,13 @@ HG_HD __forceinline__ double pair_field(const Rel& q, const Tables& T) {
     double v = 0.0;
 #pragma unroll
     for (int a = 0; a < 2; a++) {
-      const double s = a ? 1.0 : -1.0;
-      v += s * cmul(g.y[a], log_ratio2<LEAN>(Ez.num[1][a], Ez.den[1][a], Ez.num[0][a],
-                                             Ez.den[0][a], T));
-      v += s * cmul(g.z[a], log_ratio2<LEAN>(Ey.num[1][a], Ey.den[1][a], Ey.num[0][a],
-                                             Ey.den[0][a], T));
-      v -= s * cmul(g.x[a], face_x<LEAN>(g, a, T));
+      const double sy = a ? g.y[a] : -g.y[a], sz = a ? g.z[a] : -g.z[a];
+      const double sx = a ? -g.x[a] : g.x[a];
+      v = cfma(sy, log_ratio2<LEAN>(Ez.num[1][a], Ez.den[1][a], Ez.num[0][a], Ez.den[0][a], T),
+               v);
+      v = cfma(sz, log_ratio2<LEAN>(Ey.num[1][a], Ey.den[1][a], Ey.num[0][a], Ey.den[0][a], T),
+               v);
+      v = cfma(sx, face_x<LEAN>(g, a, T), v);
     }
     return v;
   } else if (F == kGn) {
@@ -455,12 +583,13 @@ HG_HD __forceinline__ double pair_field(const Rel& q, const Tables& T) {
     double v = 0.0;
 #pragma unroll
     for (int a = 0; a < 2; a++) {
-      const double s = a ? 1.0 : -1.0;
-      v += s * cmul(g.z[a], log_ratio2<LEAN>(Ex.num[1][a], Ex.den[1][a], Ex.num[0][a],
-                                             Ex.den[0][a], T));
-      v += s * cmul(g.x[a], log_ratio2<LEAN>(Ez.num[a][1], Ez.den[a][1], Ez.num[a][0],
-                                             Ez.den[a][0], T));
-      v -= s * cmul(g.y[a], face_y<LEAN>(g, a, T));
+      const double sz = a ? g.z[a] : -g.z[a], sx = a ? g.x[a] : -g.x[a];
+      const double sy = a ? -g.y[a] : g.y[a];
+      v = cfma(sz, log_ratio2<LEAN>(Ex.num[1][a], Ex.den[1][a], Ex.num[0][a], Ex.den[0][a], T),
+               v);
+      v = cfma(sx, log_ratio2<LEAN>(Ez.num[a][1], Ez.den[a][1], Ez.num[a][0], Ez.den[a][0], T),
+               v);
+      v = cfma(sy, face_y<LEAN>(g, a, T), v);
     }
     return v;
   } else if (F == kGee) {
@@ -519,14 +648,12 @@ HG_HD __forceinline__ double pair_gz_faces(const Rel& q, const Tables& T, double
   double v = 0.0;
 #pragma unroll
   for (int a = 0; a < 2; a++) {
-    const double s = a ? 1.0 : -1.0;
-    v += s * cmul(g.x[a], log_ratio2<LEAN>(Ey.num[a][1], Ey.den[a][1], Ey.num[a][0],
-                                           Ey.den[a][0], T));
-    v += s * cmul(g.y[a], log_ratio2<LEAN>(Ex.num[a][1], Ex.den[a][1], Ex.num[a][0],
-                                           Ex.den[a][0], T));
+    const double sx = a ? g.x[a] : -g.x[a], sy = a ? g.y[a] : -g.y[a];
+    v = cfma(sx, log_ratio2<LEAN>(Ey.num[a][1], Ey.den[a][1], Ey.num[a][0], Ey.den[a][0], T), v);
+    v = cfma(sy, log_ratio2<LEAN>(Ex.num[a][1], Ex.den[a][1], Ex.num[a][0], Ex.den[a][0], T), v);
   }
-  v -= cmul(g.z[1], o_top) - cmul(g.z[0], o_bottom);
-  return v;
+  v = cfma(-g.z[1], o_top, v);
+  return cfma(g.z[0], o_bottom, v);
 }
 
 }  // namespace hg
