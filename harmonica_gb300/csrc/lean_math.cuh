@@ -494,11 +494,16 @@ HG_HD __forceinline__ double lm_log_quot(double p1, double p2, double q1, double
   const bool near1 = (E == 0) && (k == 64);
   if (!near1 && (E > 1000 || E < -1000)) return log((ONE_FACTOR ? p1 : p1 * p2) / d);
   // numerator p1 p2 c_k 2^-E - q1 q2, exact when c_k 2^-E = 1
-  const double cp = near1 ? 1.0 : ll2d(d2ll(T.logc[k]) - ((long long)E << 52));
-  const double num = ONE_FACTOR ? fma(p1, cp, -d) : fma(p1, p2 * cp, -d);
+  double num;
+  if (near1) {
+    num = ONE_FACTOR ? p1 - d : fma(p1, p2, -d);
+  } else {
+    const double cp = ll2d(d2ll(T.logc[k]) - ((long long)E << 52));  // c_k 2^-E, exact
+    num = fma(ONE_FACTOR ? p1 : p1 * p2, cp, -d);
+  }
   const long long bn = d2ll(num);
-  const int en = (int)((bn >> 52) & 0x7ff);
-  if (en == 0x7ff || (en == 0 && (bn << 1) != 0)) return log((ONE_FACTOR ? p1 : p1 * p2) / d);
+  const int en = (int)((bn >> 52) & 0x7ff);  // 0: zero or subnormal, counted as t = 0
+  if (en == 0x7ff) return log((ONE_FACTOR ? p1 : p1 * p2) / d);
   // t = num / d: significands divided as pairs, scaled by 2^(en - ed)
   F2 t = f2_div(mant_f2(bn), mant_f2(bd));
   const int sc = en - ed;

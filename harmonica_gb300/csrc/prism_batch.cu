@@ -23,6 +23,11 @@
 
 namespace hg {
 
+// Resident CTAs per SM for the persistent kernels: they dispatch every field
+// at run time, so the register budget is set by the heaviest (the potential,
+// all 12 logs and 6 face angles); 4 CTAs fit it without spills.
+constexpr int kBatchMinBlocks = 4;
+
 int set_error(int code, const std::string& msg);
 int cuda_check(cudaError_t e, const char* what);
 
@@ -69,7 +74,7 @@ __device__ __forceinline__ void run_item(const ProblemDev& P, const WorkItem& w,
   if (active) part[P.part_offset + (int64_t)w.chunk * P.n_obs + i] = acc[0];
 }
 
-__global__ void __launch_bounds__(kThreads) batch_kernel(const ProblemDev* __restrict__ probs,
+__global__ void __launch_bounds__(kThreads, kBatchMinBlocks) batch_kernel(const ProblemDev* __restrict__ probs,
                                                          const WorkItem* __restrict__ items,
                                                          int64_t n_items,
                                                          unsigned long long* __restrict__ counter,
@@ -323,7 +328,7 @@ __device__ __forceinline__ void run_plan_item(const hg_problem_plan& P, const hg
   if (active) P.partials[(int64_t)w.chunk * P.n_obs + i] = acc[0];
 }
 
-__global__ void __launch_bounds__(kThreads) round_kernel(const hg_problem_plan* __restrict__ probs,
+__global__ void __launch_bounds__(kThreads, kBatchMinBlocks) round_kernel(const hg_problem_plan* __restrict__ probs,
                                                          const hg_work_item* __restrict__ items,
                                                          int64_t n_items,
                                                          unsigned long long* __restrict__ counter) {

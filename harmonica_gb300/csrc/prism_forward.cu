@@ -38,10 +38,13 @@ int cuda_check(cudaError_t e, const char* what) {
 // code hides its latency with more warps; the fused all-field kernel needs
 // more registers).
 #ifndef HG_FWD_MIN_BLOCKS
-#define HG_FWD_MIN_BLOCKS 4
+#define HG_FWD_MIN_BLOCKS 6
+#endif
+#ifndef HG_FWD_MIN_BLOCKS_ALL
+#define HG_FWD_MIN_BLOCKS_ALL 4
 #endif
 template <int F> struct MinBlocks { static constexpr int value = HG_FWD_MIN_BLOCKS; };
-template <> struct MinBlocks<kAll> { static constexpr int value = 3; };
+template <> struct MinBlocks<kAll> { static constexpr int value = HG_FWD_MIN_BLOCKS_ALL; };
 
 // out_mask: for kAll, which of the ten fields are written (compact rows).
 template <int F, class Source>

@@ -86,11 +86,43 @@ HG_HD __forceinline__ int sgn(double v) {
   return is_zero(v) ? 0 : (bits_of(v) < 0 ? -1 : 1);
 }
 
+// Predicates and sign operations on the high word only.  An exact test of all
+// 64 bits for zero is compiled into an FP64 compare (a slow-pipe
+// instruction); these stay integer.  is_tiny is true for zero AND subnormal
+// values: used only where a subnormal length behaves as zero within rounding
+// (the exact predicates above decide the singular points).
+HG_HD __forceinline__ unsigned hi_word(double v) {
+  return (unsigned)((unsigned long long)bits_of(v) >> 32);
+}
+HG_HD __forceinline__ bool is_tiny(double v) { return (hi_word(v) & 0x7ff00000u) == 0; }
+HG_HD __forceinline__ bool sign_bit(double v) { return (int)hi_word(v) < 0; }
+HG_HD __forceinline__ bool neg_not_tiny(double v) { return sign_bit(v) && !is_tiny(v); }
+HG_HD __forceinline__ bool nonpos_or_tiny(double v) { return sign_bit(v) || is_tiny(v); }
+constexpr long long kSignBit = (long long)0x8000000000000000ULL;
+HG_HD __forceinline__ double flip_sign(double v) { return lean::ll2d(bits_of(v) ^ kSignBit); }
+HG_HD __forceinline__ double abs_bits(double v) { return lean::ll2d(bits_of(v) & ~kSignBit); }
+// v with its sign flipped where s is negative
+HG_HD __forceinline__ double times_sign_of(double v, double s) {
+  return lean::ll2d(bits_of(v) ^ (bits_of(s) & kSignBit));
+}
+
 // Multiply a log/angle by a coefficient, with the limit 0 * (singular) = 0.
-HG_HD __forceinline__ double cmul(double coef, double v) { return is_zero(coef) ? 0.0 : coef * v; }
+HG_HD __forceinline__ double cmul(double coef, double v) { return is_tiny(coef) ? 0.0 : coef * v; }
 // acc + coef * v with the same limit (one FMA)
 HG_HD __forceinline__ double cfma(double coef, double v, double acc) {
-  return fma(coef, is_zero(coef) ? 0.0 : v, acc);
+  return fma(coef, is_tiny(coef) ? 0.0 : v, acc);
+}
+// acc + (NEG ? -coef : coef) * v: the sign folds into the FMA operand (a
+// negated coefficient tested as bits would cost an FP64 negation)
+template <bool NEG>
+HG_HD __forceinline__ double cfma_s(double coef, double v, double acc) {
+  const double w = is_tiny(coef) ? 0.0 : v;
+  return NEG ? fma(-coef, w, acc) : fma(coef, w, acc);
+}
+// the same with the sign as an argument (a constant after loop unrolling)
+HG_HD __forceinline__ double cfma_sgn(double coef, bool neg, double v, double acc) {
+  const double w = is_tiny(coef) ? 0.0 : v;
+  return neg ? fma(-coef, w, acc) : fma(coef, w, acc);
 }
 
 template <bool LEAN> struct Math;
@@ -188,8 +220,8 @@ struct AxisCase {
 
 HG_HD __forceinline__ AxisCase axis_case(double a1, double a2) {
   AxisCase c;
-  c.reflect = is_nonpos(a2);
-  c.straddle = is_neg(c.reflect ? -a2 : a1);
+  c.reflect = nonpos_or_tiny(a2);
+  c.straddle = neg_not_tiny(c.reflect ? flip_sign(a2) : a1);
   return c;
 }
 
@@ -197,8 +229,8 @@ HG_HD __forceinline__ AxisCase axis_case(double a1, double a2) {
 // den = |lo| + r_lo (lo + r_lo, or r_lo - lo when lo < 0).
 HG_HD __forceinline__ void edge_ratio(AxisCase c, double a1, double a2, double r1, double r2,
                                       double& num, double& den) {
-  const double lo = c.reflect ? -a2 : a1;
-  const double hi = c.reflect ? -a1 : a2;
+  const double lo = c.reflect ? flip_sign(a2) : a1;
+  const double hi = c.reflect ? flip_sign(a1) : a2;
   const double rlo = c.reflect ? r2 : r1;
   const double rhi = c.reflect ? r1 : r2;
   den = fabs(lo) + rlo;
@@ -370,20 +402,20 @@ HG_HD __forceinline__ void pair_complex_f2(lean::F2 aa, lean::F2 asq, lean::F2 b
 // A and B are each scaled by a power of two before the product A conj(B).
 HG_HD __forceinline__ bool face_angle_f2(double a, double b1, double b2, double c1, double c2,
                                          double r11, double r12, double r21, double r22,
-                                         bool same_sign, double bdiff, const Tables& T,
+                                         bool same_sign, double width, const Tables& T,
                                          double& o) {
   using namespace lean;
-  const auto ex = [](double v) { return (int)((d2ll(v) >> 52) & 0x7ff); };
+  const auto ex = [](double v) { return (int)((hi_word(v) >> 20) & 0x7ffu); };
   int top = ex(r11);
   top = max(top, ex(r12));
   top = max(top, ex(r21));
   top = max(top, ex(r22));
   const int lim = top - 16;
-  const auto small = [&](double v) { return !is_zero(v) && ex(v) < lim; };
+  const auto small = [&](double v) { return !is_tiny(v) && ex(v) < lim; };
   if (small(a) || small(b1) || small(b2) || small(c1) || small(c2) || top >= 0x7fe ||
-      (same_sign && ex(bdiff) < 2 * lim - 1023))
+      ex(width) < lim)
     return false;
-  const F2 fa = scaled_f2(d2ll(fabs(a)), top);
+  const F2 fa = scaled_f2(d2ll(abs_bits(a)), top);
   const F2 fb1 = scaled_f2(d2ll(b1), top), fb2 = scaled_f2(d2ll(b2), top);
   const F2 fc1 = scaled_f2(d2ll(c1), top), fc2 = scaled_f2(d2ll(c2), top);
   F2 asq = two_prod(fa.h, fa.h);
@@ -393,7 +425,9 @@ HG_HD __forceinline__ bool face_angle_f2(double a, double b1, double b2, double 
   c2sq.l = ffma(2.0f * fc2.h, fc2.l, c2sq.l);
   F2 bdq1{0.0f, 0.0f}, bdq2{0.0f, 0.0f};
   if (same_sign) {
-    const F2 fbd = scaled_f2(d2ll(bdiff), 2 * top - 1023);
+    // bdiff = (b2 - b1)(b2 + b1): the width from FP64 (no cancellation), the
+    // same-sign sum on pairs
+    const F2 fbd = f2_mul(scaled_f2(d2ll(width), top), f2_add(fb2, fb1));
     bdq1 = f2_mul(fbd, f2_add(asq, c1sq));
     bdq2 = f2_mul(fbd, f2_add(asq, c2sq));
   }
@@ -411,19 +445,20 @@ HG_HD __forceinline__ bool face_angle_f2(double a, double b1, double b2, double 
   return true;
 }
 
+// width = b2 - b1 (shared by the two faces normal to one axis).
 template <bool LEAN>
 HG_HD __forceinline__ double face_angle(double a, bool upper, double b1, double b2, double c1,
                                         double c2, double r11, double r12, double r21, double r22,
-                                        const Tables& T) {
-  if (is_zero(a)) {
+                                        double width, const Tables& T) {
+  if (is_tiny(a)) {
     int s = sgn(b2) * sgn(c2) + sgn(b1) * sgn(c1) - sgn(b1) * sgn(c2) - sgn(b2) * sgn(c1);
     return (upper ? -kHalfPi : kHalfPi) * (double)s;
   }
-  const bool same_sign = !(is_neg(b1) && !is_nonpos(b2));
-  const double bdiff = (b2 - b1) * (b2 + b1);
+  const bool same_sign = !(neg_not_tiny(b1) && !nonpos_or_tiny(b2));
   double o;
-  if (LEAN && face_angle_f2(a, b1, b2, c1, c2, r11, r12, r21, r22, same_sign, bdiff, T, o))
-    return is_neg(a) ? -o : o;
+  if (LEAN && face_angle_f2(a, b1, b2, c1, c2, r11, r12, r21, r22, same_sign, width, T, o))
+    return times_sign_of(o, a);
+  const double bdiff = width * (b2 + b1);
   const double aa = fabs(a);
   const double asq = a * a;
   // O = [arg c_{2,c2} - arg c_{1,c2}] - [arg c_{2,c1} - arg c_{1,c1}] = arg A - arg B
@@ -438,26 +473,26 @@ HG_HD __forceinline__ double face_angle(double a, bool upper, double b1, double 
   } else {
     o = atan2(ai, ar) - atan2(bi, br);
   }
-  return is_neg(a) ? -o : o;
+  return times_sign_of(o, a);
 }
 
 template <bool LEAN>
 HG_HD __forceinline__ double face_x(const Geom& g, int i, const Tables& T) {
   // in-plane (y_j, z_k), r[i][j][k]
   return face_angle<LEAN>(g.x[i], i == 1, g.y[0], g.y[1], g.z[0], g.z[1], g.r[i][0][0],
-                          g.r[i][0][1], g.r[i][1][0], g.r[i][1][1], T);
+                          g.r[i][0][1], g.r[i][1][0], g.r[i][1][1], g.y[1] - g.y[0], T);
 }
 template <bool LEAN>
 HG_HD __forceinline__ double face_y(const Geom& g, int j, const Tables& T) {
   // in-plane (x_i, z_k), r[i][j][k]
   return face_angle<LEAN>(g.y[j], j == 1, g.x[0], g.x[1], g.z[0], g.z[1], g.r[0][j][0],
-                          g.r[0][j][1], g.r[1][j][0], g.r[1][j][1], T);
+                          g.r[0][j][1], g.r[1][j][0], g.r[1][j][1], g.x[1] - g.x[0], T);
 }
 template <bool LEAN>
 HG_HD __forceinline__ double face_z(const Geom& g, int k, const Tables& T) {
   // in-plane (x_i, y_j), r[i][j][k]
   return face_angle<LEAN>(g.z[k], k == 1, g.x[0], g.x[1], g.y[0], g.y[1], g.r[0][0][k],
-                          g.r[0][1][k], g.r[1][0][k], g.r[1][1][k], T);
+                          g.r[0][1][k], g.r[1][0][k], g.r[1][1][k], g.x[1] - g.x[0], T);
 }
 
 // ---------------------------------------------------------------------------
@@ -492,29 +527,28 @@ HG_HD __forceinline__ void pair_all(const Rel& q, const Tables& T, double out[kN
   for (int a = 0; a < 2; a++)
 #pragma unroll
     for (int b = 0; b < 2; b++) {
-      // s_a s_b times the coefficient; Lx[j][k], Ly[i][k], Lz[i][j]
-      const bool pos = a == b;
-      const double xa = pos ? g.x[a] : -g.x[a], ya = pos ? g.y[a] : -g.y[a];
-      pot = cfma(xa * g.y[b], Lz[a][b], pot);
-      pot = cfma(ya * g.z[b], Lx[a][b], pot);
-      pot = cfma(xa * g.z[b], Ly[a][b], pot);
-      ge = cfma(pos ? g.y[b] : -g.y[b], Lz[a][b], ge);
-      ge = cfma(pos ? g.z[b] : -g.z[b], Ly[a][b], ge);
-      gn = cfma(pos ? g.z[b] : -g.z[b], Lx[a][b], gn);
-      gn = cfma(xa, Lz[a][b], gn);
-      gz = cfma(xa, Ly[a][b], gz);
-      gz = cfma(ya, Lx[a][b], gz);
+      // s_a s_b = +1 when a == b; Lx[j][k], Ly[i][k], Lz[i][j]
+      const bool ng = a != b;
+      pot = cfma_sgn(g.x[a] * g.y[b], ng, Lz[a][b], pot);
+      pot = cfma_sgn(g.y[a] * g.z[b], ng, Lx[a][b], pot);
+      pot = cfma_sgn(g.x[a] * g.z[b], ng, Ly[a][b], pot);
+      ge = cfma_sgn(g.y[b], ng, Lz[a][b], ge);
+      ge = cfma_sgn(g.z[b], ng, Ly[a][b], ge);
+      gn = cfma_sgn(g.z[b], ng, Lx[a][b], gn);
+      gn = cfma_sgn(g.x[a], ng, Lz[a][b], gn);
+      gz = cfma_sgn(g.x[a], ng, Ly[a][b], gz);
+      gz = cfma_sgn(g.y[a], ng, Lx[a][b], gz);
     }
 #pragma unroll
   for (int a = 0; a < 2; a++) {
-    // -s_a (pot: -s_a / 2)
-    const double m = a ? -1.0 : 1.0;
-    pot = cfma(0.5 * m * g.x2[a], Ox[a], pot);
-    pot = cfma(0.5 * m * g.y2[a], Oy[a], pot);
-    pot = cfma(0.5 * m * g.z2[a], Oz[a], pot);
-    ge = cfma(a ? -g.x[a] : g.x[a], Ox[a], ge);
-    gn = cfma(a ? -g.y[a] : g.y[a], Oy[a], gn);
-    gz = cfma(a ? -g.z[a] : g.z[a], Oz[a], gz);
+    // face terms carry -s_a (potential: -s_a / 2)
+    const bool ng = a == 1;
+    pot = cfma_sgn(0.5 * g.x2[a], ng, Ox[a], pot);
+    pot = cfma_sgn(0.5 * g.y2[a], ng, Oy[a], pot);
+    pot = cfma_sgn(0.5 * g.z2[a], ng, Oz[a], pot);
+    ge = cfma_sgn(g.x[a], ng, Ox[a], ge);
+    gn = cfma_sgn(g.y[a], ng, Oy[a], gn);
+    gz = cfma_sgn(g.z[a], ng, Oz[a], gz);
   }
   out[kPotential] = pot;
   out[kGe] = ge;
@@ -545,16 +579,19 @@ HG_HD __forceinline__ double pair_field(const Rel& q, const Tables& T) {
     edges_y(g, Ey);
     edges_x(g, Ex);
     double v = 0.0;
-#pragma unroll
-    for (int a = 0; a < 2; a++) {
-      const double sx = a ? g.x[a] : -g.x[a], sy = a ? g.y[a] : -g.y[a];
-      const double sz = a ? -g.z[a] : g.z[a];
-      v = cfma(sx, log_ratio2<LEAN>(Ey.num[a][1], Ey.den[a][1], Ey.num[a][0], Ey.den[a][0], T),
-               v);
-      v = cfma(sy, log_ratio2<LEAN>(Ex.num[a][1], Ex.den[a][1], Ex.num[a][0], Ex.den[a][0], T),
-               v);
-      v = cfma(sz, face_z<LEAN>(g, a, T), v);
-    }
+    // s_a x_a L^y_a + s_a y_a L^x_a - s_a z_a O_a, s_0 = -1, s_1 = +1
+    const auto ly = [&](int a) {
+      return log_ratio2<LEAN>(Ey.num[a][1], Ey.den[a][1], Ey.num[a][0], Ey.den[a][0], T);
+    };
+    const auto lx = [&](int a) {
+      return log_ratio2<LEAN>(Ex.num[a][1], Ex.den[a][1], Ex.num[a][0], Ex.den[a][0], T);
+    };
+    v = cfma_s<true>(g.x[0], ly(0), v);
+    v = cfma_s<false>(g.x[1], ly(1), v);
+    v = cfma_s<true>(g.y[0], lx(0), v);
+    v = cfma_s<false>(g.y[1], lx(1), v);
+    v = cfma_s<false>(g.z[0], face_z<LEAN>(g, 0, T), v);
+    v = cfma_s<true>(g.z[1], face_z<LEAN>(g, 1, T), v);
     return v;
   } else if (F == kGe) {
     // sum_j s_j y_j sum_i s_i Lz[i][j] + sum_k s_k z_k sum_i s_i Ly[i][k]
@@ -563,16 +600,18 @@ HG_HD __forceinline__ double pair_field(const Rel& q, const Tables& T) {
     edges_z(g, Ez);
     edges_y(g, Ey);
     double v = 0.0;
-#pragma unroll
-    for (int a = 0; a < 2; a++) {
-      const double sy = a ? g.y[a] : -g.y[a], sz = a ? g.z[a] : -g.z[a];
-      const double sx = a ? -g.x[a] : g.x[a];
-      v = cfma(sy, log_ratio2<LEAN>(Ez.num[1][a], Ez.den[1][a], Ez.num[0][a], Ez.den[0][a], T),
-               v);
-      v = cfma(sz, log_ratio2<LEAN>(Ey.num[1][a], Ey.den[1][a], Ey.num[0][a], Ey.den[0][a], T),
-               v);
-      v = cfma(sx, face_x<LEAN>(g, a, T), v);
-    }
+    const auto lz = [&](int a) {
+      return log_ratio2<LEAN>(Ez.num[1][a], Ez.den[1][a], Ez.num[0][a], Ez.den[0][a], T);
+    };
+    const auto ly = [&](int a) {
+      return log_ratio2<LEAN>(Ey.num[1][a], Ey.den[1][a], Ey.num[0][a], Ey.den[0][a], T);
+    };
+    v = cfma_s<true>(g.y[0], lz(0), v);
+    v = cfma_s<false>(g.y[1], lz(1), v);
+    v = cfma_s<true>(g.z[0], ly(0), v);
+    v = cfma_s<false>(g.z[1], ly(1), v);
+    v = cfma_s<false>(g.x[0], face_x<LEAN>(g, 0, T), v);
+    v = cfma_s<true>(g.x[1], face_x<LEAN>(g, 1, T), v);
     return v;
   } else if (F == kGn) {
     // sum_k s_k z_k sum_j s_j Lx[j][k] + sum_i s_i x_i sum_j s_j Lz[i][j]
@@ -581,16 +620,18 @@ HG_HD __forceinline__ double pair_field(const Rel& q, const Tables& T) {
     edges_x(g, Ex);
     edges_z(g, Ez);
     double v = 0.0;
-#pragma unroll
-    for (int a = 0; a < 2; a++) {
-      const double sz = a ? g.z[a] : -g.z[a], sx = a ? g.x[a] : -g.x[a];
-      const double sy = a ? -g.y[a] : g.y[a];
-      v = cfma(sz, log_ratio2<LEAN>(Ex.num[1][a], Ex.den[1][a], Ex.num[0][a], Ex.den[0][a], T),
-               v);
-      v = cfma(sx, log_ratio2<LEAN>(Ez.num[a][1], Ez.den[a][1], Ez.num[a][0], Ez.den[a][0], T),
-               v);
-      v = cfma(sy, face_y<LEAN>(g, a, T), v);
-    }
+    const auto lx = [&](int a) {
+      return log_ratio2<LEAN>(Ex.num[1][a], Ex.den[1][a], Ex.num[0][a], Ex.den[0][a], T);
+    };
+    const auto lz = [&](int a) {
+      return log_ratio2<LEAN>(Ez.num[a][1], Ez.den[a][1], Ez.num[a][0], Ez.den[a][0], T);
+    };
+    v = cfma_s<true>(g.z[0], lx(0), v);
+    v = cfma_s<false>(g.z[1], lx(1), v);
+    v = cfma_s<true>(g.x[0], lz(0), v);
+    v = cfma_s<false>(g.x[1], lz(1), v);
+    v = cfma_s<false>(g.y[0], face_y<LEAN>(g, 0, T), v);
+    v = cfma_s<true>(g.y[1], face_y<LEAN>(g, 1, T), v);
     return v;
   } else if (F == kGee) {
     return -(face_x<LEAN>(g, 1, T) - face_x<LEAN>(g, 0, T));
@@ -645,15 +686,19 @@ HG_HD __forceinline__ double pair_gz_faces(const Rel& q, const Tables& T, double
   edges_x(g, Ex);
   o_bottom = face_z<LEAN>(g, 0, T);
   o_top = face_z<LEAN>(g, 1, T);
+  const auto ly = [&](int a) {
+    return log_ratio2<LEAN>(Ey.num[a][1], Ey.den[a][1], Ey.num[a][0], Ey.den[a][0], T);
+  };
+  const auto lx = [&](int a) {
+    return log_ratio2<LEAN>(Ex.num[a][1], Ex.den[a][1], Ex.num[a][0], Ex.den[a][0], T);
+  };
   double v = 0.0;
-#pragma unroll
-  for (int a = 0; a < 2; a++) {
-    const double sx = a ? g.x[a] : -g.x[a], sy = a ? g.y[a] : -g.y[a];
-    v = cfma(sx, log_ratio2<LEAN>(Ey.num[a][1], Ey.den[a][1], Ey.num[a][0], Ey.den[a][0], T), v);
-    v = cfma(sy, log_ratio2<LEAN>(Ex.num[a][1], Ex.den[a][1], Ex.num[a][0], Ex.den[a][0], T), v);
-  }
-  v = cfma(-g.z[1], o_top, v);
-  return cfma(g.z[0], o_bottom, v);
+  v = cfma_s<true>(g.x[0], ly(0), v);
+  v = cfma_s<false>(g.x[1], ly(1), v);
+  v = cfma_s<true>(g.y[0], lx(0), v);
+  v = cfma_s<false>(g.y[1], lx(1), v);
+  v = cfma_s<true>(g.z[1], o_top, v);
+  return cfma_s<false>(g.z[0], o_bottom, v);
 }
 
 }  // namespace hg
