@@ -117,13 +117,39 @@ HG_HD __forceinline__ int round_to_int(float x) {
   return (int)std::nearbyint(x);
 #endif
 }
-HG_HD __forceinline__ float atan2_f32(float y, float x) {
-#ifdef __CUDA_ARCH__
-  return atan2f(y, x);
-#else
-  return std::atan2(y, x);
-#endif
+// FP32 estimate of atan2(y, x) within ~2e-5 rad, for branch selection only:
+// arctan on [0, 1] by an odd degree-9 polynomial (least-squares fit on
+// Chebyshev nodes, max error 1.2e-5) and the octant symmetries, with the
+// sign of y (signed zeros included) as atan2.  (0, 0) gives 0.
+HG_HD __forceinline__ float atan2_est(float y, float x) {
+  const float ax = fabsf(x), ay = fabsf(y);
+  const float mx = fmaxf(ax, ay), mn = fminf(ax, ay);
+  const float t = mn * rcp_approx(mx);
+  const float t2 = t * t;
+  float p = fmaf(t2, fmaf(t2, fmaf(t2, fmaf(t2, 0.0208451133f, -0.0851563513f), 0.180159301f),
+                          -0.330304801f),
+                 0.999866307f) *
+            t;
+  p = ay > ax ? 1.57079637f - p : p;
+  p = (f2u(x) >> 31) ? 3.14159274f - p : p;
+  p = (f2u(y) >> 31) ? -p : p;
+  return mx == 0.0f ? 0.0f : p;
 }
+
+// Generic library functions for the inputs outside the fast paths, kept out
+// of line: inlined, their code would sit between the hot instructions of every
+// call site and crowd the instruction cache.
+#ifdef __CUDA_ARCH__
+#define HG_COLD __device__ __noinline__
+#else
+#define HG_COLD inline
+#endif
+HG_COLD double cold_sqrt(double x) { return sqrt(x); }
+HG_COLD double cold_rsqrt(double x) { return 1.0 / sqrt(x); }
+HG_COLD double cold_div(double n, double d) { return n / d; }
+HG_COLD double cold_log(double x) { return log(x); }
+HG_COLD double cold_log_quot(double p, double d) { return log(p / d); }
+HG_COLD double cold_atan2(double y, double x) { return atan2(y, x); }
 
 // double -> float by truncating the mantissa, with the exponent lowered by
 // (shift - 1023): an integer-pipe conversion (no FP64 instruction).  Values
@@ -275,9 +301,33 @@ HG_HD __forceinline__ F2 scaled_f2(long long b, int top) {
   return (ef == 0 || k < -120) ? F2{0.0f, 0.0f} : m;
 }
 
-// The pair as a double times 2^k (one FP64 add).
+// The pair as a double times 2^k, assembled with integer instructions: the
+// 24-bit significand of h widened to 53 bits, the significand of l shifted
+// into its place and added or subtracted, one normalisation step.  For
+// |l| <= 2^-8 |h| (all pairs built here) and results in the normal double
+// range; within 1 ulp (the bits of l below the double's last place are
+// truncated).  A zero h gives l alone.
 HG_HD __forceinline__ double f2_to_double(F2 a, int k) {
-  return f2d_scaled(a.h, k) + f2d_scaled(a.l, k);
+  const unsigned uh = f2u(a.h), ul = f2u(a.l);
+  const int eh = (int)((uh >> 23) & 0xffu), el = (int)((ul >> 23) & 0xffu);
+  if (eh == 0) return f2d_scaled(a.l, k);
+  long long m = (long long)((uh & 0x7fffffu) | 0x800000u) << 29;  // in [2^52, 2^53)
+  int sh = el - eh + 29;  // l's significand in units of the double's last place
+  sh = sh > 30 ? 30 : sh;
+  long long lm = (long long)((ul & 0x7fffffu) | 0x800000u);
+  lm = sh >= 0 ? (lm << sh) : (sh > -25 ? (lm >> -sh) : 0);
+  lm = el == 0 ? 0 : lm;
+  m = ((uh ^ ul) >> 31) ? m - lm : m + lm;
+  long long e = (long long)(eh - 127 + 1023 + k);
+  if (m >= (1LL << 53)) {
+    m >>= 1;
+    e += 1;
+  } else if (m < (1LL << 52)) {
+    m <<= 1;
+    e -= 1;
+  }
+  return ll2d((long long)((unsigned long long)(uh >> 31) << 63) | (e << 52) |
+              (m & ((1LL << 52) - 1)));
 }
 
 // ---------------------------------------------------------------------------
@@ -288,7 +338,7 @@ HG_HD __forceinline__ double f2_to_double(F2 a, int k) {
 HG_HD __forceinline__ double lm_sqrt(double x) {
   const long long b = d2ll(x);
   const int ef = (int)((b >> 52) & 0x7ff);
-  if (b <= 0 || ef == 0 || ef == 0x7ff) return sqrt(x);
+  if (b <= 0 || ef == 0 || ef == 0x7ff) return cold_sqrt(x);
   const int e = ef - 1023;
   const int odd = e & 1;
   const int k = (e - odd) / 2;
@@ -309,7 +359,7 @@ HG_HD __forceinline__ double lm_sqrt(double x) {
 HG_HD __forceinline__ double lm_rsqrt(double x) {
   const long long b = d2ll(x);
   const int ef = (int)((b >> 52) & 0x7ff);
-  if (b <= 0 || ef == 0 || ef == 0x7ff) return 1.0 / sqrt(x);
+  if (b <= 0 || ef == 0 || ef == 0x7ff) return cold_rsqrt(x);
   const int e = ef - 1023;
   const int odd = e & 1;
   const int k = (e - odd) / 2;
@@ -324,7 +374,7 @@ HG_HD __forceinline__ double lm_rsqrt(double x) {
 HG_HD __forceinline__ double lm_div(double n, double d) {
   const long long b = d2ll(d);
   const int ef = (int)((b >> 52) & 0x7ff);
-  if (b <= 0 || ef == 0 || ef >= 0x7fe) return n / d;
+  if (b <= 0 || ef == 0 || ef >= 0x7fe) return cold_div(n, d);
   const int e = ef - 1023;
   const float rf = rcp_approx(u2f(0x3f800000u | (unsigned)((b >> 29) & 0x7fffff)));
   double r = f2d_scaled(rf, -e);  // ~ 1/d, rel. err ~2^-22
@@ -355,7 +405,7 @@ inline Tables host_tables() {
 HG_HD __forceinline__ double lm_log(double x, const Tables& T) {
   const long long b = d2ll(x);
   const int ef = (int)((b >> 52) & 0x7ff);
-  if (b <= 0 || ef == 0 || ef == 0x7ff) return log(x);
+  if (b <= 0 || ef == 0 || ef == 0x7ff) return cold_log(x);
   // x = 2^e0 m0, m0 in [1, 2); fold to m in [0.75, 1.5)
   const int top = (int)((b >> 51) & 1);  // m0 >= 1.5
   const int e = ef - 1023 + top;
@@ -418,7 +468,7 @@ HG_HD __forceinline__ double arg_core(F2 re, F2 im, int q, int j, const Tables& 
   } else {
     // estimate too far off or non-finite input: generic path on the
     // quarter-turn-rotated vector
-    delta = atan2(f2_to_double(im0, 0), f2_to_double(re0, 0));
+    delta = cold_atan2(f2_to_double(im0, 0), f2_to_double(re0, 0));
     j = 0;
   }
   if (q == 0) return j == 0 ? delta : T.th[j + kArgTableHalf] + delta;
@@ -436,7 +486,7 @@ HG_HD __forceinline__ double lm_arg_near(double pr, double pi, float est, const 
   const long long br = qm == 0 ? bpr : (qm == 1 ? bpi : (qm == 2 ? bpr ^ kSign : bpi ^ kSign));
   const long long bi = qm == 0 ? bpi : (qm == 1 ? bpr ^ kSign : (qm == 2 ? bpi ^ kSign : bpr));
   const int er = (int)((br >> 52) & 0x7ff), ei = (int)((bi >> 52) & 0x7ff);
-  if (er == 0x7ff || ei == 0x7ff) return atan2(pi, pr);
+  if (er == 0x7ff || ei == 0x7ff) return cold_atan2(pi, pr);
   const int top = (er > ei ? er : ei);
   return arg_core(scaled_f2(br, top), scaled_f2(bi, top), q, j, T);
 }
@@ -479,7 +529,7 @@ HG_HD __forceinline__ double lm_log_quot(double p1, double p2, double q1, double
   const bool ok = b1 > 0 && b2 > 0 && b3 > 0 && b4 > 0 && e1 != 0 && e2 != 0 && e3 != 0 &&
                   e4 != 0 && e1 != 0x7ff && e2 != 0x7ff && e3 != 0x7ff && e4 != 0x7ff &&
                   ed != 0 && ed < 0x7fe;
-  if (!ok) return log((ONE_FACTOR ? p1 : p1 * p2) / d);
+  if (!ok) return cold_log_quot(ONE_FACTOR ? p1 : p1 * p2, d);
   const auto mant = [](long long b) { return u2f(0x3f800000u | (unsigned)((b >> 29) & 0x7fffff)); };
   float rf = ONE_FACTOR ? mant(b1) * rcp_approx(mant(b3))
                         : (mant(b1) * mant(b2)) * rcp_approx(mant(b3) * mant(b4));
@@ -492,7 +542,7 @@ HG_HD __forceinline__ double lm_log_quot(double p1, double p2, double q1, double
   int k = round_to_int((rf - 0.75f) * 256.0f);
   k = k < 0 ? 0 : (k > kLogTableSize - 1 ? kLogTableSize - 1 : k);
   const bool near1 = (E == 0) && (k == 64);
-  if (!near1 && (E > 1000 || E < -1000)) return log((ONE_FACTOR ? p1 : p1 * p2) / d);
+  if (!near1 && (E > 1000 || E < -1000)) return cold_log_quot(ONE_FACTOR ? p1 : p1 * p2, d);
   // numerator p1 p2 c_k 2^-E - q1 q2, exact when c_k 2^-E = 1
   double num;
   if (near1) {
@@ -503,7 +553,7 @@ HG_HD __forceinline__ double lm_log_quot(double p1, double p2, double q1, double
   }
   const long long bn = d2ll(num);
   const int en = (int)((bn >> 52) & 0x7ff);  // 0: zero or subnormal, counted as t = 0
-  if (en == 0x7ff) return log((ONE_FACTOR ? p1 : p1 * p2) / d);
+  if (en == 0x7ff) return cold_log_quot(ONE_FACTOR ? p1 : p1 * p2, d);
   // t = num / d: significands divided as pairs, scaled by 2^(en - ed)
   F2 t = f2_div(mant_f2(bn), mant_f2(bd));
   const int sc = en - ed;
@@ -535,7 +585,7 @@ HG_HD __forceinline__ float arg_f32(double re, double im) {
   const int er = (int)((d2ll(re) >> 52) & 0x7ff);
   const int ei = (int)((d2ll(im) >> 52) & 0x7ff);
   const int e = er > ei ? er : ei;
-  return atan2_f32(d2f_shift(im, e), d2f_shift(re, e));
+  return atan2_est(d2f_shift(im, e), d2f_shift(re, e));
 }
 
 }  // namespace lean

@@ -45,6 +45,8 @@ int cuda_check(cudaError_t e, const char* what) {
 #endif
 template <int F> struct MinBlocks { static constexpr int value = HG_FWD_MIN_BLOCKS; };
 template <> struct MinBlocks<kAll> { static constexpr int value = HG_FWD_MIN_BLOCKS_ALL; };
+// the potential needs every log and face angle, like the fused kernel
+template <> struct MinBlocks<kPotential> { static constexpr int value = HG_FWD_MIN_BLOCKS_ALL; };
 
 // out_mask: for kAll, which of the ten fields are written (compact rows).
 template <int F, class Source>

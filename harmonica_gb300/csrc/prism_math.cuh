@@ -119,6 +119,11 @@ HG_HD __forceinline__ double cfma_s(double coef, double v, double acc) {
   const double w = is_tiny(coef) ? 0.0 : v;
   return NEG ? fma(-coef, w, acc) : fma(coef, w, acc);
 }
+// the same with a run-time sign, flipped on the bits
+HG_HD __forceinline__ double cfma_xs(double coef, bool neg, double v, double acc) {
+  const double w = is_tiny(coef) ? 0.0 : v;
+  return fma(lean::ll2d(bits_of(coef) ^ (neg ? kSignBit : 0LL)), w, acc);
+}
 // the same with the sign as an argument (a constant after loop unrolling)
 HG_HD __forceinline__ double cfma_sgn(double coef, bool neg, double v, double acc) {
   const double w = is_tiny(coef) ? 0.0 : v;
@@ -438,11 +443,30 @@ HG_HD __forceinline__ bool face_angle_f2(double a, double b1, double b2, double 
                   scaled_f2(d2ll(r21), top), same_sign, bdq1, br, bi);
   normalize_f2c(ar, ai);
   normalize_f2c(br, bi);
-  const float est = atan2_f32(ai.h, ar.h) - atan2_f32(bi.h, br.h);
+  const float est = atan2_est(ai.h, ar.h) - atan2_est(bi.h, br.h);
   const F2 pr = f2_add(f2_mul(ar, br), f2_mul(ai, bi));
   const F2 pim = f2_add(f2_mul(ai, br), f2_neg(f2_mul(ar, bi)));
   o = lm_arg_near_f2(pr, pim, est, T);
   return true;
+}
+
+// The face angle in FP64 for the faces the float-pair path declines (kept
+// out of line: rarely executed).  Same pair products and argument as
+// face_angle_f2; |o| for a > 0.
+// O = [arg c_{2,c2} - arg c_{1,c2}] - [arg c_{2,c1} - arg c_{1,c1}] = arg A - arg B
+HG_COLD double face_angle_fp64(double a, double b1, double b2, double c1, double c2, double r11,
+                               double r12, double r21, double r22, bool same_sign, double width,
+                               const Tables& T) {
+  const double bdiff = width * (b2 + b1);
+  const double aa = fabs(a);
+  const double asq = a * a;
+  double ar, ai, br, bi;
+  pair_complex(aa, asq, b1, b2, c2, c2 * c2, r12, r22, same_sign, bdiff, ar, ai);
+  pair_complex(aa, asq, b1, b2, c1, c1 * c1, r11, r21, same_sign, bdiff, br, bi);
+  const float est = lean::arg_f32(ar, ai) - lean::arg_f32(br, bi);
+  const double pr = fma(ar, br, ai * bi);
+  const double pim = fma(ai, br, -(ar * bi));
+  return lean::lm_arg_near(pr, pim, est, T);
 }
 
 // width = b2 - b1 (shared by the two faces normal to one axis).
@@ -456,43 +480,157 @@ HG_HD __forceinline__ double face_angle(double a, bool upper, double b1, double 
   }
   const bool same_sign = !(neg_not_tiny(b1) && !nonpos_or_tiny(b2));
   double o;
-  if (LEAN && face_angle_f2(a, b1, b2, c1, c2, r11, r12, r21, r22, same_sign, width, T, o))
-    return times_sign_of(o, a);
-  const double bdiff = width * (b2 + b1);
-  const double aa = fabs(a);
-  const double asq = a * a;
-  // O = [arg c_{2,c2} - arg c_{1,c2}] - [arg c_{2,c1} - arg c_{1,c1}] = arg A - arg B
-  double ar, ai, br, bi;
-  pair_complex(aa, asq, b1, b2, c2, c2 * c2, r12, r22, same_sign, bdiff, ar, ai);
-  pair_complex(aa, asq, b1, b2, c1, c1 * c1, r11, r21, same_sign, bdiff, br, bi);
   if (LEAN) {
-    const float est = lean::arg_f32(ar, ai) - lean::arg_f32(br, bi);
-    const double pr = fma(ar, br, ai * bi);
-    const double pim = fma(ai, br, -(ar * bi));
-    o = lean::lm_arg_near(pr, pim, est, T);
-  } else {
-    o = atan2(ai, ar) - atan2(bi, br);
+    if (!face_angle_f2(a, b1, b2, c1, c2, r11, r12, r21, r22, same_sign, width, T, o))
+      o = face_angle_fp64(a, b1, b2, c1, c2, r11, r12, r21, r22, same_sign, width, T);
+    return times_sign_of(o, a);
   }
+  const double bdiff = width * (b2 + b1);
+  double ar, ai, br, bi;
+  pair_complex(fabs(a), a * a, b1, b2, c2, c2 * c2, r12, r22, same_sign, bdiff, ar, ai);
+  pair_complex(fabs(a), a * a, b1, b2, c1, c1 * c1, r11, r21, same_sign, bdiff, br, bi);
+  o = atan2(ai, ar) - atan2(bi, br);
   return times_sign_of(o, a);
 }
 
-template <bool LEAN>
-HG_HD __forceinline__ double face_x(const Geom& g, int i, const Tables& T) {
-  // in-plane (y_j, z_k), r[i][j][k]
-  return face_angle<LEAN>(g.x[i], i == 1, g.y[0], g.y[1], g.z[0], g.z[1], g.r[i][0][0],
-                          g.r[i][0][1], g.r[i][1][0], g.r[i][1][1], g.y[1] - g.y[0], T);
+// ---------------------------------------------------------------------------
+// Rolled evaluation.  The float-pair face angle is ~1000 instructions and a
+// merged log ~300; inlined once per face or log they make a loop body larger
+// than the instruction cache (warps then stall on instruction fetch).  The
+// helpers below evaluate the faces and logs in loops that are not unrolled,
+// with the per-iteration inputs chosen by selects (registers only), so the
+// kernel holds one copy of each.
+
+// Inputs of the face normal to `axis` (0 = x, 1 = y, 2 = z) at bound k:
+// x faces: b = y, c = z; y faces: b = x, c = z; z faces: b = x, c = y.
+struct FaceIn {
+  double a, b1, b2, c1, c2, r11, r12, r21, r22, width;
+};
+HG_HD __forceinline__ FaceIn face_in(const Geom& g, int axis, bool k) {
+  const bool X = axis == 0, Y = axis == 1;
+  FaceIn f;
+  f.a = X ? (k ? g.x[1] : g.x[0]) : (Y ? (k ? g.y[1] : g.y[0]) : (k ? g.z[1] : g.z[0]));
+  f.b1 = X ? g.y[0] : g.x[0];
+  f.b2 = X ? g.y[1] : g.x[1];
+  f.c1 = (X || Y) ? g.z[0] : g.y[0];
+  f.c2 = (X || Y) ? g.z[1] : g.y[1];
+  // r_{b c}: index of the vertex distance for in-plane corners (b_i, c_j)
+  const auto r = [&](int bi, int cj) {
+    const double rx = k ? g.r[1][bi][cj] : g.r[0][bi][cj];  // x face: r[k][b][c]
+    const double ry = k ? g.r[bi][1][cj] : g.r[bi][0][cj];  // y face: r[b][k][c]
+    const double rz = k ? g.r[bi][cj][1] : g.r[bi][cj][0];  // z face: r[b][c][k]
+    return X ? rx : (Y ? ry : rz);
+  };
+  f.r11 = r(0, 0);
+  f.r12 = r(0, 1);
+  f.r21 = r(1, 0);
+  f.r22 = r(1, 1);
+  f.width = X ? g.y[1] - g.y[0] : g.x[1] - g.x[0];
+  return f;
 }
+
 template <bool LEAN>
-HG_HD __forceinline__ double face_y(const Geom& g, int j, const Tables& T) {
-  // in-plane (x_i, z_k), r[i][j][k]
-  return face_angle<LEAN>(g.y[j], j == 1, g.x[0], g.x[1], g.z[0], g.z[1], g.r[0][j][0],
-                          g.r[0][j][1], g.r[1][j][0], g.r[1][j][1], g.x[1] - g.x[0], T);
+HG_HD __forceinline__ double face_of(const Geom& g, int axis, bool k, const Tables& T) {
+  const FaceIn f = face_in(g, axis, k);
+  return face_angle<LEAN>(f.a, k, f.b1, f.b2, f.c1, f.c2, f.r11, f.r12, f.r21, f.r22, f.width,
+                          T);
 }
+
+// The two faces normal to AXIS: o0 at the lower bound, o1 at the upper.
+template <int AXIS, bool LEAN>
+HG_HD __forceinline__ void faces2(const Geom& g, const Tables& T, double& o0, double& o1) {
+  o0 = 0.0;
+  o1 = 0.0;
+#pragma unroll 1
+  for (int k = 0; k < 2; k++) {
+    const double o = face_of<LEAN>(g, AXIS, k, T);
+    o0 = k ? o0 : o;
+    o1 = k ? o : o1;
+  }
+}
+
+// acc + sum_k (k ? -c1 : c0) O_k over the two faces normal to AXIS, the
+// product accumulated inside the loop (c0, c1 the face coefficients before
+// the -s_k sign: -s_0 = +1, -s_1 = -1).
+template <int AXIS, bool LEAN>
+HG_HD __forceinline__ double faces2_dot(const Geom& g, double c0, double c1, const Tables& T,
+                                        double acc) {
+#pragma unroll 1
+  for (int k = 0; k < 2; k++) {
+    const double o = face_of<LEAN>(g, AXIS, k, T);
+    acc = cfma_xs(k ? c1 : c0, k, o, acc);
+  }
+  return acc;
+}
+
+// All six faces, O[axis][k].
 template <bool LEAN>
-HG_HD __forceinline__ double face_z(const Geom& g, int k, const Tables& T) {
-  // in-plane (x_i, y_j), r[i][j][k]
-  return face_angle<LEAN>(g.z[k], k == 1, g.x[0], g.x[1], g.y[0], g.y[1], g.r[0][0][k],
-                          g.r[0][1][k], g.r[1][0][k], g.r[1][1][k], g.x[1] - g.x[0], T);
+HG_HD __forceinline__ void faces6(const Geom& g, const Tables& T, double O[3][2]) {
+#pragma unroll
+  for (int a = 0; a < 3; a++) O[a][0] = O[a][1] = 0.0;
+#pragma unroll 1
+  for (int f = 0; f < 6; f++) {
+    const int axis = f >> 1;
+    const bool k = f & 1;
+    const double o = face_of<LEAN>(g, axis, k, T);
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      O[a][0] = (axis == a && !k) ? o : O[a][0];
+      O[a][1] = (axis == a && k) ? o : O[a][1];
+    }
+  }
+}
+
+// Single edge logs of one axis, L[p][s] = ln(num/den), for the three axes in
+// one rolled loop: Lx from Ex, Ly from Ey, Lz from Ez.
+template <bool LEAN>
+HG_HD __forceinline__ void logs12(const EdgeSet& Ex, const EdgeSet& Ey, const EdgeSet& Ez,
+                                  const Tables& T, double Lx[2][2], double Ly[2][2],
+                                  double Lz[2][2]) {
+#pragma unroll
+  for (int p = 0; p < 2; p++)
+#pragma unroll
+    for (int q = 0; q < 2; q++) Lx[p][q] = Ly[p][q] = Lz[p][q] = 0.0;
+#pragma unroll 1
+  for (int axis = 0; axis < 3; axis++) {
+    const bool X = axis == 0, Y = axis == 1;
+#pragma unroll
+    for (int p = 0; p < 2; p++)
+#pragma unroll
+      for (int q = 0; q < 2; q++) {
+        const double n = X ? Ex.num[p][q] : (Y ? Ey.num[p][q] : Ez.num[p][q]);
+        const double d = X ? Ex.den[p][q] : (Y ? Ey.den[p][q] : Ez.den[p][q]);
+        const double l = log_ratio1<LEAN>(n, d, T);
+        Lx[p][q] = X ? l : Lx[p][q];
+        Ly[p][q] = Y ? l : Ly[p][q];
+        Lz[p][q] = (!X && !Y) ? l : Lz[p][q];
+      }
+  }
+}
+
+// sum over the 4 merged logs  c_m ln(R_{m,1} / R_{m,0})  of two edge sets,
+// m = 0, 1 from E0 (coefficients e0_0, e0_1) and m = 2, 3 from E1, with the
+// ratio pair of entry m at [idx(m)][1] over [idx(m)][0] (T0 = false) or
+// [1][idx(m)] over [0][idx(m)] (T0 = true; likewise T1 for E1); the
+// coefficient signs are -, +, -, + (s_0 = -1, s_1 = +1).
+template <bool LEAN, bool T0, bool T1>
+HG_HD __forceinline__ double merged_logs4(const EdgeSet& E0, const EdgeSet& E1, double c00,
+                                          double c01, double c10, double c11, const Tables& T,
+                                          double acc) {
+#pragma unroll 1
+  for (int m = 0; m < 4; m++) {
+    const bool b = m & 1, second = m >= 2;
+    const auto pick = [&](const double (&A)[2][2], const double (&B)[2][2], bool hi) {
+      const double a0 = T0 ? A[hi][0] : A[0][hi], a1 = T0 ? A[hi][1] : A[1][hi];
+      const double b0 = T1 ? B[hi][0] : B[0][hi], b1 = T1 ? B[hi][1] : B[1][hi];
+      return second ? (b ? b1 : b0) : (b ? a1 : a0);
+    };
+    const double n1 = pick(E0.num, E1.num, true), d1 = pick(E0.den, E1.den, true);
+    const double n0 = pick(E0.num, E1.num, false), d0 = pick(E0.den, E1.den, false);
+    const double coef = second ? (b ? c11 : c10) : (b ? c01 : c00);
+    acc = cfma_xs(coef, !b, log_ratio2<LEAN>(n1, d1, n0, d0, T), acc);
+  }
+  return acc;
 }
 
 // ---------------------------------------------------------------------------
@@ -507,21 +645,12 @@ HG_HD __forceinline__ void pair_all(const Rel& q, const Tables& T, double out[kN
   edges_y(g, Ey);
   edges_z(g, Ez);
   double Lx[2][2], Ly[2][2], Lz[2][2];
-#pragma unroll
-  for (int a = 0; a < 2; a++)
-#pragma unroll
-    for (int b = 0; b < 2; b++) {
-      Lx[a][b] = log_ratio1<LEAN>(Ex.num[a][b], Ex.den[a][b], T);
-      Ly[a][b] = log_ratio1<LEAN>(Ey.num[a][b], Ey.den[a][b], T);
-      Lz[a][b] = log_ratio1<LEAN>(Ez.num[a][b], Ez.den[a][b], T);
-    }
-  double Ox[2], Oy[2], Oz[2];
-#pragma unroll
-  for (int a = 0; a < 2; a++) {
-    Ox[a] = face_x<LEAN>(g, a, T);
-    Oy[a] = face_y<LEAN>(g, a, T);
-    Oz[a] = face_z<LEAN>(g, a, T);
-  }
+  logs12<LEAN>(Ex, Ey, Ez, T, Lx, Ly, Lz);
+  double O[3][2];
+  faces6<LEAN>(g, T, O);
+  const double* Ox = O[0];
+  const double* Oy = O[1];
+  const double* Oz = O[2];
   double pot = 0.0, ge = 0.0, gn = 0.0, gz = 0.0;
 #pragma unroll
   for (int a = 0; a < 2; a++)
@@ -578,67 +707,29 @@ HG_HD __forceinline__ double pair_field(const Rel& q, const Tables& T) {
     EdgeSet Ey, Ex;
     edges_y(g, Ey);
     edges_x(g, Ex);
-    double v = 0.0;
-    // s_a x_a L^y_a + s_a y_a L^x_a - s_a z_a O_a, s_0 = -1, s_1 = +1
-    const auto ly = [&](int a) {
-      return log_ratio2<LEAN>(Ey.num[a][1], Ey.den[a][1], Ey.num[a][0], Ey.den[a][0], T);
-    };
-    const auto lx = [&](int a) {
-      return log_ratio2<LEAN>(Ex.num[a][1], Ex.den[a][1], Ex.num[a][0], Ex.den[a][0], T);
-    };
-    v = cfma_s<true>(g.x[0], ly(0), v);
-    v = cfma_s<false>(g.x[1], ly(1), v);
-    v = cfma_s<true>(g.y[0], lx(0), v);
-    v = cfma_s<false>(g.y[1], lx(1), v);
-    v = cfma_s<false>(g.z[0], face_z<LEAN>(g, 0, T), v);
-    v = cfma_s<true>(g.z[1], face_z<LEAN>(g, 1, T), v);
-    return v;
+    const double v =
+        merged_logs4<LEAN, false, false>(Ey, Ex, g.x[0], g.x[1], g.y[0], g.y[1], T, 0.0);
+    return faces2_dot<2, LEAN>(g, g.z[0], g.z[1], T, v);
   } else if (F == kGe) {
     // sum_j s_j y_j sum_i s_i Lz[i][j] + sum_k s_k z_k sum_i s_i Ly[i][k]
     //   - sum_i s_i x_i Ox[i]
     EdgeSet Ez, Ey;
     edges_z(g, Ez);
     edges_y(g, Ey);
-    double v = 0.0;
-    const auto lz = [&](int a) {
-      return log_ratio2<LEAN>(Ez.num[1][a], Ez.den[1][a], Ez.num[0][a], Ez.den[0][a], T);
-    };
-    const auto ly = [&](int a) {
-      return log_ratio2<LEAN>(Ey.num[1][a], Ey.den[1][a], Ey.num[0][a], Ey.den[0][a], T);
-    };
-    v = cfma_s<true>(g.y[0], lz(0), v);
-    v = cfma_s<false>(g.y[1], lz(1), v);
-    v = cfma_s<true>(g.z[0], ly(0), v);
-    v = cfma_s<false>(g.z[1], ly(1), v);
-    v = cfma_s<false>(g.x[0], face_x<LEAN>(g, 0, T), v);
-    v = cfma_s<true>(g.x[1], face_x<LEAN>(g, 1, T), v);
-    return v;
+    const double v =
+        merged_logs4<LEAN, true, true>(Ez, Ey, g.y[0], g.y[1], g.z[0], g.z[1], T, 0.0);
+    return faces2_dot<0, LEAN>(g, g.x[0], g.x[1], T, v);
   } else if (F == kGn) {
     // sum_k s_k z_k sum_j s_j Lx[j][k] + sum_i s_i x_i sum_j s_j Lz[i][j]
     //   - sum_j s_j y_j Oy[j]
     EdgeSet Ex, Ez;
     edges_x(g, Ex);
     edges_z(g, Ez);
-    double v = 0.0;
-    const auto lx = [&](int a) {
-      return log_ratio2<LEAN>(Ex.num[1][a], Ex.den[1][a], Ex.num[0][a], Ex.den[0][a], T);
-    };
-    const auto lz = [&](int a) {
-      return log_ratio2<LEAN>(Ez.num[a][1], Ez.den[a][1], Ez.num[a][0], Ez.den[a][0], T);
-    };
-    v = cfma_s<true>(g.z[0], lx(0), v);
-    v = cfma_s<false>(g.z[1], lx(1), v);
-    v = cfma_s<true>(g.x[0], lz(0), v);
-    v = cfma_s<false>(g.x[1], lz(1), v);
-    v = cfma_s<false>(g.y[0], face_y<LEAN>(g, 0, T), v);
-    v = cfma_s<true>(g.y[1], face_y<LEAN>(g, 1, T), v);
-    return v;
-  } else if (F == kGee) {
-    return -(face_x<LEAN>(g, 1, T) - face_x<LEAN>(g, 0, T));
-  } else if (F == kGnn) {
-    return -(face_y<LEAN>(g, 1, T) - face_y<LEAN>(g, 0, T));
-  } else if (F == kGzz) {
-    return -(face_z<LEAN>(g, 1, T) - face_z<LEAN>(g, 0, T));
+    const double v =
+        merged_logs4<LEAN, true, false>(Ex, Ez, g.z[0], g.z[1], g.x[0], g.x[1], T, 0.0);
+    return faces2_dot<1, LEAN>(g, g.y[0], g.y[1], T, v);
+  } else if (F == kGee || F == kGnn || F == kGzz) {
+    return faces2_dot<(F == kGee ? 0 : (F == kGnn ? 1 : 2)), LEAN>(g, 1.0, 1.0, T, 0.0);
   } else {
     // g_en / g_ez / g_nz: sum_{p,s} s_p s_s L[p][s] = ln(R11 R00 / (R01 R10))
     EdgeSet E;
@@ -658,9 +749,11 @@ template <bool LEAN>
 HG_HD __forceinline__ void pair_tensor6(const Rel& q, const Tables& T, double t[6]) {
   Geom g;
   make_geom<LEAN>(q, g);
-  t[0] = -(face_x<LEAN>(g, 1, T) - face_x<LEAN>(g, 0, T));
-  t[1] = -(face_y<LEAN>(g, 1, T) - face_y<LEAN>(g, 0, T));
-  t[2] = -(face_z<LEAN>(g, 1, T) - face_z<LEAN>(g, 0, T));
+  double O[3][2];
+  faces6<LEAN>(g, T, O);
+  t[0] = O[0][0] - O[0][1];
+  t[1] = O[1][0] - O[1][1];
+  t[2] = O[2][0] - O[2][1];
   EdgeSet E;
   edges_z(g, E);
   t[3] = log_quot<LEAN>(E.num[1][1] * E.num[0][0], E.den[0][1] * E.den[1][0],
@@ -684,19 +777,8 @@ HG_HD __forceinline__ double pair_gz_faces(const Rel& q, const Tables& T, double
   EdgeSet Ey, Ex;
   edges_y(g, Ey);
   edges_x(g, Ex);
-  o_bottom = face_z<LEAN>(g, 0, T);
-  o_top = face_z<LEAN>(g, 1, T);
-  const auto ly = [&](int a) {
-    return log_ratio2<LEAN>(Ey.num[a][1], Ey.den[a][1], Ey.num[a][0], Ey.den[a][0], T);
-  };
-  const auto lx = [&](int a) {
-    return log_ratio2<LEAN>(Ex.num[a][1], Ex.den[a][1], Ex.num[a][0], Ex.den[a][0], T);
-  };
-  double v = 0.0;
-  v = cfma_s<true>(g.x[0], ly(0), v);
-  v = cfma_s<false>(g.x[1], ly(1), v);
-  v = cfma_s<true>(g.y[0], lx(0), v);
-  v = cfma_s<false>(g.y[1], lx(1), v);
+  faces2<2, LEAN>(g, T, o_bottom, o_top);
+  double v = merged_logs4<LEAN, false, false>(Ey, Ex, g.x[0], g.x[1], g.y[0], g.y[1], T, 0.0);
   v = cfma_s<true>(g.z[1], o_top, v);
   return cfma_s<false>(g.z[0], o_bottom, v);
 }
