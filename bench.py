@@ -21,7 +21,13 @@ cost is uniform, so pairs/s over batches equals pairs/s over the full survey.
   sqrt + 2 log + 1 atan2) at basic=1, sqrt=4, log=20, atan2=30), over the
   average kernel time; ``peak`` is the FP64 fused multiply-add rate measured
   live by the hg_fp64_peak_probe launch (no FP64 figure exists in the
-  measured peak file).
+  measured peak file).  The kernel executes far fewer FP64
+  instructions per pair than that convention counts (float-pair elementary
+  functions), so ``frac`` exceeds 1; ``fp64_pipe_frac`` is the hardware
+  figure: the kernel's FP64 instructions per pair (ncu count, recorded in
+  profiles/forward_kernel_gz_layer1e6.md) x pairs/s over the measured FP64
+  instruction peak.  ``traffic`` is the DRAM bytes of one step's launch from
+  the same profile (the 24 MB layer read once; it stays in L2).
 * ``cpu_baseline``: the CPU oracle (a C/OpenMP restatement of the reference's
   per-vertex loop) on all host cores, on a bounded sample of stations of the
   same workload.
@@ -45,6 +51,11 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 
 ALGO_FLOP_PER_PAIR_GZ = 720.0
+# ncu counts for forward_kernel<g_z, LayerSource> (profiles/forward_kernel_gz_layer1e6.md):
+# FP64 thread-instructions per pair (sm__thread_inst_executed_pipe_fp64_pred_on / pairs) and
+# DRAM read+write bytes of one default step's launch (5000 stations x 1e6 prisms).
+FP64_INST_PER_PAIR_GZ = 77.3
+TRAFFIC_BYTES_GZ_STEP = 25159424 + 21248
 METRIC = "FP64 g_z prism-station pairs/s"
 WORKLOAD = "layer_topography_1e6: 1000x1000 prisms (200 m grid), 500x500 stations, g_z"
 
@@ -738,7 +749,11 @@ def main():
             torch.distributed.destroy_process_group()
         return
     avg_launch_s = dev_time / args.steps
-    achieved = ALGO_FLOP_PER_PAIR_GZ * (pairs / world / args.steps) / avg_launch_s / 1e12
+    kernel_pairs_per_s = (pairs / world / args.steps) / avg_launch_s
+    achieved = ALGO_FLOP_PER_PAIR_GZ * kernel_pairs_per_s / 1e12
+    # the probe's peak is in flops (2 per FMA); the FP64 pipe issues 1 instruction per FMA
+    fp64_pipe_frac = FP64_INST_PER_PAIR_GZ * kernel_pairs_per_s / (peak * 1e12 / 2.0)
+    default_step = args.stations_per_step == 5000
     line = {
         "metric": METRIC,
         "value": value,
@@ -765,8 +780,10 @@ def main():
             "peak": peak,
             "unit": "TFLOP/s",
             "frac": achieved / peak,
-            "traffic": None,
+            "traffic": TRAFFIC_BYTES_GZ_STEP if default_step else None,
             "flop_per_pair": ALGO_FLOP_PER_PAIR_GZ,
+            "fp64_inst_per_pair": FP64_INST_PER_PAIR_GZ,
+            "fp64_pipe_frac": fp64_pipe_frac,
             "peak_source": "measured live: hg_fp64_peak_probe (FP64 FMA chains)",
         },
         "cpu_baseline": base,

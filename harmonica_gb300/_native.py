@@ -202,7 +202,7 @@ PROTOTYPES = {
     ),
     "hg_round_run": (
         ctypes.c_int,
-        [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p,
+        [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p,
          ctypes.c_void_p],
     ),
     "hg_round_reduce": (

@@ -20,6 +20,21 @@ template <> struct NumOut<kAll> { static constexpr int value = kNumFields; };
 
 HG_HD __forceinline__ bool is_tensor(int f) { return f >= kGee && f <= kGnz; }
 
+// Resident CTAs per SM the register allocation must allow (FP64-pipe bound
+// code hides its latency with more warps; the fused all-field kernel needs
+// more registers).
+#ifndef HG_FWD_MIN_BLOCKS
+#define HG_FWD_MIN_BLOCKS 6
+#endif
+#ifndef HG_FWD_MIN_BLOCKS_ALL
+#define HG_FWD_MIN_BLOCKS_ALL 4
+#endif
+template <int F> struct MinBlocks { static constexpr int value = HG_FWD_MIN_BLOCKS; };
+template <> struct MinBlocks<kAll> { static constexpr int value = HG_FWD_MIN_BLOCKS_ALL; };
+// the potential needs every log and face angle, like the fused kernel
+template <> struct MinBlocks<kPotential> { static constexpr int value = HG_FWD_MIN_BLOCKS_ALL; };
+
+
 // ---------------------------------------------------------------------------
 // Prism sources: how a CTA loads prism p into shared memory.
 struct ListSource {

@@ -23,10 +23,7 @@
 
 namespace hg {
 
-// Resident CTAs per SM for the persistent kernels: they dispatch every field
-// at run time, so the register budget is set by the heaviest (the potential,
-// all 12 logs and 6 face angles); 4 CTAs fit it without spills.
-constexpr int kBatchMinBlocks = 4;
+
 
 int set_error(int code, const std::string& msg);
 int cuda_check(cudaError_t e, const char* what);
@@ -74,11 +71,14 @@ __device__ __forceinline__ void run_item(const ProblemDev& P, const WorkItem& w,
   if (active) part[P.part_offset + (int64_t)w.chunk * P.n_obs + i] = acc[0];
 }
 
-__global__ void __launch_bounds__(kThreads, kBatchMinBlocks) batch_kernel(const ProblemDev* __restrict__ probs,
-                                                         const WorkItem* __restrict__ items,
-                                                         int64_t n_items,
-                                                         unsigned long long* __restrict__ counter,
-                                                         double* __restrict__ part) {
+// Persistent kernel for the work items of one field F (the items of a batch
+// are grouped by field and each group runs its own launch): specialised per
+// field, so it keeps that field's register budget and instruction footprint.
+template <int F>
+__global__ void __launch_bounds__(kThreads, MinBlocks<F>::value)
+    batch_kernel(const ProblemDev* __restrict__ probs, const WorkItem* __restrict__ items,
+                 int64_t n_items, unsigned long long* __restrict__ counter,
+                 double* __restrict__ part) {
   __shared__ SmemTile sh;
   __shared__ SmemTables tabs;
   __shared__ long long next;
@@ -90,19 +90,24 @@ __global__ void __launch_bounds__(kThreads, kBatchMinBlocks) batch_kernel(const 
     const long long it = next;
     if (it >= n_items) break;
     const WorkItem w = items[it];
-    const ProblemDev P = probs[w.problem];
-    switch (P.field) {  // uniform across the CTA
-      case kPotential: run_item<kPotential>(P, w, sh, T, part); break;
-      case kGe: run_item<kGe>(P, w, sh, T, part); break;
-      case kGn: run_item<kGn>(P, w, sh, T, part); break;
-      case kGz: run_item<kGz>(P, w, sh, T, part); break;
-      case kGee: run_item<kGee>(P, w, sh, T, part); break;
-      case kGnn: run_item<kGnn>(P, w, sh, T, part); break;
-      case kGzz: run_item<kGzz>(P, w, sh, T, part); break;
-      case kGen: run_item<kGen>(P, w, sh, T, part); break;
-      case kGez: run_item<kGez>(P, w, sh, T, part); break;
-      default: run_item<kGnz>(P, w, sh, T, part); break;
-    }
+    run_item<F>(probs[w.problem], w, sh, T, part);
+  }
+}
+
+using BatchKernel = void (*)(const ProblemDev*, const WorkItem*, int64_t, unsigned long long*,
+                             double*);
+BatchKernel batch_kernel_for(int f) {
+  switch (f) {
+    case kPotential: return batch_kernel<kPotential>;
+    case kGe: return batch_kernel<kGe>;
+    case kGn: return batch_kernel<kGn>;
+    case kGz: return batch_kernel<kGz>;
+    case kGee: return batch_kernel<kGee>;
+    case kGnn: return batch_kernel<kGnn>;
+    case kGzz: return batch_kernel<kGzz>;
+    case kGen: return batch_kernel<kGen>;
+    case kGez: return batch_kernel<kGez>;
+    default: return batch_kernel<kGnz>;
   }
 }
 
@@ -126,6 +131,9 @@ using namespace hg;
 struct hg_batch {
   int64_t n_problems = 0;
   int64_t n_items = 0;
+  int64_t seg_begin[kNumFields] = {};  // the items of field f: [seg_begin, seg_begin + seg_count)
+  int64_t seg_count[kNumFields] = {};
+  int32_t seg_ctas[kNumFields] = {};   // CTAs of field f's persistent launch
   int64_t n_ctas = 0;
   int64_t partials = 0;  // doubles
   double pairs = 0.0;
@@ -136,7 +144,7 @@ struct hg_batch {
 
 namespace {
 
-constexpr size_t kCounterBytes = 256;  // counter, then the partials (256-byte aligned)
+constexpr size_t kCounterBytes = 256;  // one counter per field, then the partials (256-byte aligned)
 
 int64_t round_up(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
 
@@ -155,14 +163,21 @@ int hg_batch_create(const hg_problem* problems, int64_t n_problems, int64_t chun
   if (rc != HG_OK) return rc;
   int sms = kSmCount;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-  if (n_ctas <= 0) {
-    int per_sm = 0;
-    rc = cuda_check(
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel, kThreads, 0),
-        "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
-    if (rc != HG_OK) return rc;
-    n_ctas = (int32_t)std::max(1, per_sm) * sms;
+  // CTAs of each field's persistent launch: the given count, else one full
+  // wave of that field's kernel
+  int32_t ctas_for[kNumFields];
+  for (int f = 0; f < kNumFields; f++) {
+    ctas_for[f] = n_ctas;
+    if (n_ctas <= 0) {
+      int per_sm = 0;
+      rc = cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                          &per_sm, batch_kernel_for(f), kThreads, 0),
+                      "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+      if (rc != HG_OK) return rc;
+      ctas_for[f] = (int32_t)std::max(1, per_sm) * sms;
+    }
   }
+  if (n_ctas <= 0) n_ctas = ctas_for[kGz];
   std::vector<ProblemDev> probs((size_t)n_problems);
   int64_t total_pairs_all = 0;
   for (int64_t p = 0; p < n_problems; p++) {
@@ -217,15 +232,26 @@ int hg_batch_create(const hg_problem* problems, int64_t n_problems, int64_t chun
         cost.push_back(np);  // every item runs kThreads threads over np prisms
       }
   }
-  // longest items first (list scheduling), ties in creation order
+  // grouped by field; within a field longest items first (list
+  // scheduling), ties in creation order
   std::vector<int64_t> order(items.size());
   for (size_t k = 0; k < order.size(); k++) order[k] = (int64_t)k;
-  std::stable_sort(order.begin(), order.end(),
-                   [&](int64_t a, int64_t b) { return cost[(size_t)a] > cost[(size_t)b]; });
+  const auto field_of = [&](int64_t k) { return probs[(size_t)items[(size_t)k].problem].field; };
+  std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) {
+    const int fa = field_of(a), fb = field_of(b);
+    if (fa != fb) return fa < fb;
+    return cost[(size_t)a] > cost[(size_t)b];
+  });
   std::vector<WorkItem> sorted(items.size());
   for (size_t k = 0; k < order.size(); k++) sorted[k] = items[(size_t)order[k]];
 
   hg_batch* b = new hg_batch();
+  for (size_t k = 0; k < order.size(); k++) {
+    const int f = field_of(order[k]);
+    if (b->seg_count[f] == 0) b->seg_begin[f] = (int64_t)k;
+    b->seg_count[f]++;
+  }
+  for (int f = 0; f < kNumFields; f++) b->seg_ctas[f] = ctas_for[f];
   b->n_problems = n_problems;
   b->n_items = (int64_t)sorted.size();
   b->n_ctas = n_ctas;
@@ -280,12 +306,15 @@ int hg_batch_run(const hg_batch* batch, void* workspace, size_t workspace_bytes,
   cudaStream_t st = (cudaStream_t)stream;
   unsigned long long* counter = static_cast<unsigned long long*>(workspace);
   double* part = reinterpret_cast<double*>(static_cast<char*>(workspace) + kCounterBytes);
-  int rc = cuda_check(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st),
+  // one work counter per field
+  int rc = cuda_check(cudaMemsetAsync(counter, 0, sizeof(unsigned long long) * kNumFields, st),
                       "cudaMemsetAsync(counter)");
   if (rc != HG_OK) return rc;
-  if (batch->n_items > 0) {
-    batch_kernel<<<(unsigned)batch->n_ctas, kThreads, 0, st>>>(batch->d_probs, batch->d_items,
-                                                              batch->n_items, counter, part);
+  for (int f = 0; f < kNumFields; f++) {
+    if (batch->seg_count[f] == 0) continue;
+    batch_kernel_for(f)<<<(unsigned)batch->seg_ctas[f], kThreads, 0, st>>>(
+        batch->d_probs, batch->d_items + batch->seg_begin[f], batch->seg_count[f], counter + f,
+        part);
     rc = cuda_check(cudaGetLastError(), "batch_kernel launch");
     if (rc != HG_OK) return rc;
   }
@@ -328,10 +357,11 @@ __device__ __forceinline__ void run_plan_item(const hg_problem_plan& P, const hg
   if (active) P.partials[(int64_t)w.chunk * P.n_obs + i] = acc[0];
 }
 
-__global__ void __launch_bounds__(kThreads, kBatchMinBlocks) round_kernel(const hg_problem_plan* __restrict__ probs,
-                                                         const hg_work_item* __restrict__ items,
-                                                         int64_t n_items,
-                                                         unsigned long long* __restrict__ counter) {
+// Persistent kernel over the work items of one field F in a round.
+template <int F>
+__global__ void __launch_bounds__(kThreads, MinBlocks<F>::value)
+    round_kernel(const hg_problem_plan* __restrict__ probs, const hg_work_item* __restrict__ items,
+                 int64_t n_items, unsigned long long* __restrict__ counter) {
   __shared__ SmemTile sh;
   __shared__ SmemTables tabs;
   __shared__ long long next;
@@ -343,19 +373,24 @@ __global__ void __launch_bounds__(kThreads, kBatchMinBlocks) round_kernel(const 
     const long long it = next;
     if (it >= n_items) break;
     const hg_work_item w = items[it];
-    const hg_problem_plan P = probs[w.problem];
-    switch (P.field) {  // uniform across the CTA
-      case kPotential: run_plan_item<kPotential>(P, w, sh, T); break;
-      case kGe: run_plan_item<kGe>(P, w, sh, T); break;
-      case kGn: run_plan_item<kGn>(P, w, sh, T); break;
-      case kGz: run_plan_item<kGz>(P, w, sh, T); break;
-      case kGee: run_plan_item<kGee>(P, w, sh, T); break;
-      case kGnn: run_plan_item<kGnn>(P, w, sh, T); break;
-      case kGzz: run_plan_item<kGzz>(P, w, sh, T); break;
-      case kGen: run_plan_item<kGen>(P, w, sh, T); break;
-      case kGez: run_plan_item<kGez>(P, w, sh, T); break;
-      default: run_plan_item<kGnz>(P, w, sh, T); break;
-    }
+    run_plan_item<F>(probs[w.problem], w, sh, T);
+  }
+}
+
+using RoundKernel = void (*)(const hg_problem_plan*, const hg_work_item*, int64_t,
+                             unsigned long long*);
+RoundKernel round_kernel_for(int f) {
+  switch (f) {
+    case kPotential: return round_kernel<kPotential>;
+    case kGe: return round_kernel<kGe>;
+    case kGn: return round_kernel<kGn>;
+    case kGz: return round_kernel<kGz>;
+    case kGee: return round_kernel<kGee>;
+    case kGnn: return round_kernel<kGnn>;
+    case kGzz: return round_kernel<kGzz>;
+    case kGen: return round_kernel<kGen>;
+    case kGez: return round_kernel<kGez>;
+    default: return round_kernel<kGnz>;
   }
 }
 
@@ -376,30 +411,45 @@ __global__ void round_reduce_kernel(const hg_problem_plan* __restrict__ probs,
 
 extern "C" {
 
-int hg_round_run(const hg_problem_plan* problems, const hg_work_item* items, int64_t n_items,
-                 int32_t n_ctas, void* counter, void* stream) {
-  if (n_items < 0 || !counter || (n_items > 0 && (!problems || !items)))
-    return set_error(HG_ERR_INVALID, "bad arguments");
+int hg_round_run(const hg_problem_plan* problems, const hg_work_item* items,
+                 const int64_t* field_counts, int32_t n_ctas, void* counter, void* stream) {
+  if (!field_counts || !counter) return set_error(HG_ERR_INVALID, "bad arguments");
+  int64_t n_items = 0;
+  for (int f = 0; f < kNumFields; f++) {
+    if (field_counts[f] < 0) return set_error(HG_ERR_INVALID, "negative item count");
+    n_items += field_counts[f];
+  }
+  if (n_items > 0 && (!problems || !items)) return set_error(HG_ERR_INVALID, "bad arguments");
   cudaStream_t st = (cudaStream_t)stream;
   if (n_items == 0) return HG_OK;
-  if (n_ctas <= 0) {
-    int device = 0, sms = kSmCount, per_sm = 0;
-    int rc = cuda_check(cudaGetDevice(&device), "cudaGetDevice");
-    if (rc != HG_OK) return rc;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    rc = cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, round_kernel,
-                                                                  kThreads, 0),
-                    "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
-    if (rc != HG_OK) return rc;
-    n_ctas = (int32_t)std::max(1, per_sm) * sms;
-  }
-  int rc = cuda_check(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st),
-                      "cudaMemsetAsync(counter)");
+  int sms = kSmCount, device = 0;
+  int rc = cuda_check(cudaGetDevice(&device), "cudaGetDevice");
   if (rc != HG_OK) return rc;
-  const int64_t ctas = std::min<int64_t>(n_ctas, n_items);
-  round_kernel<<<(unsigned)ctas, kThreads, 0, st>>>(problems, items, n_items,
-                                                    static_cast<unsigned long long*>(counter));
-  return cuda_check(cudaGetLastError(), "round_kernel launch");
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  rc = cuda_check(cudaMemsetAsync(counter, 0, sizeof(unsigned long long) * kNumFields, st),
+                  "cudaMemsetAsync(counter)");
+  if (rc != HG_OK) return rc;
+  int64_t begin = 0;
+  for (int f = 0; f < kNumFields; f++) {
+    const int64_t n = field_counts[f];
+    if (n == 0) continue;
+    int64_t ctas = n_ctas;
+    if (ctas <= 0) {
+      int per_sm = 0;
+      rc = cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, round_kernel_for(f),
+                                                                    kThreads, 0),
+                      "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+      if (rc != HG_OK) return rc;
+      ctas = (int64_t)std::max(1, per_sm) * sms;
+    }
+    ctas = std::min<int64_t>(ctas, n);
+    round_kernel_for(f)<<<(unsigned)ctas, kThreads, 0, st>>>(
+        problems, items + begin, n, static_cast<unsigned long long*>(counter) + f);
+    rc = cuda_check(cudaGetLastError(), "round_kernel launch");
+    if (rc != HG_OK) return rc;
+    begin += n;
+  }
+  return HG_OK;
 }
 
 int hg_round_reduce(const hg_problem_plan* problems, const int32_t* problem_ids, int64_t n_ids,

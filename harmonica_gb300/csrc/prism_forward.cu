@@ -34,20 +34,6 @@ int cuda_check(cudaError_t e, const char* what) {
   return set_error(HG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-// Resident CTAs per SM the register allocation must allow (FP64-pipe bound
-// code hides its latency with more warps; the fused all-field kernel needs
-// more registers).
-#ifndef HG_FWD_MIN_BLOCKS
-#define HG_FWD_MIN_BLOCKS 6
-#endif
-#ifndef HG_FWD_MIN_BLOCKS_ALL
-#define HG_FWD_MIN_BLOCKS_ALL 4
-#endif
-template <int F> struct MinBlocks { static constexpr int value = HG_FWD_MIN_BLOCKS; };
-template <> struct MinBlocks<kAll> { static constexpr int value = HG_FWD_MIN_BLOCKS_ALL; };
-// the potential needs every log and face angle, like the fused kernel
-template <> struct MinBlocks<kPotential> { static constexpr int value = HG_FWD_MIN_BLOCKS_ALL; };
-
 // out_mask: for kAll, which of the ten fields are written (compact rows).
 template <int F, class Source>
 __global__ void __launch_bounds__(kThreads, MinBlocks<F>::value) forward_kernel(

@@ -139,7 +139,8 @@ class PrismServer:
             self.copy = torch.cuda.Stream(self.dev)
             self.table_dev = torch.empty(self.max_active * ctypes.sizeof(_native.HgProblemPlan),
                                          dtype=torch.uint8, device=self.dev)
-            self.counter = torch.zeros(1, dtype=torch.int64, device=self.dev)
+            self.counter = torch.zeros(10, dtype=torch.int64,
+                                       device=self.dev)  # one per field code
             self.flags = torch.zeros(self.max_active, dtype=torch.int32, device=self.dev)
         self.table = (_native.HgProblemPlan * self.max_active)()
         self._ring = [self._pinned_round_buffers() for _ in range(self.rounds_in_flight + 2)]
@@ -315,10 +316,12 @@ class PrismServer:
             self._copy_event.record(self.copy)
 
     def _plan_round(self):
-        """Items for the next round: shortest remaining work first."""
+        """Items for the next round: shortest remaining work first, then grouped
+        by field (each field runs its own specialised persistent launch).
+        Returns (items, per-field item counts, finishing requests)."""
         reqs = [r for r in self.active.values() if r.next_item < r.n_items]
         if not reqs:
-            return None, []
+            return None, None, []
         reqs.sort(key=lambda r: (r.n_items - r.next_item) * r.chunk)
         budget = self.round_pairs
         parts, finishing = [], []
@@ -333,14 +336,18 @@ class PrismServer:
             items[:, 1] = k // r.n_chunks  # tile
             items[:, 2] = k % r.n_chunks   # chunk
             items[:, 3] = 0
-            parts.append(items)
+            parts.append((FIELD_CODES[r.field], items))
             r.next_item += take
             budget -= take * per_item
             if r.next_item == r.n_items:
                 finishing.append(r)
-        return np.concatenate(parts), finishing
+        counts = np.zeros(10, dtype=np.int64)
+        for code, items in parts:
+            counts[code] += items.shape[0]
+        order = sorted(range(len(parts)), key=lambda i: parts[i][0])  # stable
+        return np.concatenate([parts[i][1] for i in order]), counts, finishing
 
-    def _launch_round(self, items, finishing):
+    def _launch_round(self, items, counts, finishing):
         torch = self.torch
         buf = self._ring[self._ring_next]
         self._ring_next = (self._ring_next + 1) % len(self._ring)
@@ -362,8 +369,9 @@ class PrismServer:
             self.table_dev.copy_(buf["table"], non_blocking=True)
             items_dev = buf["items"][: items.size].to(self.dev, non_blocking=True)
             stream = self.compute.cuda_stream
+            field_counts = (ctypes.c_int64 * 10)(*counts.tolist())
             _native.check(self.lib.hg_round_run(self.table_dev.data_ptr(), items_dev.data_ptr(),
-                                                items.shape[0], self.n_ctas,
+                                                field_counts, self.n_ctas,
                                                 self.counter.data_ptr(), stream))
             if ids.size:
                 ids_dev = buf["ids"][: ids.size].to(self.dev, non_blocking=True)
@@ -428,9 +436,9 @@ class PrismServer:
                     pass
                 self._admit()
                 if len(self.in_flight) < self.rounds_in_flight:
-                    items, finishing = self._plan_round()
+                    items, counts, finishing = self._plan_round()
                     if items is not None:
-                        self._launch_round(items, finishing)
+                        self._launch_round(items, counts, finishing)
                         continue
                 self._retire(block=len(self.in_flight) >= self.rounds_in_flight)
         except Exception as exc:  # noqa: BLE001 - fail every waiting request

@@ -133,12 +133,12 @@ int hg_layer_forward(const double *obs_e, const double *obs_n, const double *obs
 /*
  * ---------------------------------------------------------------------------
  * Batched forward: many independent problems (each its own points, prisms
- * and ONE field) in one persistent launch.  Replaces a Python loop of
- * harmonica prism_gravity calls (gravity.py:51-236), one per problem, with a
- * single launch whose work items (problem, 128-point tile, prism chunk) are
- * pulled from a device queue by a persistent grid; each point's chunks are
- * added in fixed order, so every result is bitwise the same alone and in any
- * batch.
+ * and ONE field) in one persistent launch per field present.  Replaces a
+ * Python loop of harmonica prism_gravity calls (gravity.py:51-236), one per
+ * problem, with launches whose work items (problem, 128-point tile, prism
+ * chunk) are pulled from a device queue by a persistent grid running that
+ * field's specialised kernel; each point's chunks are added in fixed order,
+ * so every result is bitwise the same alone and in any batch.
  */
 typedef struct hg_problem {
   const double *obs_e;       /* n_obs (device) */
@@ -160,7 +160,8 @@ typedef struct hg_batch hg_batch; /* opaque plan */
  * Build the work list of a batch (host work + two small device copies; the
  * plan keeps device pointers of the problems, which must stay valid until
  * hg_batch_destroy).  chunk_prisms <= 0 and n_ctas <= 0 choose automatically
- * (about 16 work items per CTA; one CTA per free slot of every SM).
+ * (about 16 work items per CTA; per field, one full wave of that field's
+ * kernel).  A given n_ctas applies to every field's launch.
  */
 int hg_batch_create(const hg_problem *problems, int64_t n_problems, int64_t chunk_prisms,
                     int32_t n_ctas, hg_batch **batch);
@@ -168,13 +169,14 @@ int hg_batch_create(const hg_problem *problems, int64_t n_problems, int64_t chun
 /* Bytes of device workspace hg_batch_run needs. */
 int hg_batch_workspace(const hg_batch *batch, size_t *bytes);
 
-/* Work items, persistent CTAs and prism-point pairs of the plan. */
+/* Work items, persistent CTAs (of the g_z launch, or the given count) and prism-point pairs. */
 int hg_batch_info(const hg_batch *batch, int64_t *n_items, int64_t *n_ctas, double *pairs);
 
 /*
- * Run the batch on `stream`: one memset and two launches, no allocation and
- * no host synchronisation (capturable in a CUDA graph; replays recompute
- * from the current contents of the problems' input buffers).
+ * Run the batch on `stream`: one memset, one launch per field present and
+ * one reduction launch, no allocation and no host synchronisation
+ * (capturable in a CUDA graph; replays recompute from the current contents
+ * of the problems' input buffers).
  */
 int hg_batch_run(const hg_batch *batch, void *workspace, size_t workspace_bytes, void *stream);
 
@@ -217,12 +219,15 @@ typedef struct hg_work_item {
 } hg_work_item;
 
 /*
- * Run n_items items (device array) over the problem table (device array)
- * with n_ctas persistent CTAs (<= 0: one per free slot of every SM).
- * `counter` is 8 bytes of device memory the call zeroes and uses.
+ * Run one round: the items (device array) are grouped by field, in field-code
+ * order, with field_counts[f] (host array of 10) items of field f; every
+ * field present gets its own persistent launch over the problem table
+ * (device array) with n_ctas CTAs (<= 0: one full wave of that field's
+ * kernel).  `counter` is 80 bytes of device memory (one counter per field)
+ * the call zeroes and uses.
  */
-int hg_round_run(const hg_problem_plan *problems, const hg_work_item *items, int64_t n_items,
-                 int32_t n_ctas, void *counter, void *stream);
+int hg_round_run(const hg_problem_plan *problems, const hg_work_item *items,
+                 const int64_t *field_counts, int32_t n_ctas, void *counter, void *stream);
 
 /* out = units * sum over chunks of partials, for the listed problems (device int32 ids). */
 int hg_round_reduce(const hg_problem_plan *problems, const int32_t *problem_ids, int64_t n_ids,
