@@ -83,6 +83,7 @@ struct LayerSource {
 // ---------------------------------------------------------------------------
 struct SmemTile {
   double w[kTile], e[kTile], s[kTile], n[kTile], b[kTile], t[kTile], rho[kTile];
+  double dx[kTile], dy[kTile], dz[kTile];  // extents
   int null[kTile];
 };
 
@@ -90,6 +91,7 @@ struct SmemTables {
   double logc[lean::kLogTableSize], logl[lean::kLogTableSize];
   double th[lean::kArgTableSize];
   float csf[2 * lean::kArgTableSize], snf[2 * lean::kArgTableSize];
+  float loglf[2 * lean::kLogTableSize], thf[2 * lean::kArgTableSize];
 
   // Copy the constant tables of lean_math.cuh; the caller synchronises.
   __device__ __forceinline__ Tables stage() {
@@ -101,8 +103,10 @@ struct SmemTables {
     for (int t = threadIdx.x; t < 2 * lean::kArgTableSize; t += blockDim.x) {
       csf[t] = lean::kArgCosF[t];
       snf[t] = lean::kArgSinF[t];
+      thf[t] = lean::kArgThF[t];
     }
-    return Tables{logc, logl, th, csf, snf};
+    for (int t = threadIdx.x; t < 2 * lean::kLogTableSize; t += blockDim.x) loglf[t] = lean::kLogLF[t];
+    return Tables{logc, logl, th, csf, snf, loglf, thf};
   }
 };
 
@@ -131,6 +135,9 @@ __device__ __forceinline__ void accumulate(const Source& src, int64_t p0, int64_
       sh.b[threadIdx.x] = b;
       sh.t[threadIdx.x] = t;
       sh.rho[threadIdx.x] = rho;
+      sh.dx[threadIdx.x] = e - w;
+      sh.dy[threadIdx.x] = n - s;
+      sh.dz[threadIdx.x] = t - b;
       sh.null[threadIdx.x] = null;
     }
     __syncthreads();
@@ -142,6 +149,9 @@ __device__ __forceinline__ void accumulate(const Source& src, int64_t p0, int64_
       q.y2 = sh.n[p] - pn;
       q.z1 = sh.b[p] - pu;
       q.z2 = sh.t[p] - pu;
+      q.dx = sh.dx[p];
+      q.dy = sh.dy[p];
+      q.dz = sh.dz[p];
       if (check_singular && active) {
 #pragma unroll
         for (int f = kGee; f <= kGnz; f++)

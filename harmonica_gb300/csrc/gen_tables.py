@@ -12,7 +12,8 @@ functions in lean_math.cuh, correctly rounded with mpmath.
   sine of the double TH[j]; COSF/SINF hold the same cosine and sine as
   float pairs (hi = nearest float, lo = nearest float to the remainder),
   interleaved hi, lo.
-* kThirdHi/kThirdLo: 1/3 as a float pair.
+* kThirdHi/kThirdLo: 1/3 as a float pair; LOGLF = -ln C[k] and THF = TH[j]
+  as float pairs; ln 2 and pi/2 as three floats (12-bit head).
 
 Run:  python harmonica_gb300/csrc/gen_tables.py   (writes next to this file)
 """
@@ -87,6 +88,28 @@ def main():
     hi, lo = f32pair(mp.mpf(1) / 3)
     lines.append(f"constexpr float kThirdHi = {fl(hi)};")
     lines.append(f"constexpr float kThirdLo = {fl(lo)};")
+    # -ln(C[k]) and TH[j] as float pairs, interleaved hi, lo
+    lines.append("HG_TABLE_QUAL float kLogLF[2 * kLogTableSize] = {")
+    for ck in c:
+        hi, lo = f32pair(-mp.log(mp.mpf(ck)))
+        lines.append(f"    {fl(hi)}, {fl(lo)},")
+    lines.append("};")
+    lines.append("HG_TABLE_QUAL float kArgThF[2 * kArgTableSize] = {")
+    for j in range(-32, 33):
+        hi, lo = f32pair(mp.mpf(j) * mp.pi / 128)
+        lines.append(f"    {fl(hi)}, {fl(lo)},")
+    lines.append("};")
+    # ln 2 and pi/2 as three floats: the first with 12 significant bits (an
+    # integer of up to 12 bits times it is exact in a float), the second the
+    # nearest float to the remainder, the third the nearest to what is left
+    for name, val in (("Ln2", mp.log(2)), ("Pio2", mp.pi / 2)):
+        m, e = mp.frexp(val)
+        f1 = float(mp.ldexp(mp.floor(mp.ldexp(m, 12)), e - 12))
+        f2 = float(np.float32(float(val - mp.mpf(f1))))
+        f3 = float(np.float32(float(val - mp.mpf(f1) - mp.mpf(f2))))
+        lines.append(f"constexpr float k{name}F1 = {fl(f1)};")
+        lines.append(f"constexpr float k{name}F2 = {fl(f2)};")
+        lines.append(f"constexpr float k{name}F3 = {fl(f3)};")
     # constants split in a high part with 40 significant bits (so that an
     # integer of up to 13 bits times the high part is exact) and a low part
     for name, val in (("Ln2", mp.log(2)), ("Pio2", mp.pi / 2)):

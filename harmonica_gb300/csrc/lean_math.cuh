@@ -263,6 +263,11 @@ HG_HD __forceinline__ F2 f2_add(F2 a, F2 b) {
   return quick_two_sum(s.h, fadd(s.l, fadd(a.l, b.l)));
 }
 HG_HD __forceinline__ F2 f2_neg(F2 a) { return F2{-a.h, -a.l}; }
+HG_HD __forceinline__ F2 f2_sub(F2 a, F2 b) { return f2_add(a, f2_neg(b)); }
+HG_HD __forceinline__ F2 f2_sq(F2 a) {
+  const F2 p = two_prod(a.h, a.h);
+  return quick_two_sum(p.h, ffma(2.0f * a.h, a.l, p.l));
+}
 
 // a / b for b > 0: FP32 reciprocal refined to float accuracy, the quotient
 // rounded to a float and one correction from the exact-by-FMA residual.
@@ -274,6 +279,18 @@ HG_HD __forceinline__ F2 f2_div(F2 a, F2 b) {
   r = fadd(r, a.l);
   r = ffma(-qh, b.l, r);
   return F2{qh, fmul(r, y)};
+}
+
+// sqrt(a) for a pair a > 0 (normal): FP32 rsqrt seed refined to float
+// accuracy, s = a.h y, one Newton correction from the pair residual
+// a - s^2 (exact product by FMA): ~2^-46.
+HG_HD __forceinline__ F2 f2_sqrt(F2 a) {
+  float y = rsqrt_approx(a.h);
+  y = fmul(y, ffma(fmul(-0.5f, a.h), fmul(y, y), 1.5f));
+  const float s = fmul(a.h, y);
+  const F2 s2 = two_prod(s, s);
+  const float res = fadd(fsub(fsub(a.h, s2.h), s2.l), a.l);
+  return quick_two_sum(s, fmul(res, fmul(0.5f, y)));
 }
 
 // The significand of a normal double (bits b) as a pair in [1, 2):
@@ -389,16 +406,18 @@ struct Tables {
   const double* logc;
   const double* logl;
   const double* th;
-  const float* csf;  // cos(th_j) as float pairs (hi, lo)
-  const float* snf;  // sin(th_j) as float pairs
+  const float* csf;    // cos(th_j) as float pairs (hi, lo)
+  const float* snf;    // sin(th_j) as float pairs
+  const float* loglf;  // -ln(c_k) as float pairs
+  const float* thf;    // th_j as float pairs
 };
 
 // Host view of the tables (the device kernels stage them in shared memory).
 inline Tables host_tables() {
 #ifdef __CUDA_ARCH__
-  return Tables{nullptr, nullptr, nullptr, nullptr, nullptr};
+  return Tables{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
 #else
-  return Tables{kLogC, kLogL, kArgTh, kArgCosF, kArgSinF};
+  return Tables{kLogC, kLogL, kArgTh, kArgCosF, kArgSinF, kLogLF, kArgThF};
 #endif
 }
 
@@ -491,14 +510,104 @@ HG_HD __forceinline__ double lm_arg_near(double pr, double pi, float est, const 
   return arg_core(scaled_f2(br, top), scaled_f2(bi, top), q, j, T);
 }
 
+// A double as a float pair (values below 2^-120 in magnitude give 0).
+HG_HD __forceinline__ F2 double_to_f2(double x) { return scaled_f2(d2ll(x), 1023); }
+
+// arg_core with the result as a float pair: theta_j and q pi/2 added on
+// pairs (no FP64 instruction on the fast path).
+HG_HD __forceinline__ F2 arg_core_f2(F2 re, F2 im, int q, int j, const Tables& T) {
+  const F2 re0 = re, im0 = im;
+  if (j != 0) {  // rotate by -th_j
+    const int jj = 2 * (j + kArgTableHalf);
+    const F2 C{T.csf[jj], T.csf[jj + 1]}, S{T.snf[jj], T.snf[jj + 1]};
+    const F2 r2 = f2_add(f2_mul(re, C), f2_mul(im, S));
+    im = f2_add(f2_mul(im, C), f2_neg(f2_mul(re, S)));
+    re = r2;
+  }
+  const F2 u = f2_div(im, re);
+  F2 a;
+  if (re.h > 0.0f && fabsf(u.h) < 0.02f) {
+    F2 s2 = two_prod(u.h, u.h);
+    s2.l = ffma(2.0f * u.h, u.l, s2.l);  // u^2
+    F2 w = two_prod(s2.h, u.h);
+    w.l = ffma(s2.h, u.l, ffma(s2.l, u.h, w.l));  // u^3
+    const float tail = fmul(s2.h, ffma(s2.h, -0.142857143f, 0.2f));  // u^2/5 - u^4/7
+    F2 c = two_prod(w.h, -kThirdHi);
+    c.l = ffma(w.h, fsub(tail, kThirdLo), ffma(w.l, -kThirdHi, c.l));  // u^3 (-1/3 + tail)
+    a = quick_two_sum(u.h, c.h);
+    a.l = fadd(a.l, fadd(u.l, c.l));
+  } else {
+    // estimate too far off or non-finite input: generic path on the
+    // quarter-turn-rotated vector
+    a = double_to_f2(cold_atan2(f2_to_double(im0, 0), f2_to_double(re0, 0)));
+    j = 0;
+  }
+  if (j != 0) {
+    const int jj = 2 * (j + kArgTableHalf);
+    a = f2_add(a, F2{T.thf[jj], T.thf[jj + 1]});
+  }
+  if (q != 0) {  // q pi/2 with pi/2 in three floats (q * F1 exact)
+    const float qf = (float)q;
+    F2 p = two_prod(qf, kPio2F2);
+    p.l = ffma(qf, kPio2F3, p.l);
+    a = f2_add(a, f2_add(F2{fmul(qf, kPio2F1), 0.0f}, p));
+  }
+  return a;
+}
+
 // The same for a vector given as float pairs (finite, magnitude ~1).
-HG_HD __forceinline__ double lm_arg_near_f2(F2 pr, F2 pi, float est, const Tables& T) {
+HG_HD __forceinline__ F2 lm_arg_near_f2(F2 pr, F2 pi, float est, const Tables& T) {
   int q, j;
   arg_plan(est, q, j);
   const int qm = q & 3;
   const F2 r0 = qm == 0 ? pr : (qm == 1 ? pi : (qm == 2 ? f2_neg(pr) : f2_neg(pi)));
   const F2 i0 = qm == 0 ? pi : (qm == 1 ? f2_neg(pr) : (qm == 2 ? f2_neg(pi) : pr));
-  return arg_core(r0, i0, q, j, T);
+  return arg_core_f2(r0, i0, q, j, T);
+}
+
+// log1p(t) for |t| <= 2^-8.5 on float pairs:
+//   t - t^2/2 + t^3 (1/3 - t/4 + t^2/5 - t^3/6)
+// with t, t^2, t^3 and 1/3 as pairs and the tail in FP32 (~2^-47 relative).
+HG_HD __forceinline__ F2 log1p_series_f2(F2 t) {
+  F2 s2 = two_prod(t.h, t.h);
+  s2.l = ffma(2.0f * t.h, t.l, s2.l);  // t^2
+  F2 w = two_prod(s2.h, t.h);
+  w.l = ffma(s2.h, t.l, ffma(s2.l, t.h, w.l));  // t^3
+  const float tail = fmul(t.h, ffma(t.h, ffma(t.h, -0.166666672f, 0.2f), -0.25f));
+  F2 c = two_prod(w.h, kThirdHi);
+  c.l = ffma(w.h, fadd(tail, kThirdLo), ffma(w.l, kThirdHi, c.l));  // t^3 (1/3 + tail)
+  F2 v = quick_two_sum(fmul(-0.5f, s2.h), c.h);
+  v.l = fadd(v.l, ffma(-0.5f, s2.l, c.l));
+  F2 lp = quick_two_sum(t.h, v.h);
+  lp.l = fadd(lp.l, fadd(t.l, v.l));
+  return lp;
+}
+
+// ln(1 + t) for t > -1 on float pairs (t given accurately, as from a
+// cancellation-free numerator).  Small |t|: the series.  Otherwise Tang's
+// reduction of w = 1 + t = 2^E m with c_k ~ 1/m from the table, the reduced
+// argument formed as t c' + (c' - 1) (c' = c_k 2^-E; c' - 1 exact), so no
+// digit of t is lost, then E ln2 - ln c_k + log1p(reduced) on pairs.
+HG_HD __forceinline__ F2 log1p_f2(F2 t, const Tables& T) {
+  if (fabsf(t.h) < 0.0026f) return log1p_series_f2(t);
+  const F2 w = f2_add(F2{1.0f, 0.0f}, t);
+  const unsigned uw = f2u(w.h);
+  int E = (int)((uw >> 23) & 0xffu) - 127;
+  float m = u2f((uw & 0x7fffffu) | 0x3f800000u);  // [1, 2)
+  if (m >= 1.5f) {
+    m = fmul(m, 0.5f);
+    E += 1;
+  }
+  int k = round_to_int((m - 0.75f) * 256.0f);
+  k = k < 0 ? 0 : (k > kLogTableSize - 1 ? kLogTableSize - 1 : k);
+  const float cp = fmul(d2f_trunc(T.logc[k]), pow2f(-E));  // c_k is a float: exact
+  const F2 red = f2_add(f2_mul(t, F2{cp, 0.0f}), two_sum(cp, -1.0f));
+  const F2 lp = log1p_series_f2(red);
+  const float ef = (float)E;
+  F2 e2 = two_prod(ef, kLn2F2);
+  e2.l = ffma(ef, kLn2F3, e2.l);
+  const F2 eln2 = f2_add(F2{fmul(ef, kLn2F1), 0.0f}, e2);  // E ln 2 (E * F1 exact)
+  return f2_add(f2_add(eln2, F2{T.loglf[2 * k], T.loglf[2 * k + 1]}), lp);
 }
 
 // ln((p1 p2) / (q1 q2)) for positive normal arguments, without forming the
@@ -562,18 +671,7 @@ HG_HD __forceinline__ double lm_log_quot(double p1, double p2, double q1, double
   t.l = fmul(t.l, scale);
   if (bn < 0) t = f2_neg(t);
   if (en == 0 || sc < -120) t = F2{0.0f, 0.0f};  // |t| < 2^-120 counts as 0
-  F2 s2 = two_prod(t.h, t.h);
-  s2.l = ffma(2.0f * t.h, t.l, s2.l);  // t^2
-  F2 w = two_prod(s2.h, t.h);
-  w.l = ffma(s2.h, t.l, ffma(s2.l, t.h, w.l));  // t^3
-  const float tail = fmul(t.h, ffma(t.h, ffma(t.h, -0.166666672f, 0.2f), -0.25f));
-  F2 c = two_prod(w.h, kThirdHi);
-  c.l = ffma(w.h, fadd(tail, kThirdLo), ffma(w.l, kThirdHi, c.l));  // t^3 (1/3 + tail)
-  F2 v = quick_two_sum(fmul(-0.5f, s2.h), c.h);
-  v.l = fadd(v.l, ffma(-0.5f, s2.l, c.l));
-  F2 lp = quick_two_sum(t.h, v.h);
-  lp.l = fadd(lp.l, fadd(t.l, v.l));
-  const double p = f2_to_double(lp, 0);  // log1p(t)
+  const double p = f2_to_double(log1p_series_f2(t), 0);  // log1p(t)
   if (near1) return p;
   const double edd = small_int_to_double(E);
   return fma(edd, kLn2Hi, T.logl[k]) + fma(edd, kLn2Lo, p);

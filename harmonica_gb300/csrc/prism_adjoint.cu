@@ -68,6 +68,9 @@ __global__ void __launch_bounds__(kThreads) adjoint_kernel(
       q.y2 = n - sh.n[k];
       q.z1 = b - sh.u[k];
       q.z2 = t - sh.u[k];
+      q.dx = e - w;
+      q.dy = n - s;
+      q.dz = t - b;
       const double wk = sh.w[k];
       if (F == kGz) {
         double ob, ot;

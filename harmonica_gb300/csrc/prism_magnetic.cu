@@ -76,6 +76,9 @@ __global__ void __launch_bounds__(kThreads) magnetic_kernel(
       q.y2 = sh.n[p] - pn;
       q.z1 = sh.b[p] - pu;
       q.z2 = sh.t[p] - pu;
+      q.dx = sh.e[p] - sh.w[p];
+      q.dy = sh.n[p] - sh.s[p];
+      q.dz = sh.t[p] - sh.b[p];
       const double me = sh.me[p], mn = sh.mn[p], mu = sh.mu[p];
       double t6[6];
       pair_tensor6<true>(q, T, t6);  // ee nn uu en eu nu

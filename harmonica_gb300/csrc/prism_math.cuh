@@ -143,9 +143,12 @@ template <> struct Math<false> {
 };
 
 // ---------------------------------------------------------------------------
-// Observation-relative bounds of one (point, prism) pair.
+// Observation-relative bounds of one (point, prism) pair, and the prism's
+// extents (east - west, north - south, top - bottom: exact, not differences
+// of the relative bounds).
 struct Rel {
   double x1, x2, y1, y2, z1, z2;
+  double dx, dy, dz;
 };
 
 // Singular-point predicates; they mirror choclo's
@@ -398,13 +401,45 @@ HG_HD __forceinline__ void pair_complex_f2(lean::F2 aa, lean::F2 asq, lean::F2 b
   im = f2_mul(f2_mul(aa, c), d);
 }
 
-// Face angle on float pairs: every length is scaled by 2^-s, s the exponent
-// of the largest vertex distance of the face (the distances bound all
-// coordinates).  Returns false (and leaves o) when a nonzero coordinate or the
-// face width is below 2^-16 of that scale: then a product of up to six
+// Face angle on float pairs, inputs already float pairs at a common scale
+// where the largest of the face's vertex distances is in [1, 2): |a| (the
+// caller applies the sign of a), the in-plane coordinates, the four vertex
+// distances and the width b2 - b1 (given separately: no cancellation).
+// A and B are each scaled by a power of two before the product A conj(B).
+HG_HD __forceinline__ lean::F2 face_core_f2(lean::F2 fa, lean::F2 fb1, lean::F2 fb2,
+                                            lean::F2 fc1, lean::F2 fc2, lean::F2 fr11,
+                                            lean::F2 fr12, lean::F2 fr21, lean::F2 fr22,
+                                            lean::F2 fw, bool same_sign, const Tables& T) {
+  using namespace lean;
+  F2 asq = two_prod(fa.h, fa.h);
+  asq.l = ffma(2.0f * fa.h, fa.l, asq.l);
+  F2 c1sq = two_prod(fc1.h, fc1.h), c2sq = two_prod(fc2.h, fc2.h);
+  c1sq.l = ffma(2.0f * fc1.h, fc1.l, c1sq.l);
+  c2sq.l = ffma(2.0f * fc2.h, fc2.l, c2sq.l);
+  F2 bdq1{0.0f, 0.0f}, bdq2{0.0f, 0.0f};
+  if (same_sign) {
+    // bdiff = (b2 - b1)(b2 + b1): the width from the caller, the same-sign sum
+    const F2 fbd = f2_mul(fw, f2_add(fb2, fb1));
+    bdq1 = f2_mul(fbd, f2_add(asq, c1sq));
+    bdq2 = f2_mul(fbd, f2_add(asq, c2sq));
+  }
+  F2 ar, ai, br, bi;
+  pair_complex_f2(fa, asq, fb1, fb2, fc2, c2sq, fr12, fr22, same_sign, bdq2, ar, ai);
+  pair_complex_f2(fa, asq, fb1, fb2, fc1, c1sq, fr11, fr21, same_sign, bdq1, br, bi);
+  normalize_f2c(ar, ai);
+  normalize_f2c(br, bi);
+  const float est = atan2_est(ai.h, ar.h) - atan2_est(bi.h, br.h);
+  const F2 pr = f2_add(f2_mul(ar, br), f2_mul(ai, bi));
+  const F2 pim = f2_add(f2_mul(ai, br), f2_neg(f2_mul(ar, bi)));
+  return lm_arg_near_f2(pr, pim, est, T);
+}
+
+// Face angle from FP64 inputs: every length is scaled by 2^-s, s the
+// exponent of the largest vertex distance of the face (the distances bound
+// all coordinates).  Returns false (and leaves o) when a nonzero coordinate
+// or the face width is below 2^-16 of that scale: then a product of up to six
 // scaled lengths could leave the normal float range, and the caller takes the
 // FP64 path (a point within ~1e-5 face sizes of an edge line or face plane).
-// A and B are each scaled by a power of two before the product A conj(B).
 HG_HD __forceinline__ bool face_angle_f2(double a, double b1, double b2, double c1, double c2,
                                          double r11, double r12, double r21, double r22,
                                          bool same_sign, double width, const Tables& T,
@@ -420,33 +455,10 @@ HG_HD __forceinline__ bool face_angle_f2(double a, double b1, double b2, double 
   if (small(a) || small(b1) || small(b2) || small(c1) || small(c2) || top >= 0x7fe ||
       ex(width) < lim)
     return false;
-  const F2 fa = scaled_f2(d2ll(abs_bits(a)), top);
-  const F2 fb1 = scaled_f2(d2ll(b1), top), fb2 = scaled_f2(d2ll(b2), top);
-  const F2 fc1 = scaled_f2(d2ll(c1), top), fc2 = scaled_f2(d2ll(c2), top);
-  F2 asq = two_prod(fa.h, fa.h);
-  asq.l = ffma(2.0f * fa.h, fa.l, asq.l);
-  F2 c1sq = two_prod(fc1.h, fc1.h), c2sq = two_prod(fc2.h, fc2.h);
-  c1sq.l = ffma(2.0f * fc1.h, fc1.l, c1sq.l);
-  c2sq.l = ffma(2.0f * fc2.h, fc2.l, c2sq.l);
-  F2 bdq1{0.0f, 0.0f}, bdq2{0.0f, 0.0f};
-  if (same_sign) {
-    // bdiff = (b2 - b1)(b2 + b1): the width from FP64 (no cancellation), the
-    // same-sign sum on pairs
-    const F2 fbd = f2_mul(scaled_f2(d2ll(width), top), f2_add(fb2, fb1));
-    bdq1 = f2_mul(fbd, f2_add(asq, c1sq));
-    bdq2 = f2_mul(fbd, f2_add(asq, c2sq));
-  }
-  F2 ar, ai, br, bi;
-  pair_complex_f2(fa, asq, fb1, fb2, fc2, c2sq, scaled_f2(d2ll(r12), top),
-                  scaled_f2(d2ll(r22), top), same_sign, bdq2, ar, ai);
-  pair_complex_f2(fa, asq, fb1, fb2, fc1, c1sq, scaled_f2(d2ll(r11), top),
-                  scaled_f2(d2ll(r21), top), same_sign, bdq1, br, bi);
-  normalize_f2c(ar, ai);
-  normalize_f2c(br, bi);
-  const float est = atan2_est(ai.h, ar.h) - atan2_est(bi.h, br.h);
-  const F2 pr = f2_add(f2_mul(ar, br), f2_mul(ai, bi));
-  const F2 pim = f2_add(f2_mul(ai, br), f2_neg(f2_mul(ar, bi)));
-  o = lm_arg_near_f2(pr, pim, est, T);
+  const auto f = [&](double v) { return scaled_f2(d2ll(v), top); };
+  o = f2_to_double(face_core_f2(f(abs_bits(a)), f(b1), f(b2), f(c1), f(c2), f(r11), f(r12),
+                                f(r21), f(r22), f(width), same_sign, T),
+                   0);
   return true;
 }
 
@@ -634,6 +646,141 @@ HG_HD __forceinline__ double merged_logs4(const EdgeSet& E0, const EdgeSet& E1, 
 }
 
 // ---------------------------------------------------------------------------
+// g_z of one pair on float pairs.
+//
+// Every length of the pair is scaled by 2^-s (s: the exponent of its largest
+// coordinate) and held as a float pair; vertex distances by float-pair square
+// roots; the four merged edge logs from cancellation-free numerators
+// (merged_t); the two face angles by face_core_f2; the combination summed on
+// pairs and returned as a double (integer assembly).  No FP64 instruction on
+// this path.  Pairs whose scaled geometry could leave the float range (a
+// nonzero coordinate below 2^-40 of the scale, a vertex distance or extent
+// below 2^-20, a face coordinate below 2^-16 of its face) take the FP64 path.
+
+// t = R(u1) / R(u0) - 1 for the merged log of the two edges parallel to one
+// axis at in-plane offset v, at u0 and u1 = u0 + du (su = u0 + u1), with edge
+// ends lo < hi after reflection (lo < 0 only when the point projects inside
+// the edge) and vertex distances rl0 = r(lo, u0), rl1 = r(lo, u1), rh0, rh1.
+// With dQ = u1^2 - u0^2 = du su, Dl = dQ / (rl1 + rl0) = rl1 - rl0, Dh
+// likewise, P_k = rl_k + rh_k, Sl = rl0 + rl1, Sh = rh0 + rh1:
+//   lo >= 0: R = (hi + rh)/(lo + rl), D = lo + rl, N = hi + rh,
+//       t = -dA [Dl + (hi + lo)(D0 (Dl + Dh) + Dl P1) / (P0 P1)] / (D1 N0)
+//   lo < 0:  R = (hi + rh)(rl - lo)/(v^2 + u^2), M = rl - lo,
+//       X = rh0 Dl - rl0 Dh - hi Sl + lo Sh,
+//       t = dQ M1 X / (Sh Sl M0 (v^2 + u1^2))
+// (both follow from expanding N1 D0 - D1 N0, resp. the products, in the
+// differences Dl, Dh).  Every sum adds terms of one sign, so t keeps its
+// relative accuracy however far the prism is; the direct numerator
+// N1 D0 - D1 N0 loses it with the square of the distance.
+HG_HD __forceinline__ lean::F2 merged_t(bool straddle, lean::F2 lo, lean::F2 hi, lean::F2 v,
+                                        lean::F2 u1, lean::F2 rl0, lean::F2 rl1, lean::F2 rh0,
+                                        lean::F2 rh1, lean::F2 dA, lean::F2 du, lean::F2 su) {
+  using namespace lean;
+  const F2 dQ = f2_mul(du, su);
+  const F2 Sl = f2_add(rl0, rl1), Sh = f2_add(rh0, rh1);
+  const F2 Dl = f2_div(dQ, Sl), Dh = f2_div(dQ, Sh);
+  if (!straddle) {
+    const F2 D0 = f2_add(lo, rl0), D1 = f2_add(lo, rl1), N0 = f2_add(hi, rh0);
+    const F2 P0 = f2_add(rl0, rh0), P1 = f2_add(rl1, rh1);
+    const F2 inner = f2_add(f2_mul(D0, f2_add(Dl, Dh)), f2_mul(Dl, P1));
+    const F2 br = f2_add(Dl, f2_div(f2_mul(f2_add(hi, lo), inner), f2_mul(P0, P1)));
+    return f2_neg(f2_div(f2_mul(dA, br), f2_mul(D1, N0)));
+  }
+  const F2 M0 = f2_sub(rl0, lo), M1 = f2_sub(rl1, lo);
+  const F2 Q1 = f2_add(f2_sq(v), f2_sq(u1));
+  const F2 X = f2_add(f2_add(f2_mul(rh0, Dl), f2_neg(f2_mul(rl0, Dh))),
+                      f2_add(f2_neg(f2_mul(hi, Sl)), f2_mul(lo, Sh)));
+  return f2_div(f2_mul(f2_mul(dQ, M1), X), f2_mul(f2_mul(Sh, Sl), f2_mul(M0, Q1)));
+}
+
+// The FP64 evaluation of g_z, for the pairs the float-pair path declines.
+HG_COLD double pair_gz_fp64(const Rel& q, const Tables& T);
+
+HG_HD __forceinline__ double pair_gz_f2(const Rel& q, const Tables& T) {
+  using namespace lean;
+  const auto ex = [](double v) { return (int)((hi_word(v) >> 20) & 0x7ffu); };
+  int top = max(max(ex(q.x1), ex(q.x2)), max(max(ex(q.y1), ex(q.y2)), max(ex(q.z1), ex(q.z2))));
+  const auto tiny_nz = [&](double v) { return !is_tiny(v) && ex(v) < top - 40; };
+  if (top >= 0x7fe || tiny_nz(q.x1) || tiny_nz(q.x2) || tiny_nz(q.y1) || tiny_nz(q.y2) ||
+      tiny_nz(q.z1) || tiny_nz(q.z2) || ex(q.dx) < top - 20 || ex(q.dy) < top - 20 ||
+      ex(q.dz) < top - 20)
+    return pair_gz_fp64(q, T);
+  const auto f = [&](double v) { return scaled_f2(d2ll(v), top); };
+  const F2 x[2] = {f(q.x1), f(q.x2)}, y[2] = {f(q.y1), f(q.y2)}, z[2] = {f(q.z1), f(q.z2)};
+  const F2 dx = f(q.dx), dy = f(q.dy), dz = f(q.dz);
+  F2 r[2][2][2];
+  {
+    const F2 x2[2] = {f2_sq(x[0]), f2_sq(x[1])}, y2[2] = {f2_sq(y[0]), f2_sq(y[1])};
+    const F2 z2[2] = {f2_sq(z[0]), f2_sq(z[1])};
+    bool ok = true;
+#pragma unroll
+    for (int i = 0; i < 2; i++)
+#pragma unroll
+      for (int k = 0; k < 2; k++) {
+        const F2 xz = f2_add(x2[i], z2[k]);
+#pragma unroll
+        for (int j = 0; j < 2; j++) {
+          r[i][j][k] = f2_sqrt(f2_add(xz, y2[j]));
+          ok = ok && r[i][j][k].h >= 0x1p-20f;
+        }
+      }
+    if (!ok) return pair_gz_fp64(q, T);
+  }
+  // edge cases of the x and y axes (from the FP64 bounds: exact decisions)
+  const AxisCase cx = axis_case(q.x1, q.x2), cy = axis_case(q.y1, q.y2);
+  const F2 sz = f2_add(z[0], z[1]);
+  F2 v{0.0f, 0.0f};
+#pragma unroll 1
+  for (int m = 0; m < 4; m++) {
+    // m = 0, 1: y-edges at x_m (coefficient x_m); m = 2, 3: x-edges at y_(m-2)
+    const bool b = m & 1, yx = m >= 2;
+    const AxisCase c = yx ? cx : cy;
+    const F2 a1 = yx ? x[0] : y[0], a2 = yx ? x[1] : y[1];
+    const F2 lo = c.reflect ? f2_neg(a2) : a1, hi = c.reflect ? f2_neg(a1) : a2;
+    const int il = c.reflect ? 1 : 0;  // index of the lo end along the edge axis
+    // vertex distances r(lo/hi end, z_k) of this edge pair
+    const auto rv = [&](int end, int k) {
+      const F2 ry = b ? r[1][end][k] : r[0][end][k];  // y-edge at x_b: r[b][end][k]
+      const F2 rx = b ? r[end][1][k] : r[end][0][k];  // x-edge at y_b: r[end][b][k]
+      return yx ? rx : ry;
+    };
+    const F2 rl0 = il ? rv(1, 0) : rv(0, 0), rl1 = il ? rv(1, 1) : rv(0, 1);
+    const F2 rh0 = il ? rv(0, 0) : rv(1, 0), rh1 = il ? rv(0, 1) : rv(1, 1);
+    const F2 off = yx ? (b ? y[1] : y[0]) : (b ? x[1] : x[0]);  // coefficient and in-plane offset
+    const F2 t = merged_t(c.straddle, lo, hi, off, z[1], rl0, rl1, rh0, rh1, yx ? dx : dy, dz, sz);
+    const F2 L = log1p_f2(t, T);
+    // s_b * off * L, s_0 = -1
+    if (off.h != 0.0f) v = f2_add(v, f2_mul(b ? off : f2_neg(off), L));
+  }
+  // faces normal to z: - s_k z_k O_k
+  const bool same_sign = !(neg_not_tiny(q.x1) && !nonpos_or_tiny(q.x2));
+#pragma unroll 1
+  for (int k = 0; k < 2; k++) {
+    const double zd = k ? q.z2 : q.z1;
+    const F2 zk = k ? z[1] : z[0];
+    if (is_tiny(zd)) continue;  // the point in the face plane: zero coefficient, finite O
+    const F2 r11 = k ? r[0][0][1] : r[0][0][0], r12 = k ? r[0][1][1] : r[0][1][0];
+    const F2 r21 = k ? r[1][0][1] : r[1][0][0], r22 = k ? r[1][1][1] : r[1][1][0];
+    // rescale the face so that its largest vertex distance is in [1, 2)
+    const auto fe = [](F2 a) { return (int)((f2u(a.h) >> 23) & 0xffu); };
+    const int ftop = max(max(fe(r11), fe(r12)), max(fe(r21), fe(r22)));
+    const float sc = pow2f(127 - ftop);
+    const auto g = [&](F2 a) { return F2{fmul(a.h, sc), fmul(a.l, sc)}; };
+    const auto fsmall = [&](F2 a) { return a.h != 0.0f && fe(a) < ftop - 16; };
+    const F2 za = zk;
+    if (fsmall(za) || fsmall(x[0]) || fsmall(x[1]) || fsmall(y[0]) || fsmall(y[1]) ||
+        fe(dx) < ftop - 16)
+      return pair_gz_fp64(q, T);
+    F2 o = face_core_f2(g(za.h < 0.0f ? f2_neg(za) : za), g(x[0]), g(x[1]), g(y[0]), g(y[1]),
+                        g(r11), g(r12), g(r21), g(r22), g(dx), same_sign, T);
+    if (za.h < 0.0f) o = f2_neg(o);
+    // - s_k z_k O_k: +z_0 O_0, -z_1 O_1
+    v = f2_add(v, f2_mul(k ? f2_neg(zk) : zk, o));
+  }
+  return f2_to_double(v, top - 1023);
+}
+
+// ---------------------------------------------------------------------------
 // All ten fields of one pair: the signed edge/face combinations (without G,
 // rho and units).  s = -1 for index 0 (lower bound), +1 for index 1 (upper).
 template <bool LEAN>
@@ -702,6 +849,7 @@ HG_HD __forceinline__ double pair_field(const Rel& q, const Tables& T) {
   Geom g;
   make_geom<LEAN>(q, g);
   if (F == kGz) {
+    if (LEAN) return pair_gz_f2(q, T);
     // sum_i s_i x_i sum_k s_k Ly[i][k] + sum_j s_j y_j sum_k s_k Lx[j][k]
     //   - sum_k s_k z_k Oz[k]
     EdgeSet Ey, Ex;
@@ -739,6 +887,18 @@ HG_HD __forceinline__ double pair_field(const Rel& q, const Tables& T) {
     return log_quot<LEAN>(E.num[1][1] * E.num[0][0], E.den[0][1] * E.den[1][0],
                           E.den[1][1] * E.den[0][0], E.num[0][1] * E.num[1][0], T);
   }
+}
+
+// g_z in FP64 (edge sums, exact near-1 log numerators, FP64-input faces).
+HG_COLD double pair_gz_fp64(const Rel& q, const Tables& T) {
+  Geom g;
+  make_geom<true>(q, g);
+  EdgeSet Ey, Ex;
+  edges_y(g, Ey);
+  edges_x(g, Ex);
+  const double v =
+      merged_logs4<true, false, false>(Ey, Ex, g.x[0], g.x[1], g.y[0], g.y[1], T, 0.0);
+  return faces2_dot<2, true>(g, g.z[0], g.z[1], T, v);
 }
 
 // The six gradient-tensor combinations of one pair (the second derivatives

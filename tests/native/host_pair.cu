@@ -39,7 +39,8 @@ void host_prism_gravity(int field, int64_t n_obs, const double* e, const double*
     for (int64_t j = 0; j < m; j++) {
       const double* p = prisms + 6 * j;
       if (p[0] == p[1] || p[2] == p[3] || p[4] == p[5] || rho[j] == 0.0) continue;
-      Rel q{p[0] - e[i], p[1] - e[i], p[2] - n[i], p[3] - n[i], p[4] - u[i], p[5] - u[i]};
+      Rel q{p[0] - e[i], p[1] - e[i], p[2] - n[i], p[3] - n[i], p[4] - u[i], p[5] - u[i],
+            p[1] - p[0], p[3] - p[2], p[5] - p[4]};
       double v;
       if (mode == 2) {
         double all[kNumFields];
