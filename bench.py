@@ -21,13 +21,16 @@ cost is uniform, so pairs/s over batches equals pairs/s over the full survey.
   sqrt + 2 log + 1 atan2) at basic=1, sqrt=4, log=20, atan2=30), over the
   average kernel time; ``peak`` is the FP64 fused multiply-add rate measured
   live by the hg_fp64_peak_probe launch (no FP64 figure exists in the
-  measured peak file).  The kernel executes far fewer FP64
-  instructions per pair than that convention counts (float-pair elementary
-  functions), so ``frac`` exceeds 1; ``fp64_pipe_frac`` is the hardware
-  figure: the kernel's FP64 instructions per pair (ncu count, recorded in
-  profiles/forward_kernel_gz_layer1e6.md) x pairs/s over the measured FP64
-  instruction peak.  ``traffic`` is the DRAM bytes of one step's launch from
-  the same profile (the 24 MB layer read once; it stays in L2).
+  measured peak file).  The kernel evaluates the pair on float pairs
+  and executes ~9 FP64 instructions per pair instead of the convention's
+  720 flop, so ``frac`` far exceeds 1: it rates the algorithm, not the
+  hardware.  ``fp64_pipe_frac`` is the FP64 pipe's hardware use (ncu FP64
+  instructions per pair, recorded in profiles/forward_kernel_gz_layer1e6.md,
+  x pairs/s over the measured FP64 instruction peak); ``hw`` is the binding
+  resource, warp-instruction issue (ncu instructions per pair x pairs/s over
+  4 per clock per SM at the sampled clock).  ``traffic`` is the DRAM bytes of
+  one step's launch from the same profile (the 24 MB layer read once; it
+  stays in L2).
 * ``cpu_baseline``: the CPU oracle (a C/OpenMP restatement of the reference's
   per-vertex loop) on all host cores, on a bounded sample of stations of the
   same workload.
@@ -52,10 +55,13 @@ sys.path.insert(0, HERE)
 
 ALGO_FLOP_PER_PAIR_GZ = 720.0
 # ncu counts for forward_kernel<g_z, LayerSource> (profiles/forward_kernel_gz_layer1e6.md):
-# FP64 thread-instructions per pair (sm__thread_inst_executed_pipe_fp64_pred_on / pairs) and
-# DRAM read+write bytes of one default step's launch (5000 stations x 1e6 prisms).
-FP64_INST_PER_PAIR_GZ = 77.3
+# FP64 thread-instructions per pair (sm__sass_thread_inst_executed_op_fp64_pred_on / pairs),
+# warp instructions issued per pair (smsp__inst_executed / pairs) and DRAM read+write bytes of
+# one default step's launch (5000 stations x 1e6 prisms).
+FP64_INST_PER_PAIR_GZ = 9.14
+WARP_INST_PER_PAIR_GZ = 95.12
 TRAFFIC_BYTES_GZ_STEP = 25159424 + 21248
+ISSUE_PER_SM_PER_CLOCK = 4  # one warp instruction per clock per SM sub-partition, 4 per SM
 METRIC = "FP64 g_z prism-station pairs/s"
 WORKLOAD = "layer_topography_1e6: 1000x1000 prisms (200 m grid), 500x500 stations, g_z"
 
@@ -754,6 +760,12 @@ def main():
     # the probe's peak is in flops (2 per FMA); the FP64 pipe issues 1 instruction per FMA
     fp64_pipe_frac = FP64_INST_PER_PAIR_GZ * kernel_pairs_per_s / (peak * 1e12 / 2.0)
     default_step = args.stations_per_step == 5000
+    # the binding hardware resource: warp-instruction issue, against 4 per clock per SM at
+    # the SM clock sampled during the timed steps
+    n_sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    sm_hz = (clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 0.0) * 1e6
+    issue_peak = ISSUE_PER_SM_PER_CLOCK * n_sms * sm_hz
+    issue_rate = WARP_INST_PER_PAIR_GZ * kernel_pairs_per_s
     line = {
         "metric": METRIC,
         "value": value,
@@ -784,6 +796,15 @@ def main():
             "flop_per_pair": ALGO_FLOP_PER_PAIR_GZ,
             "fp64_inst_per_pair": FP64_INST_PER_PAIR_GZ,
             "fp64_pipe_frac": fp64_pipe_frac,
+            "hw": {
+                "bound": "instruction issue",
+                "achieved": issue_rate / 1e9,
+                "peak": issue_peak / 1e9 if issue_peak else None,
+                "unit": "G warp-instructions/s",
+                "frac": issue_rate / issue_peak if issue_peak else None,
+                "warp_inst_per_pair": WARP_INST_PER_PAIR_GZ,
+                "peak_source": "4 warp instructions per clock per SM x SMs x sampled SM clock",
+            },
             "peak_source": "measured live: hg_fp64_peak_probe (FP64 FMA chains)",
         },
         "cpu_baseline": base,
