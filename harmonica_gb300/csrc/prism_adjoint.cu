@@ -32,9 +32,16 @@ struct PointTile {
 
 constexpr int kAdjOut = 3;  // density, bottom, top
 
+#ifndef HG_ADJ_MIN_BLOCKS
+#define HG_ADJ_MIN_BLOCKS 4
+#endif
+// Resident CTAs per SM: the potential's adjoint needs every log and face angle
+template <int F> struct AdjMinBlocks { static constexpr int value = HG_ADJ_MIN_BLOCKS; };
+template <> struct AdjMinBlocks<kPotential> { static constexpr int value = 3; };
+
 // part layout: [chunk][output][prism]
 template <int F, class Source>
-__global__ void __launch_bounds__(kThreads) adjoint_kernel(
+__global__ void __launch_bounds__(kThreads, AdjMinBlocks<F>::value) adjoint_kernel(
     const double* __restrict__ oe, const double* __restrict__ on, const double* __restrict__ ou,
     const double* __restrict__ weights, int64_t n_obs, Source src, int64_t n_prisms,
     int64_t chunk, double* __restrict__ part) {

@@ -693,92 +693,196 @@ HG_HD __forceinline__ lean::F2 merged_t(bool straddle, lean::F2 lo, lean::F2 hi,
   return f2_div(f2_mul(f2_mul(dQ, M1), X), f2_mul(f2_mul(Sh, Sl), f2_mul(M0, Q1)));
 }
 
-// The FP64 evaluation of g_z, for the pairs the float-pair path declines.
-HG_COLD double pair_gz_fp64(const Rel& q, const Tables& T);
+// Float-pair geometry of one pair: every length scaled by 2^(1023 - top),
+// top the largest biased exponent of the six observation-relative bounds.
+struct GeomF2 {
+  lean::F2 c[3][2];     // bounds c[axis][0 lower, 1 upper]
+  lean::F2 d[3];        // extents
+  lean::F2 r[2][2][2];  // vertex distances r[i][j][k]
+  int top;
+};
 
-HG_HD __forceinline__ double pair_gz_f2(const Rel& q, const Tables& T) {
+HG_HD __forceinline__ double rel_bound(const Rel& q, int axis, int k) {
+  return axis == 0 ? (k ? q.x2 : q.x1) : (axis == 1 ? (k ? q.y2 : q.y1) : (k ? q.z2 : q.z1));
+}
+
+// false: the scaled geometry could leave the float range (a nonzero bound
+// below 2^-40 of the scale, an extent or a vertex distance below 2^-20);
+// the pair then takes the FP64 path.
+HG_HD __forceinline__ bool make_geom_f2(const Rel& q, GeomF2& g) {
   using namespace lean;
   const auto ex = [](double v) { return (int)((hi_word(v) >> 20) & 0x7ffu); };
-  int top = max(max(ex(q.x1), ex(q.x2)), max(max(ex(q.y1), ex(q.y2)), max(ex(q.z1), ex(q.z2))));
+  const int top =
+      max(max(ex(q.x1), ex(q.x2)), max(max(ex(q.y1), ex(q.y2)), max(ex(q.z1), ex(q.z2))));
   const auto tiny_nz = [&](double v) { return !is_tiny(v) && ex(v) < top - 40; };
   if (top >= 0x7fe || tiny_nz(q.x1) || tiny_nz(q.x2) || tiny_nz(q.y1) || tiny_nz(q.y2) ||
       tiny_nz(q.z1) || tiny_nz(q.z2) || ex(q.dx) < top - 20 || ex(q.dy) < top - 20 ||
       ex(q.dz) < top - 20)
-    return pair_gz_fp64(q, T);
+    return false;
   const auto f = [&](double v) { return scaled_f2(d2ll(v), top); };
-  const F2 x[2] = {f(q.x1), f(q.x2)}, y[2] = {f(q.y1), f(q.y2)}, z[2] = {f(q.z1), f(q.z2)};
-  const F2 dx = f(q.dx), dy = f(q.dy), dz = f(q.dz);
-  F2 r[2][2][2];
-  {
-    const F2 x2[2] = {f2_sq(x[0]), f2_sq(x[1])}, y2[2] = {f2_sq(y[0]), f2_sq(y[1])};
-    const F2 z2[2] = {f2_sq(z[0]), f2_sq(z[1])};
-    bool ok = true;
+  g.top = top;
+  g.c[0][0] = f(q.x1);
+  g.c[0][1] = f(q.x2);
+  g.c[1][0] = f(q.y1);
+  g.c[1][1] = f(q.y2);
+  g.c[2][0] = f(q.z1);
+  g.c[2][1] = f(q.z2);
+  g.d[0] = f(q.dx);
+  g.d[1] = f(q.dy);
+  g.d[2] = f(q.dz);
+  F2 sq[3][2];
 #pragma unroll
-    for (int i = 0; i < 2; i++)
-#pragma unroll
-      for (int k = 0; k < 2; k++) {
-        const F2 xz = f2_add(x2[i], z2[k]);
-#pragma unroll
-        for (int j = 0; j < 2; j++) {
-          r[i][j][k] = f2_sqrt(f2_add(xz, y2[j]));
-          ok = ok && r[i][j][k].h >= 0x1p-20f;
-        }
-      }
-    if (!ok) return pair_gz_fp64(q, T);
+  for (int a = 0; a < 3; a++) {
+    sq[a][0] = f2_sq(g.c[a][0]);
+    sq[a][1] = f2_sq(g.c[a][1]);
   }
-  // edge cases of the x and y axes (from the FP64 bounds: exact decisions)
-  const AxisCase cx = axis_case(q.x1, q.x2), cy = axis_case(q.y1, q.y2);
-  const F2 sz = f2_add(z[0], z[1]);
+  bool ok = true;
+#pragma unroll
+  for (int i = 0; i < 2; i++)
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+      const F2 xz = f2_add(sq[0][i], sq[2][k]);
+#pragma unroll
+      for (int j = 0; j < 2; j++) {
+        g.r[i][j][k] = f2_sqrt(f2_add(xz, sq[1][j]));
+        ok = ok && g.r[i][j][k].h >= 0x1p-20f;
+      }
+    }
+  return ok;
+}
+
+// Outside limit of a face angle for a point in the face plane (face_angle):
+// (upper ? -pi/2 : pi/2) * (sgn products), out of line (rare).
+HG_COLD lean::F2 face_limit_f2(double b1, double b2, double c1, double c2, bool upper) {
+  const int s = sgn(b2) * sgn(c2) + sgn(b1) * sgn(c1) - sgn(b1) * sgn(c2) - sgn(b2) * sgn(c1);
+  const float sf = (float)(upper ? -s : s);
+  return lean::F2{lean::fmul(1.57079637f, sf), lean::fmul(-4.37113883e-8f, sf)};
+}
+
+// same_sign: the in-plane b bounds have one sign (pair_complex), from the
+// caller (shared by the two faces).
+template <int U>
+HG_HD __forceinline__ bool face_f2(const Rel& q, const GeomF2& g, bool k, bool same_sign,
+                                   const Tables& T, lean::F2& o) {
+  using namespace lean;
+  constexpr int B = U == 0 ? 1 : 0, C = U == 2 ? 1 : 2;
+  // r at in-plane corner (bi, ci) of the face at bound k (2-way select)
+  const auto idx = [&](int bi, int ci) {
+    int i0[3], i1[3];
+    i0[U] = 0;
+    i1[U] = 1;
+    i0[B] = i1[B] = bi;
+    i0[C] = i1[C] = ci;
+    return k ? g.r[i1[0]][i1[1]][i1[2]] : g.r[i0[0]][i0[1]][i0[2]];
+  };
+  if (is_tiny(rel_bound(q, U, k))) {
+    o = face_limit_f2(rel_bound(q, B, 0), rel_bound(q, B, 1), rel_bound(q, C, 0),
+                      rel_bound(q, C, 1), k);
+    return true;
+  }
+  const F2 r11 = idx(0, 0), r12 = idx(0, 1), r21 = idx(1, 0), r22 = idx(1, 1);
+  const auto fe = [](F2 a) { return (int)((f2u(a.h) >> 23) & 0xffu); };
+  const int ftop = max(max(fe(r11), fe(r12)), max(fe(r21), fe(r22)));
+  const auto fsmall = [&](F2 a) { return a.h != 0.0f && fe(a) < ftop - 16; };
+  const F2 a = k ? g.c[U][1] : g.c[U][0];
+  if (fsmall(a) || fsmall(g.c[B][0]) || fsmall(g.c[B][1]) || fsmall(g.c[C][0]) ||
+      fsmall(g.c[C][1]) || fe(g.d[B]) < ftop - 16)
+    return false;
+  const float sc = pow2f(127 - ftop);
+  const auto h = [&](F2 v) { return F2{fmul(v.h, sc), fmul(v.l, sc)}; };
+  const bool neg = a.h < 0.0f;
+  o = face_core_f2(h(neg ? f2_neg(a) : a), h(g.c[B][0]), h(g.c[B][1]), h(g.c[C][0]),
+                   h(g.c[C][1]), h(r11), h(r12), h(r21), h(r22), h(g.d[B]), same_sign, T);
+  if (neg) o = f2_neg(o);
+  return true;
+}
+
+// First derivative along axis U (U = 2: g_z, 0: g_e, 1: g_n combinations) on
+// float pairs:
+//   sum over the two edge families (A, V) of sum_a s_a v_a ln(R(u_1)/R(u_0))
+//   - sum_k s_k u_k O_k
+// where the family's edges are parallel to A at V-bound v_a and the merged
+// log pairs them along U (merged_t); s_0 = -1, s_1 = +1.  Families:
+// U = z: (A = y, V = x), (A = x, V = y); U = x: (A = z, V = y), (A = y, V = z);
+// U = y: (A = x, V = z), (A = z, V = x).  With o_faces, the two face angles
+// O_0, O_1 are returned as well (adjoint).  false: FP64 path.
+template <int U>
+HG_HD __forceinline__ bool pair_grad_f2(const Rel& q, const Tables& T, double& out,
+                                        double* o_faces) {
+  using namespace lean;
+  GeomF2 g;
+  if (!make_geom_f2(q, g)) return false;
+  constexpr int A0 = U == 2 ? 1 : (U == 0 ? 2 : 0), V0 = 3 - U - A0;  // first family
+  const AxisCase case0 = axis_case(rel_bound(q, A0, 0), rel_bound(q, A0, 1));
+  const AxisCase case1 = axis_case(rel_bound(q, V0, 0), rel_bound(q, V0, 1));  // second: A = V0
+  const F2 su = f2_add(g.c[U][0], g.c[U][1]);
   F2 v{0.0f, 0.0f};
 #pragma unroll 1
   for (int m = 0; m < 4; m++) {
-    // m = 0, 1: y-edges at x_m (coefficient x_m); m = 2, 3: x-edges at y_(m-2)
-    const bool b = m & 1, yx = m >= 2;
-    const AxisCase c = yx ? cx : cy;
-    const F2 a1 = yx ? x[0] : y[0], a2 = yx ? x[1] : y[1];
+    const bool b = m & 1, second = m >= 2;
+    const AxisCase c = second ? case1 : case0;
+    const F2 a1 = second ? g.c[V0][0] : g.c[A0][0], a2 = second ? g.c[V0][1] : g.c[A0][1];
     const F2 lo = c.reflect ? f2_neg(a2) : a1, hi = c.reflect ? f2_neg(a1) : a2;
-    const int il = c.reflect ? 1 : 0;  // index of the lo end along the edge axis
-    // vertex distances r(lo/hi end, z_k) of this edge pair
-    const auto rv = [&](int end, int k) {
-      const F2 ry = b ? r[1][end][k] : r[0][end][k];  // y-edge at x_b: r[b][end][k]
-      const F2 rx = b ? r[end][1][k] : r[end][0][k];  // x-edge at y_b: r[end][b][k]
-      return yx ? rx : ry;
+    // r of the vertex at A-end `end` (compile time), V-bound b, U-bound eu:
+    // family 0 indexes (A0 = end, V0 = b), family 1 (V0 = end, A0 = b)
+    const auto rv = [&](int end, int eu) {
+      const auto at = [&](int ia, int iv) {
+        int id[3] = {0, 0, 0};
+        id[A0] = ia;
+        id[V0] = iv;
+        id[U] = eu;
+        return g.r[id[0]][id[1]][id[2]];
+      };
+      const F2 f0 = b ? at(end, 1) : at(end, 0);
+      const F2 f1 = b ? at(1, end) : at(0, end);
+      return second ? f1 : f0;
     };
+    const bool il = c.reflect;  // A-end of lo
     const F2 rl0 = il ? rv(1, 0) : rv(0, 0), rl1 = il ? rv(1, 1) : rv(0, 1);
     const F2 rh0 = il ? rv(0, 0) : rv(1, 0), rh1 = il ? rv(0, 1) : rv(1, 1);
-    const F2 off = yx ? (b ? y[1] : y[0]) : (b ? x[1] : x[0]);  // coefficient and in-plane offset
-    const F2 t = merged_t(c.straddle, lo, hi, off, z[1], rl0, rl1, rh0, rh1, yx ? dx : dy, dz, sz);
+    const F2 off = second ? (b ? g.c[A0][1] : g.c[A0][0]) : (b ? g.c[V0][1] : g.c[V0][0]);
+    const F2 t = merged_t(c.straddle, lo, hi, off, g.c[U][1], rl0, rl1, rh0, rh1,
+                          second ? g.d[V0] : g.d[A0], g.d[U], su);
     const F2 L = log1p_f2(t, T);
-    // s_b * off * L, s_0 = -1
     if (off.h != 0.0f) v = f2_add(v, f2_mul(b ? off : f2_neg(off), L));
   }
-  // faces normal to z: - s_k z_k O_k
-  const bool same_sign = !(neg_not_tiny(q.x1) && !nonpos_or_tiny(q.x2));
+  constexpr int B = U == 0 ? 1 : 0;
+  const bool same_sign = !(neg_not_tiny(rel_bound(q, B, 0)) && !nonpos_or_tiny(rel_bound(q, B, 1)));
 #pragma unroll 1
   for (int k = 0; k < 2; k++) {
-    const double zd = k ? q.z2 : q.z1;
-    const F2 zk = k ? z[1] : z[0];
-    if (is_tiny(zd)) continue;  // the point in the face plane: zero coefficient, finite O
-    const F2 r11 = k ? r[0][0][1] : r[0][0][0], r12 = k ? r[0][1][1] : r[0][1][0];
-    const F2 r21 = k ? r[1][0][1] : r[1][0][0], r22 = k ? r[1][1][1] : r[1][1][0];
-    // rescale the face so that its largest vertex distance is in [1, 2)
-    const auto fe = [](F2 a) { return (int)((f2u(a.h) >> 23) & 0xffu); };
-    const int ftop = max(max(fe(r11), fe(r12)), max(fe(r21), fe(r22)));
-    const float sc = pow2f(127 - ftop);
-    const auto g = [&](F2 a) { return F2{fmul(a.h, sc), fmul(a.l, sc)}; };
-    const auto fsmall = [&](F2 a) { return a.h != 0.0f && fe(a) < ftop - 16; };
-    const F2 za = zk;
-    if (fsmall(za) || fsmall(x[0]) || fsmall(x[1]) || fsmall(y[0]) || fsmall(y[1]) ||
-        fe(dx) < ftop - 16)
-      return pair_gz_fp64(q, T);
-    F2 o = face_core_f2(g(za.h < 0.0f ? f2_neg(za) : za), g(x[0]), g(x[1]), g(y[0]), g(y[1]),
-                        g(r11), g(r12), g(r21), g(r22), g(dx), same_sign, T);
-    if (za.h < 0.0f) o = f2_neg(o);
-    // - s_k z_k O_k: +z_0 O_0, -z_1 O_1
-    v = f2_add(v, f2_mul(k ? f2_neg(zk) : zk, o));
+    F2 o;
+    if (!face_f2<U>(q, g, k, same_sign, T, o)) return false;
+    if (o_faces) o_faces[k] = f2_to_double(o, 0);
+    const F2 uk = k ? g.c[U][1] : g.c[U][0];
+    if (uk.h != 0.0f) v = f2_add(v, f2_mul(k ? f2_neg(uk) : uk, o));  // -s_k u_k O_k
   }
-  return f2_to_double(v, top - 1023);
+  out = f2_to_double(v, g.top - 1023);
+  return true;
 }
+
+// Diagonal tensor combination O_0 - O_1 of the faces normal to U on float
+// pairs.  false: FP64 path.
+template <int U>
+HG_HD __forceinline__ bool pair_diag_f2(const Rel& q, const Tables& T, double& out) {
+  using namespace lean;
+  GeomF2 g;
+  if (!make_geom_f2(q, g)) return false;
+  constexpr int B = U == 0 ? 1 : 0;
+  const bool same_sign = !(neg_not_tiny(rel_bound(q, B, 0)) && !nonpos_or_tiny(rel_bound(q, B, 1)));
+  F2 v{0.0f, 0.0f};
+#pragma unroll 1
+  for (int k = 0; k < 2; k++) {
+    F2 o;
+    if (!face_f2<U>(q, g, k, same_sign, T, o)) return false;
+    v = f2_add(v, k ? f2_neg(o) : o);
+  }
+  out = f2_to_double(v, 0);
+  return true;
+}
+
+// FP64 evaluations for the pairs the float-pair paths decline (out of line).
+template <int F>
+HG_COLD double pair_field_fp64(const Rel& q, const Tables& T);
 
 // ---------------------------------------------------------------------------
 // All ten fields of one pair: the signed edge/face combinations (without G,
@@ -840,7 +944,7 @@ HG_HD __forceinline__ void pair_all(const Rel& q, const Tables& T, double out[kN
 
 // One field of one pair, with the edge logs merged where coefficients allow.
 template <int F, bool LEAN>
-HG_HD __forceinline__ double pair_field(const Rel& q, const Tables& T) {
+HG_HD __forceinline__ double pair_field_geom(const Rel& q, const Tables& T) {
   if (F == kPotential) {
     double out[kNumFields];
     pair_all<LEAN>(q, T, out);
@@ -849,7 +953,6 @@ HG_HD __forceinline__ double pair_field(const Rel& q, const Tables& T) {
   Geom g;
   make_geom<LEAN>(q, g);
   if (F == kGz) {
-    if (LEAN) return pair_gz_f2(q, T);
     // sum_i s_i x_i sum_k s_k Ly[i][k] + sum_j s_j y_j sum_k s_k Lx[j][k]
     //   - sum_k s_k z_k Oz[k]
     EdgeSet Ey, Ex;
@@ -889,16 +992,28 @@ HG_HD __forceinline__ double pair_field(const Rel& q, const Tables& T) {
   }
 }
 
-// g_z in FP64 (edge sums, exact near-1 log numerators, FP64-input faces).
-HG_COLD double pair_gz_fp64(const Rel& q, const Tables& T) {
-  Geom g;
-  make_geom<true>(q, g);
-  EdgeSet Ey, Ex;
-  edges_y(g, Ey);
-  edges_x(g, Ex);
-  const double v =
-      merged_logs4<true, false, false>(Ey, Ex, g.x[0], g.x[1], g.y[0], g.y[1], T, 0.0);
-  return faces2_dot<2, true>(g, g.z[0], g.z[1], T, v);
+template <int F>
+HG_COLD double pair_field_fp64(const Rel& q, const Tables& T) {
+  return pair_field_geom<F, true>(q, T);
+}
+
+// One field of one pair.  With the lean math, the acceleration components and
+// the diagonal tensor components run on float pairs (pair_grad_f2,
+// pair_diag_f2); the rest, and the pairs those decline, on the FP64
+// geometry (pair_field_geom).
+template <int F, bool LEAN>
+HG_HD __forceinline__ double pair_field(const Rel& q, const Tables& T) {
+  if (LEAN && (F == kGe || F == kGn || F == kGz)) {
+    double v;
+    if (pair_grad_f2<(F == kGe ? 0 : (F == kGn ? 1 : 2))>(q, T, v, nullptr)) return v;
+    return pair_field_fp64<F>(q, T);
+  }
+  if (LEAN && (F == kGee || F == kGnn || F == kGzz)) {
+    double v;
+    if (pair_diag_f2<(F == kGee ? 0 : (F == kGnn ? 1 : 2))>(q, T, v)) return v;
+    return pair_field_fp64<F>(q, T);
+  }
+  return pair_field_geom<F, LEAN>(q, T);
 }
 
 // The six gradient-tensor combinations of one pair (the second derivatives
@@ -929,9 +1044,18 @@ HG_HD __forceinline__ void pair_tensor6(const Rel& q, const Tables& T, double t[
 // g_z combination of one pair together with its two horizontal face angles
 // (the derivatives of the combination with respect to the bottom and top
 // coordinates: d/dz_bottom = O_bottom, d/dz_top = -O_top), for the adjoint.
+HG_COLD double pair_gz_faces_fp64(const Rel& q, const Tables& T, double* o);
+
 template <bool LEAN>
 HG_HD __forceinline__ double pair_gz_faces(const Rel& q, const Tables& T, double& o_bottom,
                                            double& o_top) {
+  if (LEAN) {
+    double v, o[2];
+    if (!pair_grad_f2<2>(q, T, v, o)) v = pair_gz_faces_fp64(q, T, o);
+    o_bottom = o[0];
+    o_top = o[1];
+    return v;
+  }
   Geom g;
   make_geom<LEAN>(q, g);
   EdgeSet Ey, Ex;
@@ -941,6 +1065,10 @@ HG_HD __forceinline__ double pair_gz_faces(const Rel& q, const Tables& T, double
   double v = merged_logs4<LEAN, false, false>(Ey, Ex, g.x[0], g.x[1], g.y[0], g.y[1], T, 0.0);
   v = cfma_s<true>(g.z[1], o_top, v);
   return cfma_s<false>(g.z[0], o_bottom, v);
+}
+
+HG_COLD double pair_gz_faces_fp64(const Rel& q, const Tables& T, double* o) {
+  return pair_gz_faces<false>(q, T, o[0], o[1]);
 }
 
 }  // namespace hg
