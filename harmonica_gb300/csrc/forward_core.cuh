@@ -24,7 +24,7 @@ HG_HD __forceinline__ bool is_tensor(int f) { return f >= kGee && f <= kGnz; }
 // code hides its latency with more warps; the fused all-field kernel needs
 // more registers).
 #ifndef HG_FWD_MIN_BLOCKS
-#define HG_FWD_MIN_BLOCKS 6
+#define HG_FWD_MIN_BLOCKS 5
 #endif
 #ifndef HG_FWD_MIN_BLOCKS_ALL
 #define HG_FWD_MIN_BLOCKS_ALL 4

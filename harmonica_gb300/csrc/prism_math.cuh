@@ -43,6 +43,7 @@
 #define HG_HD __host__ __device__
 
 #include "lean_math.cuh"
+#include "lean_packed.cuh"
 
 namespace hg {
 
@@ -730,24 +731,23 @@ HG_HD __forceinline__ bool make_geom_f2(const Rel& q, GeomF2& g) {
   g.d[0] = f(q.dx);
   g.d[1] = f(q.dy);
   g.d[2] = f(q.dz);
-  F2 sq[3][2];
+  // squares and vertex distances two at a time (lanes: lower/upper bound)
+  P2 sq[3];
 #pragma unroll
-  for (int a = 0; a < 3; a++) {
-    sq[a][0] = f2_sq(g.c[a][0]);
-    sq[a][1] = f2_sq(g.c[a][1]);
-  }
+  for (int a = 0; a < 3; a++) sq[a] = p2_sq(pk(g.c[a][0], g.c[a][1]));
+  const F2 xs[2] = {lane0(sq[0]), lane1(sq[0])}, ys[2] = {lane0(sq[1]), lane1(sq[1])};
   bool ok = true;
 #pragma unroll
-  for (int i = 0; i < 2; i++)
+  for (int i = 0; i < 2; i++) {
+    const P2 xz = p2_add(pk(xs[i], xs[i]), sq[2]);  // x_i^2 + z_k^2, lanes k
 #pragma unroll
-    for (int k = 0; k < 2; k++) {
-      const F2 xz = f2_add(sq[0][i], sq[2][k]);
-#pragma unroll
-      for (int j = 0; j < 2; j++) {
-        g.r[i][j][k] = f2_sqrt(f2_add(xz, sq[1][j]));
-        ok = ok && g.r[i][j][k].h >= 0x1p-20f;
-      }
+    for (int j = 0; j < 2; j++) {
+      const P2 r = p2_sqrt(p2_add(xz, pk(ys[j], ys[j])));
+      g.r[i][j][0] = lane0(r);
+      g.r[i][j][1] = lane1(r);
+      ok = ok && r.h.x >= 0x1p-20f && r.h.y >= 0x1p-20f;
     }
+  }
   return ok;
 }
 
@@ -880,6 +880,220 @@ HG_HD __forceinline__ bool pair_diag_f2(const Rel& q, const Tables& T, double& o
   return true;
 }
 
+// ---------------------------------------------------------------------------
+// Packed evaluation (lean_packed.cuh): the two faces normal to an axis, and
+// the two merged logs of an edge family, each evaluated together in the two
+// lanes of float2 registers.  Same formulas as the scalar float-pair path.
+
+HG_HD __forceinline__ void pair_complex_p2(lean::P2 aa, lean::P2 asq, lean::P2 b1, lean::P2 b2,
+                                           lean::P2 c, lean::P2 csq, lean::P2 r1, lean::P2 r2,
+                                           bool same_sign, lean::P2 bdq, lean::P2& re,
+                                           lean::P2& im) {
+  using namespace lean;
+  re = p2_add(p2_mul(asq, p2_mul(r1, r2)), p2_mul(p2_mul(b1, b2), csq));
+  P2 x = p2_add(p2_mul(b2, r1), p2_mul(same_sign ? b1 : p2_neg(b1), r2));
+  P2 d = x;
+  if (same_sign) {
+    const float2 sg = mk2(x.h.x < 0.0f ? -1.0f : 1.0f, x.h.y < 0.0f ? -1.0f : 1.0f);
+    x = p2_scale(x, sg);
+    d = p2_scale(bdq, sg);
+    re = p2_mul(re, x);
+  }
+  im = p2_mul(p2_mul(aa, c), d);
+}
+
+// Scales each lane's complex number (re, im) by a power of two so that its
+// larger component is in [1, 2).
+HG_HD __forceinline__ void normalize_p2c(lean::P2& re, lean::P2& im) {
+  using namespace lean;
+  const auto sc = [](float r, float i) {
+    const int er = (int)((f2u(r) >> 23) & 0xffu), ei = (int)((f2u(i) >> 23) & 0xffu);
+    const int e = er > ei ? er : ei;
+    return u2f((unsigned)(254 - (e > 253 ? 253 : e)) << 23);  // 2^(127 - e)
+  };
+  const float2 s = mk2(sc(re.h.x, im.h.x), sc(re.h.y, im.h.y));
+  re = p2_scale(re, s);
+  im = p2_scale(im, s);
+}
+
+// face_core_f2 for two faces at once (lanes); inputs as there.
+HG_HD __forceinline__ lean::P2 face_core_p2(lean::P2 fa, lean::P2 fb1, lean::P2 fb2,
+                                            lean::P2 fc1, lean::P2 fc2, lean::P2 fr11,
+                                            lean::P2 fr12, lean::P2 fr21, lean::P2 fr22,
+                                            lean::P2 fw, bool same_sign, const Tables& T) {
+  using namespace lean;
+  P2 asq = two_prod2(fa.h, fa.h);
+  asq.l = fma2(add2(fa.h, fa.h), fa.l, asq.l);
+  P2 c1sq = two_prod2(fc1.h, fc1.h), c2sq = two_prod2(fc2.h, fc2.h);
+  c1sq.l = fma2(add2(fc1.h, fc1.h), fc1.l, c1sq.l);
+  c2sq.l = fma2(add2(fc2.h, fc2.h), fc2.l, c2sq.l);
+  P2 bdq1{sp2(0.0f), sp2(0.0f)}, bdq2{sp2(0.0f), sp2(0.0f)};
+  if (same_sign) {
+    const P2 fbd = p2_mul(fw, p2_add(fb2, fb1));
+    bdq1 = p2_mul(fbd, p2_add(asq, c1sq));
+    bdq2 = p2_mul(fbd, p2_add(asq, c2sq));
+  }
+  P2 ar, ai, br, bi;
+  pair_complex_p2(fa, asq, fb1, fb2, fc2, c2sq, fr12, fr22, same_sign, bdq2, ar, ai);
+  pair_complex_p2(fa, asq, fb1, fb2, fc1, c1sq, fr11, fr21, same_sign, bdq1, br, bi);
+  normalize_p2c(ar, ai);
+  normalize_p2c(br, bi);
+  const float est0 = atan2_est(ai.h.x, ar.h.x) - atan2_est(bi.h.x, br.h.x);
+  const float est1 = atan2_est(ai.h.y, ar.h.y) - atan2_est(bi.h.y, br.h.y);
+  const P2 pr = p2_add(p2_mul(ar, br), p2_mul(ai, bi));
+  const P2 pim = p2_add(p2_mul(ai, br), p2_neg(p2_mul(ar, bi)));
+  return arg_near_p2(pr, pim, est0, est1, T);
+}
+
+// The two faces normal to U (lanes: lower, upper bound), as face_f2.
+template <int U>
+HG_HD __forceinline__ bool faces_p2(const Rel& q, const GeomF2& g, bool same_sign,
+                                    const Tables& T, lean::P2& o) {
+  using namespace lean;
+  constexpr int B = U == 0 ? 1 : 0, C = U == 2 ? 1 : 2;
+  const auto rr = [&](int k, int bi, int ci) {
+    int id[3];
+    id[U] = k;
+    id[B] = bi;
+    id[C] = ci;
+    return g.r[id[0]][id[1]][id[2]];
+  };
+  const auto fe = [](F2 a) { return (int)((f2u(a.h) >> 23) & 0xffu); };
+  int ftop[2];
+  bool small = false;
+#pragma unroll
+  for (int k = 0; k < 2; k++) {
+    ftop[k] = max(max(fe(rr(k, 0, 0)), fe(rr(k, 0, 1))), max(fe(rr(k, 1, 0)), fe(rr(k, 1, 1))));
+    const auto fsmall = [&](F2 a) { return a.h != 0.0f && fe(a) < ftop[k] - 16; };
+    small = small || fsmall(g.c[U][k]) || fsmall(g.c[B][0]) || fsmall(g.c[B][1]) ||
+            fsmall(g.c[C][0]) || fsmall(g.c[C][1]) || fe(g.d[B]) < ftop[k] - 16;
+  }
+  if (small) return false;
+  const float2 sc = mk2(pow2f(127 - ftop[0]), pow2f(127 - ftop[1]));
+  const auto both = [&](F2 a) { return p2_scale(pk(a, a), sc); };
+  const auto per = [&](F2 a0, F2 a1) { return p2_scale(pk(a0, a1), sc); };
+  const F2 a0 = g.c[U][0], a1 = g.c[U][1];
+  const bool n0 = a0.h < 0.0f, n1 = a1.h < 0.0f;
+  o = face_core_p2(per(n0 ? f2_neg(a0) : a0, n1 ? f2_neg(a1) : a1), both(g.c[B][0]),
+                   both(g.c[B][1]), both(g.c[C][0]), both(g.c[C][1]),
+                   per(rr(0, 0, 0), rr(1, 0, 0)), per(rr(0, 0, 1), rr(1, 0, 1)),
+                   per(rr(0, 1, 0), rr(1, 1, 0)), per(rr(0, 1, 1), rr(1, 1, 1)), both(g.d[B]),
+                   same_sign, T);
+  F2 o0 = lane0(o), o1 = lane1(o);
+  if (n0) o0 = f2_neg(o0);
+  if (n1) o1 = f2_neg(o1);
+  // a point in a face plane: that face's outside limit
+  if (is_tiny(rel_bound(q, U, 0)) || is_tiny(rel_bound(q, U, 1))) {
+    const double b1 = rel_bound(q, B, 0), b2 = rel_bound(q, B, 1);
+    const double c1 = rel_bound(q, C, 0), c2 = rel_bound(q, C, 1);
+    if (is_tiny(rel_bound(q, U, 0))) o0 = face_limit_f2(b1, b2, c1, c2, false);
+    if (is_tiny(rel_bound(q, U, 1))) o1 = face_limit_f2(b1, b2, c1, c2, true);
+  }
+  o = pk(o0, o1);
+  return true;
+}
+
+// merged_t for the two merged logs of one edge family (lanes: V-bounds 0, 1);
+// the edge case is common to both lanes.
+HG_HD __forceinline__ lean::P2 merged_t_p2(bool straddle, lean::P2 lo, lean::P2 hi, lean::P2 v,
+                                           lean::P2 u1, lean::P2 rl0, lean::P2 rl1,
+                                           lean::P2 rh0, lean::P2 rh1, lean::P2 dA,
+                                           lean::P2 du, lean::P2 su) {
+  using namespace lean;
+  const P2 dQ = p2_mul(du, su);
+  const P2 Sl = p2_add(rl0, rl1), Sh = p2_add(rh0, rh1);
+  const P2 Dl = p2_div(dQ, Sl), Dh = p2_div(dQ, Sh);
+  if (!straddle) {
+    const P2 D0 = p2_add(lo, rl0), D1 = p2_add(lo, rl1), N0 = p2_add(hi, rh0);
+    const P2 P0 = p2_add(rl0, rh0), P1 = p2_add(rl1, rh1);
+    const P2 inner = p2_add(p2_mul(D0, p2_add(Dl, Dh)), p2_mul(Dl, P1));
+    const P2 br = p2_add(Dl, p2_div(p2_mul(p2_add(hi, lo), inner), p2_mul(P0, P1)));
+    return p2_neg(p2_div(p2_mul(dA, br), p2_mul(D1, N0)));
+  }
+  const P2 M0 = p2_sub(rl0, lo), M1 = p2_sub(rl1, lo);
+  const P2 Q1 = p2_add(p2_sq(v), p2_sq(u1));
+  const P2 X = p2_add(p2_add(p2_mul(rh0, Dl), p2_neg(p2_mul(rl0, Dh))),
+                      p2_add(p2_neg(p2_mul(hi, Sl)), p2_mul(lo, Sh)));
+  return p2_div(p2_mul(p2_mul(dQ, M1), X), p2_mul(p2_mul(Sh, Sl), p2_mul(M0, Q1)));
+}
+
+// pair_grad_f2 with the merged logs and the faces evaluated two at a time.
+template <int U>
+HG_HD __forceinline__ bool pair_grad_p2(const Rel& q, const Tables& T, double& out,
+                                        double* o_faces) {
+  using namespace lean;
+  GeomF2 g;
+  if (!make_geom_f2(q, g)) return false;
+  constexpr int A0 = U == 2 ? 1 : (U == 0 ? 2 : 0), V0 = 3 - U - A0;
+  const AxisCase case0 = axis_case(rel_bound(q, A0, 0), rel_bound(q, A0, 1));
+  const AxisCase case1 = axis_case(rel_bound(q, V0, 0), rel_bound(q, V0, 1));
+  const F2 su = f2_add(g.c[U][0], g.c[U][1]);
+  const auto bc = [](F2 a) { return pk(a, a); };
+  P2 v2{sp2(0.0f), sp2(0.0f)};
+#pragma unroll 1
+  for (int fam = 0; fam < 2; fam++) {
+    const bool second = fam;
+    const AxisCase c = second ? case1 : case0;
+    const F2 a1 = second ? g.c[V0][0] : g.c[A0][0], a2 = second ? g.c[V0][1] : g.c[A0][1];
+    const F2 lo = c.reflect ? f2_neg(a2) : a1, hi = c.reflect ? f2_neg(a1) : a2;
+    // r at A-end `end`, V-bound vb, U-bound eu (family 0: A0 = end, V0 = vb;
+    // family 1: V0 = end, A0 = vb)
+    const auto rv = [&](int end, int vb, int eu) {
+      const auto at = [&](int ia, int iv) {
+        int id[3] = {0, 0, 0};
+        id[A0] = ia;
+        id[V0] = iv;
+        id[U] = eu;
+        return g.r[id[0]][id[1]][id[2]];
+      };
+      return second ? at(vb, end) : at(end, vb);
+    };
+    const int il = c.reflect ? 1 : 0;
+    const auto lanes = [&](int end, int eu) {
+      return pk(il ? rv(1 - end, 0, eu) : rv(end, 0, eu), il ? rv(1 - end, 1, eu) : rv(end, 1, eu));
+    };
+    const P2 rl0 = lanes(0, 0), rl1 = lanes(0, 1), rh0 = lanes(1, 0), rh1 = lanes(1, 1);
+    const F2 o0 = second ? g.c[A0][0] : g.c[V0][0], o1 = second ? g.c[A0][1] : g.c[V0][1];
+    const P2 t = merged_t_p2(c.straddle, bc(lo), bc(hi), pk(o0, o1), bc(g.c[U][1]), rl0, rl1,
+                             rh0, rh1, bc(second ? g.d[V0] : g.d[A0]), bc(g.d[U]), bc(su));
+    P2 L = log1p_p2(t, T);
+    // s_b off_b L_b (s_0 = -1); a zero coefficient gives 0 whatever L is
+    if (o0.h == 0.0f) L.h.x = L.l.x = 0.0f;
+    if (o1.h == 0.0f) L.h.y = L.l.y = 0.0f;
+    v2 = p2_add(v2, p2_mul(pk(f2_neg(o0), o1), L));
+  }
+  constexpr int B = U == 0 ? 1 : 0;
+  const bool same_sign =
+      !(neg_not_tiny(rel_bound(q, B, 0)) && !nonpos_or_tiny(rel_bound(q, B, 1)));
+  P2 o;
+  if (!faces_p2<U>(q, g, same_sign, T, o)) return false;
+  if (o_faces) {
+    o_faces[0] = f2_to_double(lane0(o), 0);
+    o_faces[1] = f2_to_double(lane1(o), 0);
+  }
+  // -s_k u_k O_k: +u_0 O_0, -u_1 O_1 (u_k = 0: the term vanishes)
+  if (g.c[U][0].h == 0.0f) o.h.x = o.l.x = 0.0f;
+  if (g.c[U][1].h == 0.0f) o.h.y = o.l.y = 0.0f;
+  v2 = p2_add(v2, p2_mul(pk(g.c[U][0], f2_neg(g.c[U][1])), o));
+  out = f2_to_double(f2_add(lane0(v2), lane1(v2)), g.top - 1023);
+  return true;
+}
+
+// pair_diag_f2 with the two faces evaluated together.
+template <int U>
+HG_HD __forceinline__ bool pair_diag_p2(const Rel& q, const Tables& T, double& out) {
+  using namespace lean;
+  GeomF2 g;
+  if (!make_geom_f2(q, g)) return false;
+  constexpr int B = U == 0 ? 1 : 0;
+  const bool same_sign =
+      !(neg_not_tiny(rel_bound(q, B, 0)) && !nonpos_or_tiny(rel_bound(q, B, 1)));
+  P2 o;
+  if (!faces_p2<U>(q, g, same_sign, T, o)) return false;
+  out = f2_to_double(f2_sub(lane0(o), lane1(o)), 0);
+  return true;
+}
+
 // FP64 evaluations for the pairs the float-pair paths decline (out of line).
 template <int F>
 HG_COLD double pair_field_fp64(const Rel& q, const Tables& T);
@@ -1005,12 +1219,12 @@ template <int F, bool LEAN>
 HG_HD __forceinline__ double pair_field(const Rel& q, const Tables& T) {
   if (LEAN && (F == kGe || F == kGn || F == kGz)) {
     double v;
-    if (pair_grad_f2<(F == kGe ? 0 : (F == kGn ? 1 : 2))>(q, T, v, nullptr)) return v;
+    if (pair_grad_p2<(F == kGe ? 0 : (F == kGn ? 1 : 2))>(q, T, v, nullptr)) return v;
     return pair_field_fp64<F>(q, T);
   }
   if (LEAN && (F == kGee || F == kGnn || F == kGzz)) {
     double v;
-    if (pair_diag_f2<(F == kGee ? 0 : (F == kGnn ? 1 : 2))>(q, T, v)) return v;
+    if (pair_diag_p2<(F == kGee ? 0 : (F == kGnn ? 1 : 2))>(q, T, v)) return v;
     return pair_field_fp64<F>(q, T);
   }
   return pair_field_geom<F, LEAN>(q, T);
@@ -1051,7 +1265,7 @@ HG_HD __forceinline__ double pair_gz_faces(const Rel& q, const Tables& T, double
                                            double& o_top) {
   if (LEAN) {
     double v, o[2];
-    if (!pair_grad_f2<2>(q, T, v, o)) v = pair_gz_faces_fp64(q, T, o);
+    if (!pair_grad_p2<2>(q, T, v, o)) v = pair_gz_faces_fp64(q, T, o);
     o_bottom = o[0];
     o_top = o[1];
     return v;
