@@ -59,7 +59,7 @@ ALGO_FLOP_PER_PAIR_GZ = 720.0
 # warp instructions issued per pair (smsp__inst_executed / pairs) and DRAM read+write bytes of
 # one default step's launch (5000 stations x 1e6 prisms).
 FP64_INST_PER_PAIR_GZ = 9.14
-WARP_INST_PER_PAIR_GZ = 95.81
+WARP_INST_PER_PAIR_GZ = 64.15
 TRAFFIC_BYTES_GZ_STEP = 24918272 + 1273344
 ISSUE_PER_SM_PER_CLOCK = 4  # one warp instruction per clock per SM sub-partition, 4 per SM
 METRIC = "FP64 g_z prism-station pairs/s"
