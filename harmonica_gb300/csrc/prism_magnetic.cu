@@ -32,7 +32,10 @@ struct MagTile {
 
 // COMP: 0 b_e, 1 b_n, 2 b_u, 3 all three (rows e, n, u)
 template <int COMP>
-__global__ void __launch_bounds__(kThreads) magnetic_kernel(
+#ifndef HG_MAG_MIN_BLOCKS
+#define HG_MAG_MIN_BLOCKS 4
+#endif
+__global__ void __launch_bounds__(kThreads, HG_MAG_MIN_BLOCKS) magnetic_kernel(
     const double* __restrict__ oe, const double* __restrict__ on, const double* __restrict__ ou,
     int64_t n_obs, const double* __restrict__ soa, int64_t stride, int64_t n_prisms,
     int64_t chunk, double* __restrict__ dst, int64_t dst_chunk_stride, int scale_output) {

@@ -945,51 +945,106 @@ HG_HD __forceinline__ lean::P2 face_core_p2(lean::P2 fa, lean::P2 fb1, lean::P2 
   return arg_near_p2(pr, pim, est0, est1, T);
 }
 
-// The two faces normal to U (lanes: lower, upper bound), as face_f2.
-template <int U>
-HG_HD __forceinline__ bool faces_p2(const Rel& q, const GeomF2& g, bool same_sign,
-                                    const Tables& T, lean::P2& o) {
+// The two faces normal to one axis (lanes: lower, upper bound), as face_f2,
+// from their inputs: bounds along the normal (fa, ad), along the in-plane
+// axes b and c (fb, bd, fc, cd), vertex distances fr[k][bi][ci] and the b
+// width.  false: a coordinate is too small for the face's scale (FP64 path).
+HG_HD __forceinline__ bool face_pair_p2(const lean::F2 fa[2], const lean::F2 fb[2],
+                                        const lean::F2 fc[2], const lean::F2 fr[2][2][2],
+                                        lean::F2 fw, const double ad[2], const double bd[2],
+                                        const double cd[2], const Tables& T, lean::P2& o) {
   using namespace lean;
-  constexpr int B = U == 0 ? 1 : 0, C = U == 2 ? 1 : 2;
-  const auto rr = [&](int k, int bi, int ci) {
-    int id[3];
-    id[U] = k;
-    id[B] = bi;
-    id[C] = ci;
-    return g.r[id[0]][id[1]][id[2]];
-  };
   const auto fe = [](F2 a) { return (int)((f2u(a.h) >> 23) & 0xffu); };
   int ftop[2];
   bool small = false;
 #pragma unroll
   for (int k = 0; k < 2; k++) {
-    ftop[k] = max(max(fe(rr(k, 0, 0)), fe(rr(k, 0, 1))), max(fe(rr(k, 1, 0)), fe(rr(k, 1, 1))));
+    ftop[k] = max(max(fe(fr[k][0][0]), fe(fr[k][0][1])), max(fe(fr[k][1][0]), fe(fr[k][1][1])));
     const auto fsmall = [&](F2 a) { return a.h != 0.0f && fe(a) < ftop[k] - 16; };
-    small = small || fsmall(g.c[U][k]) || fsmall(g.c[B][0]) || fsmall(g.c[B][1]) ||
-            fsmall(g.c[C][0]) || fsmall(g.c[C][1]) || fe(g.d[B]) < ftop[k] - 16;
+    small = small || fsmall(fa[k]) || fsmall(fb[0]) || fsmall(fb[1]) || fsmall(fc[0]) ||
+            fsmall(fc[1]) || fe(fw) < ftop[k] - 16;
   }
   if (small) return false;
   const float2 sc = mk2(pow2f(127 - ftop[0]), pow2f(127 - ftop[1]));
   const auto both = [&](F2 a) { return p2_scale(pk(a, a), sc); };
   const auto per = [&](F2 a0, F2 a1) { return p2_scale(pk(a0, a1), sc); };
-  const F2 a0 = g.c[U][0], a1 = g.c[U][1];
-  const bool n0 = a0.h < 0.0f, n1 = a1.h < 0.0f;
-  o = face_core_p2(per(n0 ? f2_neg(a0) : a0, n1 ? f2_neg(a1) : a1), both(g.c[B][0]),
-                   both(g.c[B][1]), both(g.c[C][0]), both(g.c[C][1]),
-                   per(rr(0, 0, 0), rr(1, 0, 0)), per(rr(0, 0, 1), rr(1, 0, 1)),
-                   per(rr(0, 1, 0), rr(1, 1, 0)), per(rr(0, 1, 1), rr(1, 1, 1)), both(g.d[B]),
-                   same_sign, T);
+  const bool n0 = fa[0].h < 0.0f, n1 = fa[1].h < 0.0f;
+  const bool same_sign = !(neg_not_tiny(bd[0]) && !nonpos_or_tiny(bd[1]));
+  o = face_core_p2(per(n0 ? f2_neg(fa[0]) : fa[0], n1 ? f2_neg(fa[1]) : fa[1]), both(fb[0]),
+                   both(fb[1]), both(fc[0]), both(fc[1]), per(fr[0][0][0], fr[1][0][0]),
+                   per(fr[0][0][1], fr[1][0][1]), per(fr[0][1][0], fr[1][1][0]),
+                   per(fr[0][1][1], fr[1][1][1]), both(fw), same_sign, T);
   F2 o0 = lane0(o), o1 = lane1(o);
   if (n0) o0 = f2_neg(o0);
   if (n1) o1 = f2_neg(o1);
   // a point in a face plane: that face's outside limit
-  if (is_tiny(rel_bound(q, U, 0)) || is_tiny(rel_bound(q, U, 1))) {
-    const double b1 = rel_bound(q, B, 0), b2 = rel_bound(q, B, 1);
-    const double c1 = rel_bound(q, C, 0), c2 = rel_bound(q, C, 1);
-    if (is_tiny(rel_bound(q, U, 0))) o0 = face_limit_f2(b1, b2, c1, c2, false);
-    if (is_tiny(rel_bound(q, U, 1))) o1 = face_limit_f2(b1, b2, c1, c2, true);
+  if (is_tiny(ad[0]) || is_tiny(ad[1])) {
+    if (is_tiny(ad[0])) o0 = face_limit_f2(bd[0], bd[1], cd[0], cd[1], false);
+    if (is_tiny(ad[1])) o1 = face_limit_f2(bd[0], bd[1], cd[0], cd[1], true);
   }
   o = pk(o0, o1);
+  return true;
+}
+
+// The two faces normal to U (x faces: b = y, c = z; y faces: b = x, c = z;
+// z faces: b = x, c = y).
+template <int U>
+HG_HD __forceinline__ bool faces_p2(const Rel& q, const GeomF2& g, const Tables& T,
+                                    lean::P2& o) {
+  using namespace lean;
+  constexpr int B = U == 0 ? 1 : 0, C = U == 2 ? 1 : 2;
+  F2 fr[2][2][2];
+#pragma unroll
+  for (int k = 0; k < 2; k++)
+#pragma unroll
+    for (int bi = 0; bi < 2; bi++)
+#pragma unroll
+      for (int ci = 0; ci < 2; ci++) {
+        int id[3];
+        id[U] = k;
+        id[B] = bi;
+        id[C] = ci;
+        fr[k][bi][ci] = g.r[id[0]][id[1]][id[2]];
+      }
+  const double ad[2] = {rel_bound(q, U, 0), rel_bound(q, U, 1)};
+  const double bd[2] = {rel_bound(q, B, 0), rel_bound(q, B, 1)};
+  const double cd[2] = {rel_bound(q, C, 0), rel_bound(q, C, 1)};
+  return face_pair_p2(g.c[U], g.c[B], g.c[C], fr, g.d[B], ad, bd, cd, T, o);
+}
+
+// All six faces O[axis][k] as three face pairs in a loop over the axis that
+// is not unrolled (one copy of the face code; inputs chosen by selects).
+HG_HD __forceinline__ bool faces_all_p2(const Rel& q, const GeomF2& g, const Tables& T,
+                                        double O[3][2]) {
+  using namespace lean;
+#pragma unroll 1
+  for (int axis = 0; axis < 3; axis++) {
+    const bool X = axis == 0, Y = axis == 1;
+    F2 fr[2][2][2];
+#pragma unroll
+    for (int k = 0; k < 2; k++)
+#pragma unroll
+      for (int bi = 0; bi < 2; bi++)
+#pragma unroll
+        for (int ci = 0; ci < 2; ci++)
+          fr[k][bi][ci] = X ? g.r[k][bi][ci] : (Y ? g.r[bi][k][ci] : g.r[bi][ci][k]);
+    const F2 fa[2] = {X ? g.c[0][0] : (Y ? g.c[1][0] : g.c[2][0]),
+                      X ? g.c[0][1] : (Y ? g.c[1][1] : g.c[2][1])};
+    const F2 fb[2] = {X ? g.c[1][0] : g.c[0][0], X ? g.c[1][1] : g.c[0][1]};
+    const F2 fc[2] = {(X || Y) ? g.c[2][0] : g.c[1][0], (X || Y) ? g.c[2][1] : g.c[1][1]};
+    const F2 fw = X ? g.d[1] : g.d[0];
+    const double ad[2] = {rel_bound(q, axis, 0), rel_bound(q, axis, 1)};
+    const double bd[2] = {X ? q.y1 : q.x1, X ? q.y2 : q.x2};
+    const double cd[2] = {(X || Y) ? q.z1 : q.y1, (X || Y) ? q.z2 : q.y2};
+    P2 o;
+    if (!face_pair_p2(fa, fb, fc, fr, fw, ad, bd, cd, T, o)) return false;
+    const double o0 = f2_to_double(lane0(o), 0), o1 = f2_to_double(lane1(o), 0);
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      O[a][0] = axis == a ? o0 : O[a][0];
+      O[a][1] = axis == a ? o1 : O[a][1];
+    }
+  }
   return true;
 }
 
@@ -1062,11 +1117,8 @@ HG_HD __forceinline__ bool pair_grad_p2(const Rel& q, const Tables& T, double& o
     if (o1.h == 0.0f) L.h.y = L.l.y = 0.0f;
     v2 = p2_add(v2, p2_mul(pk(f2_neg(o0), o1), L));
   }
-  constexpr int B = U == 0 ? 1 : 0;
-  const bool same_sign =
-      !(neg_not_tiny(rel_bound(q, B, 0)) && !nonpos_or_tiny(rel_bound(q, B, 1)));
   P2 o;
-  if (!faces_p2<U>(q, g, same_sign, T, o)) return false;
+  if (!faces_p2<U>(q, g, T, o)) return false;
   if (o_faces) {
     o_faces[0] = f2_to_double(lane0(o), 0);
     o_faces[1] = f2_to_double(lane1(o), 0);
@@ -1085,11 +1137,8 @@ HG_HD __forceinline__ bool pair_diag_p2(const Rel& q, const Tables& T, double& o
   using namespace lean;
   GeomF2 g;
   if (!make_geom_f2(q, g)) return false;
-  constexpr int B = U == 0 ? 1 : 0;
-  const bool same_sign =
-      !(neg_not_tiny(rel_bound(q, B, 0)) && !nonpos_or_tiny(rel_bound(q, B, 1)));
   P2 o;
-  if (!faces_p2<U>(q, g, same_sign, T, o)) return false;
+  if (!faces_p2<U>(q, g, T, o)) return false;
   out = f2_to_double(f2_sub(lane0(o), lane1(o)), 0);
   return true;
 }
@@ -1111,8 +1160,9 @@ HG_HD __forceinline__ void pair_all(const Rel& q, const Tables& T, double out[kN
   edges_z(g, Ez);
   double Lx[2][2], Ly[2][2], Lz[2][2];
   logs12<LEAN>(Ex, Ey, Ez, T, Lx, Ly, Lz);
-  double O[3][2];
-  faces6<LEAN>(g, T, O);
+  double O[3][2] = {{0.0, 0.0}, {0.0, 0.0}, {0.0, 0.0}};
+  GeomF2 gf;
+  if (!LEAN || !make_geom_f2(q, gf) || !faces_all_p2(q, gf, T, O)) faces6<LEAN>(g, T, O);
   const double* Ox = O[0];
   const double* Oy = O[1];
   const double* Oz = O[2];
@@ -1238,8 +1288,9 @@ template <bool LEAN>
 HG_HD __forceinline__ void pair_tensor6(const Rel& q, const Tables& T, double t[6]) {
   Geom g;
   make_geom<LEAN>(q, g);
-  double O[3][2];
-  faces6<LEAN>(g, T, O);
+  double O[3][2] = {{0.0, 0.0}, {0.0, 0.0}, {0.0, 0.0}};
+  GeomF2 gf;
+  if (!LEAN || !make_geom_f2(q, gf) || !faces_all_p2(q, gf, T, O)) faces6<LEAN>(g, T, O);
   t[0] = O[0][0] - O[0][1];
   t[1] = O[1][0] - O[1][1];
   t[2] = O[2][0] - O[2][1];
