@@ -1131,6 +1131,48 @@ HG_HD __forceinline__ bool pair_grad_p2(const Rel& q, const Tables& T, double& o
   return true;
 }
 
+// The two merged logs M_v = ln(R(v, u_1) / R(v, u_0)) of the edges parallel
+// to A at the two V-bounds (lanes v = 0, 1), merged along U (merged_t).
+template <int A, int V, int U>
+HG_HD __forceinline__ lean::P2 merged_pair_p2(const Rel& q, const GeomF2& g, const Tables& T) {
+  using namespace lean;
+  const AxisCase c = axis_case(rel_bound(q, A, 0), rel_bound(q, A, 1));
+  const F2 lo = c.reflect ? f2_neg(g.c[A][1]) : g.c[A][0];
+  const F2 hi = c.reflect ? f2_neg(g.c[A][0]) : g.c[A][1];
+  const int il = c.reflect ? 1 : 0;
+  const auto rr = [&](int end, int vb, int eu) {
+    int id[3];
+    id[A] = end;
+    id[V] = vb;
+    id[U] = eu;
+    return g.r[id[0]][id[1]][id[2]];
+  };
+  const auto lanes = [&](int end, int eu) {
+    const int e = il ? 1 - end : end;
+    return pk(rr(e, 0, eu), rr(e, 1, eu));
+  };
+  const auto bc = [](F2 a) { return pk(a, a); };
+  const P2 t = merged_t_p2(c.straddle, bc(lo), bc(hi), pk(g.c[V][0], g.c[V][1]), bc(g.c[U][1]),
+                           lanes(0, 0), lanes(0, 1), lanes(1, 0), lanes(1, 1), bc(g.d[A]),
+                           bc(g.d[U]), bc(f2_add(g.c[U][0], g.c[U][1])));
+  return log1p_p2(t, T);
+}
+
+// Off-diagonal tensor combination sum_{p,s} s_p s_s L[p][s] of the 4 edges
+// parallel to A (= ln(R11 R00 / (R01 R10)), p along V, s along U) as the
+// difference of the two merged logs M_1 - M_0.  Each M keeps its relative
+// accuracy; the difference loses the first order of the distance (the FP64
+// product of the four ratios loses the second).  false: FP64 path.
+template <int A, int V, int U>
+HG_HD __forceinline__ bool pair_offdiag_p2(const Rel& q, const Tables& T, double& out) {
+  using namespace lean;
+  GeomF2 g;
+  if (!make_geom_f2(q, g)) return false;
+  const P2 M = merged_pair_p2<A, V, U>(q, g, T);
+  out = f2_to_double(f2_sub(lane1(M), lane0(M)), 0);
+  return true;
+}
+
 // pair_diag_f2 with the two faces evaluated together.
 template <int U>
 HG_HD __forceinline__ bool pair_diag_p2(const Rel& q, const Tables& T, double& out) {
@@ -1277,6 +1319,16 @@ HG_HD __forceinline__ double pair_field(const Rel& q, const Tables& T) {
     if (pair_diag_p2<(F == kGee ? 0 : (F == kGnn ? 1 : 2))>(q, T, v)) return v;
     return pair_field_fp64<F>(q, T);
   }
+  if (LEAN && (F == kGen || F == kGez || F == kGnz)) {
+    // edges along z at (x_i, y_j) for g_en, along y at (x_i, z_k) for g_ez,
+    // along x at (y_j, z_k) for g_nz: p along the first in-plane axis
+    double v;
+    const bool ok = F == kGen   ? pair_offdiag_p2<2, 0, 1>(q, T, v)
+                    : F == kGez ? pair_offdiag_p2<1, 0, 2>(q, T, v)
+                                : pair_offdiag_p2<0, 1, 2>(q, T, v);
+    if (ok) return v;
+    return pair_field_fp64<F>(q, T);
+  }
   return pair_field_geom<F, LEAN>(q, T);
 }
 
@@ -1286,6 +1338,24 @@ HG_HD __forceinline__ double pair_field(const Rel& q, const Tables& T) {
 // not masked here (the caller decides).
 template <bool LEAN>
 HG_HD __forceinline__ void pair_tensor6(const Rel& q, const Tables& T, double t[6]) {
+  if (LEAN) {
+    // float-pair geometry: faces as three packed pairs, the off-diagonal
+    // combinations as differences of merged logs (pair_offdiag_p2)
+    GeomF2 gf;
+    double O[3][2];
+    if (make_geom_f2(q, gf) && faces_all_p2(q, gf, T, O)) {
+      t[0] = O[0][0] - O[0][1];
+      t[1] = O[1][0] - O[1][1];
+      t[2] = O[2][0] - O[2][1];
+      const auto diff = [](lean::P2 M) {
+        return lean::f2_to_double(lean::f2_sub(lean::lane1(M), lean::lane0(M)), 0);
+      };
+      t[3] = diff(merged_pair_p2<2, 0, 1>(q, gf, T));
+      t[4] = diff(merged_pair_p2<1, 0, 2>(q, gf, T));
+      t[5] = diff(merged_pair_p2<0, 1, 2>(q, gf, T));
+      return;
+    }
+  }
   Geom g;
   make_geom<LEAN>(q, g);
   double O[3][2] = {{0.0, 0.0}, {0.0, 0.0}, {0.0, 0.0}};
