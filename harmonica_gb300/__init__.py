@@ -16,6 +16,7 @@ in ``include/harmonica_gb300.h``; :func:`build` compiles them in-tree.
 from ._native import build
 from .adjoint import layer_gravity_torch, prism_gravity_torch
 from .batch import PrismBatch, autotune, prism_gravity_batch
+from .device_layer import DevicePrismLayer, prism_layer_device
 from .fields import FIELDS
 from .gravity import check_prisms, prism_gravity, prism_gravity_fields
 from .layer import DatasetAccessorPrismLayer, PrismLayer, prism_layer
@@ -23,6 +24,8 @@ from .magnetic import prism_magnetic
 from .point import point_gravity
 
 __all__ = [
+    "DevicePrismLayer",
+    "prism_layer_device",
     "FIELDS",
     "PrismBatch",
     "autotune",

@@ -95,6 +95,22 @@ __global__ void reduce_chunks_kernel(const double* __restrict__ part, int64_t n_
   out[idx] = s * field_scale(row_field.f[row]);
 }
 
+// top/bottom of a layer from surface and reference (layer.py:264-312): the
+// surface is the top where it is not below the reference; a NaN surface
+// compares false and stays the top, with the reference as the bottom.
+__global__ void layer_top_bottom_kernel(const double* __restrict__ surface,
+                                        const double* __restrict__ reference, double ref_scalar,
+                                        int64_t n, double* __restrict__ top,
+                                        double* __restrict__ bottom) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double s = surface[i];
+  const double r = reference ? reference[i] : ref_scalar;
+  const bool reverse = s < r;
+  top[i] = reverse ? r : s;
+  bottom[i] = reverse ? s : r;
+}
+
 __global__ void pack_prisms_kernel(const double* __restrict__ aos, const double* __restrict__ rho,
                                    int64_t n, double* __restrict__ soa, int64_t stride) {
   int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -235,6 +251,18 @@ int hg_pack_prisms(const double* prisms_aos, const double* density, int64_t n_pr
   pack_prisms_kernel<<<(unsigned)blocks, threads, 0, (cudaStream_t)stream>>>(
       prisms_aos, density, n_prisms, prisms_soa, prism_stride);
   return cuda_check(cudaGetLastError(), "pack_prisms_kernel launch");
+}
+
+int hg_layer_top_bottom(const double* surface, const double* reference, double reference_value,
+                        int64_t n, double* top, double* bottom, void* stream) {
+  if (n < 0) return set_error(HG_ERR_INVALID, "bad size");
+  if (n == 0) return HG_OK;
+  if (!surface || !top || !bottom) return set_error(HG_ERR_INVALID, "null pointer");
+  const int threads = 256;
+  const int64_t blocks = (n + threads - 1) / threads;
+  layer_top_bottom_kernel<<<(unsigned)blocks, threads, 0, (cudaStream_t)stream>>>(
+      surface, reference, reference_value, n, top, bottom);
+  return cuda_check(cudaGetLastError(), "layer_top_bottom_kernel launch");
 }
 
 int hg_prism_forward_workspace(int64_t n_obs, int64_t n_prisms, uint32_t field_mask,

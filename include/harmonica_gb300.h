@@ -56,6 +56,17 @@ int hg_pack_prisms(const double *prisms_aos, const double *density, int64_t n_pr
                    double *prisms_soa, int64_t prism_stride, void *stream);
 
 /*
+ * Top and bottom of a layer of prisms from its surface and reference
+ * (replaces the host update in DatasetAccessorPrismLayer.update_top_bottom,
+ * src/harmonica/_forward/prisms/layer.py:264-312): element-wise, top = the
+ * reference where the surface is below it, else the surface; bottom the
+ * other one.  reference: n doubles (device), or NULL to use reference_value
+ * everywhere.  All arrays in device memory; asynchronous on `stream`.
+ */
+int hg_layer_top_bottom(const double *surface, const double *reference, double reference_value,
+                        int64_t n, double *top, double *bottom, void *stream);
+
+/*
  * Bytes of device workspace hg_prism_forward needs for this problem
  * (0 when the launch writes `out` directly).
  */

@@ -180,3 +180,13 @@ def test_layer_invalid_field(dummy_layer):
     msg = re.escape("Gravitational field 'invalid field' not recognized.")
     with pytest.raises(ValueError, match=msg):
         layer.prism_layer.gravity((0, 0, 0), field="invalid field")
+
+
+def test_device_layer_exported():
+    """The device-resident layer API is part of the package (GPU behaviour in
+    test_gpu_device_layer.py)."""
+    import harmonica_gb300 as hg
+
+    assert callable(hg.prism_layer_device)
+    assert hasattr(hg.DevicePrismLayer, "update_top_bottom")
+    assert hasattr(hg.DevicePrismLayer, "gravity")
