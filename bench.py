@@ -78,7 +78,8 @@ def parse_args():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-all-fields", action="store_true")
     p.add_argument("--all-fields-stations", type=int, default=1000)
-    p.add_argument("--workload", default="layer", choices=["layer", "batched", "inversion", "serving", "points", "magnetic"],
+    p.add_argument("--workload", default="layer", choices=["layer", "batched", "inversion", "serving", "points", "magnetic",
+                            "tesseroids"],
                    help="layer: the 1e6-prism layer (default); batched: 256 uneven "
                         "g_z/g_zz problems, one persistent graph-captured launch vs one "
                         "launch per problem")
@@ -584,6 +585,116 @@ def run_magnetic(args, rank, world, local):
                           "gpu_launches": 2 * args.steps}))
 
 
+# FP64 thread-instructions per tesseroid pair of the tesseroid forward kernel on the
+# Andes layer (ncu sm__sass_thread_inst_executed_op_{dadd,dmul,dfma}_pred_on over the
+# launch / pairs, small case of the same kernel); None until captured.
+FP64_INST_PER_TESS_PAIR = None
+
+
+def run_tesseroids(args, rank, world, local):
+    """Tesseroid layer g_z: the gallery's Andes tesseroid layer (93,121 tesseroids,
+    3,825 points 10 km above the reference), one full forward per step."""
+    import torch
+
+    import harmonica_gb300 as hg
+    from harmonica_gb300 import _native, synthetic, tesseroid
+
+    _native.build()
+    lib = _native.lib()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    L = synthetic.tesseroid_layer_andes()
+    tess, dens, coords = L["tesseroids"], L["density"], L["coordinates"]
+    n_obs, m = coords[0].size, tess.shape[0]
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).to(dev)  # noqa: E731
+    c = [T(x) for x in coords]
+    t_dev, rho = T(tess), T(dens)
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 8, dtype=torch.float64, device=dev)
+
+    def step():
+        return tesseroid.tesseroid_gravity_device(c[0], c[1], c[2], t_dev, rho, "g_z",
+                                                  status=status)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    peak = fp64_peak(torch, lib)
+    sampler = ClockSampler(local)
+    sampler.start()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    t_wall = time.perf_counter()
+    for s in range(args.steps):
+        flush.fill_(float(s))  # L2 flush between timed steps (outside the events)
+        starts[s].record()
+        out = step()
+        ends[s].record()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t_wall
+    clocks = sampler.stop()
+    if int(status.item()) != 0:
+        raise RuntimeError("tesseroid forward reported an overflow on the bench workload")
+    step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    dev_time = sum(step_ms) * 1e-3
+    pairs = n_obs * m * args.steps
+    value = pairs / dev_time
+
+    e2e = None
+    if not args.no_e2e:
+        hg.tesseroid_gravity(coords, tess, dens, field="g_z")  # warm
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            res = hg.tesseroid_gravity(coords, tess, dens, field="g_z")
+        e2e_time = time.perf_counter() - t0
+        e2e = {"value": pairs / e2e_time, "unit": "pairs/s",
+               "h2d_bytes_per_step": 8 * (3 * n_obs + 6 * m + m), "d2h_bytes_per_step": 8 * n_obs,
+               "path": "harmonica_gb300.tesseroid_gravity with numpy inputs (checks, "
+                       "points-inside test on the GPU, copies, forward)"}
+        ref_dev = out.cpu().numpy()
+        if not np.allclose(res, ref_dev, rtol=1e-12, atol=0):
+            raise RuntimeError("device and end-to-end tesseroid results differ")
+
+    base = None
+    if rank == 0 and not args.no_cpu_baseline:
+        from oracle import tesseroid_oracle
+
+        idx = np.linspace(0, n_obs - 1, max(args.cpu_sample_stations, 512)).astype(int)
+        sub = tuple(x[idx] for x in coords)
+        t0 = time.perf_counter()
+        tesseroid_oracle.tesseroid_gravity(sub, tess, dens, "g_z")
+        dt = time.perf_counter() - t0
+        base = {"value": idx.size * m / dt, "unit": "pairs/s", "cores": os.cpu_count() or 1,
+                "kind": "port",
+                "sample": f"{idx.size} strided points x all {m} tesseroids ({dt:.1f} s, "
+                          "OpenMP over points)"}
+    if rank != 0:
+        return
+    kernel_rate = n_obs * m / (dev_time / args.steps)
+    roof = {"bound": "fp64", "peak": peak, "unit": "TFLOP/s",
+            "peak_source": "measured live: hg_fp64_peak_probe (FP64 FMA chains)",
+            "traffic": None}
+    if FP64_INST_PER_TESS_PAIR:
+        # the FP64 pipe issues one instruction per FMA; the probe's peak counts 2 flops per FMA
+        achieved = 2.0 * FP64_INST_PER_TESS_PAIR * kernel_rate / 1e12
+        roof.update({"achieved": achieved, "frac": achieved / peak,
+                     "fp64_inst_per_pair": FP64_INST_PER_TESS_PAIR,
+                     "note": "achieved = FP64 instructions issued x 2 flops, per pair from ncu"})
+    print(json.dumps({
+        "metric": "FP64 tesseroid g_z pairs/s (points x tesseroids, adaptive GLQ)",
+        "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": wall / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": f"tesseroid layer, Andes region at 0.1 deg ({m} tesseroids), "
+                               f"{n_obs} points 10 km above the WGS84 reference",
+                   "l2": "flushed between timed steps (256 MB write)"},
+        "roofline": roof, "cpu_baseline": base, "e2e": e2e,
+        "gpu_launches": 3 * args.steps, "clocks": clocks, "step_ms": step_ms,
+    }))
+
+
 def main():
     args = parse_args()
     rank, world, local = dist_env()
@@ -604,6 +715,9 @@ def main():
         return
     if args.workload == "magnetic":
         run_magnetic(args, rank, world, local)
+        return
+    if args.workload == "tesseroids":
+        run_tesseroids(args, rank, world, local)
         return
 
     import torch

@@ -8,6 +8,8 @@ harmonica):
 * :func:`prism_gravity` -- ``harmonica.prism_gravity``
 * :func:`prism_layer` and the ``prism_layer`` accessor
   (:class:`DatasetAccessorPrismLayer`) -- ``harmonica.prism_layer``
+* :func:`point_gravity`, :func:`prism_magnetic`, :func:`tesseroid_gravity`
+  -- the point-mass, magnetic-prism and tesseroid forward models
 
 The all-pairs sums run in hand-written CUDA kernels behind the C ABI declared
 in ``include/harmonica_gb300.h``; :func:`build` compiles them in-tree.
@@ -22,6 +24,7 @@ from .gravity import check_prisms, prism_gravity, prism_gravity_fields
 from .layer import DatasetAccessorPrismLayer, PrismLayer, prism_layer
 from .magnetic import prism_magnetic
 from .point import point_gravity
+from .tesseroid import tesseroid_gravity
 
 __all__ = [
     "DevicePrismLayer",
@@ -41,4 +44,5 @@ __all__ = [
     "prism_layer",
     "point_gravity",
     "prism_magnetic",
+    "tesseroid_gravity",
 ]

@@ -28,7 +28,7 @@ HEADERS = (
 #: translation units compiled into the library
 SOURCES = (
     "prism_forward.cu", "prism_batch.cu", "prism_adjoint.cu", "point_forward.cu",
-    "prism_magnetic.cu", "bench_probe.cu",
+    "prism_magnetic.cu", "tesseroid_forward.cu", "bench_probe.cu",
 )
 
 ARCH_FLAGS = ("-gencode", "arch=compute_103a,code=sm_103a")
@@ -236,6 +236,21 @@ PROTOTYPES = {
         [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32,
          ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p],
+    ),
+    "hg_tesseroid_forward_workspace": (
+        ctypes.c_int, [ctypes.c_int64, ctypes.c_int64, ctypes.POINTER(ctypes.c_size_t)]
+    ),
+    "hg_tesseroid_forward": (
+        ctypes.c_int,
+        [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+         ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+         ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+         ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p],
+    ),
+    "hg_tesseroid_inside": (
+        ctypes.c_int,
+        [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+         ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p],
     ),
     "hg_fp64_peak_probe": (
         ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_void_p]

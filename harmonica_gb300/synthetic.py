@@ -134,3 +134,55 @@ def basement_layer(n_side=200, spacing=500.0, seed=5, noise_seed=6, n_stations_s
     return dict(easting=easting, northing=northing, top=np.zeros_like(bottom), bottom=bottom,
                 density=np.full_like(bottom, contrast), coordinates=coordinates,
                 noise_seed=noise_seed)
+
+
+# WGS84 semi-axes (metres)
+_WGS84_A = 6378137.0
+_WGS84_B = 6356752.314245179
+
+
+def geocentric_radius(latitude):
+    """Geocentric radius of the WGS84 ellipsoid at geodetic latitudes (degrees)."""
+    phi = np.radians(latitude)
+    a, b = _WGS84_A, _WGS84_B
+    num = (a**2 * np.cos(phi)) ** 2 + (b**2 * np.sin(phi)) ** 2
+    den = (a * np.cos(phi)) ** 2 + (b * np.sin(phi)) ** 2
+    return np.sqrt(num / den)
+
+
+def tesseroid_layer_andes(spacing=0.1, station_spacing=0.5, height=10e3, seed=9):
+    """
+    Tesseroid layer with the shape of harmonica's tesseroid-layer gallery
+    example (doc/gallery_src/forward/tesseroid_layer.py): region
+    (-78, -53, -57, -20) degrees on a 0.1-degree grid (251 x 371 =
+    93,121 tesseroids), reference surface the WGS84 geocentric radius, density
+    2670 kg/m^3 above it and 1040 - 2670 below, computation points on a
+    0.5-degree grid (51 x 75 = 3,825) 10 km above the reference.  The
+    topography is synthetic (seeded): a mountain range along -69 degrees
+    (up to ~6 km) over an ocean floor of ~-4.5 km in the east and west,
+    plus 40 random bumps.  Returns dict(tesseroids (M, 6), density (M,),
+    coordinates (3 arrays), shape).
+    """
+    w, e, s, n = -78.0, -53.0, -57.0, -20.0
+    lon = np.round(np.arange(w, e + spacing / 2, spacing), 10)
+    lat = np.round(np.arange(s, n + spacing / 2, spacing), 10)
+    glon, glat = np.meshgrid(lon, lat)
+    rng = np.random.default_rng(seed)
+    topo = 5500.0 * np.exp(-((glon + 69.0) ** 2) / (2 * 1.5**2)) - 4500.0 * (
+        1 - np.exp(-((glon + 66.0) ** 2) / (2 * 9.0**2)))
+    for _ in range(40):
+        clon, clat = rng.uniform(w, e), rng.uniform(s, n)
+        topo += rng.normal(0, 900.0) * np.exp(
+            -((glon - clon) ** 2 + (glat - clat) ** 2) / (2 * rng.uniform(0.3, 2.0) ** 2))
+    reference = geocentric_radius(glat)
+    surface = topo + reference
+    top = np.maximum(surface, reference)
+    bottom = np.minimum(surface, reference)
+    density = np.where(topo > 0, 2670.0, 1040.0 - 2670.0)
+    h = spacing / 2
+    tess = np.stack([glon - h, glon + h, glat - h, glat + h, bottom, top], axis=-1).reshape(-1, 6)
+    slon = np.arange(w, e + station_spacing / 2, station_spacing)
+    slat = np.arange(s, n + station_spacing / 2, station_spacing)
+    plon, plat = np.meshgrid(slon, slat)
+    coords = (plon.ravel(), plat.ravel(), geocentric_radius(plat).ravel() + height)
+    return dict(tesseroids=tess, density=density.ravel(), coordinates=coords, shape=glon.shape)

@@ -315,6 +315,57 @@ int hg_point_forward(const double *obs_1, const double *obs_2, const double *obs
                      int32_t spherical, int32_t field, double *out, void *workspace,
                      size_t workspace_bytes, void *stream);
 
+/*
+ * ---------------------------------------------------------------------------
+ * Tesseroids (spherical prisms) of constant density.  Replaces
+ * jit_tesseroid_gravity_parallel/serial (src/harmonica/_forward/
+ * tesseroid_gravity.py:236-333) with the adaptive discretisation and
+ * Gauss-Legendre quadrature of _tesseroid_utils.py:18-295, and the
+ * null-tesseroid discard (_tesseroid_utils.py:503-538), behind
+ * tesseroid_gravity (tesseroid_gravity.py:35-216).
+ *
+ * longitude, latitude (degrees), radius (m): n_obs computation points.
+ * tesseroids: n_tesseroids rows of (west, east, south, north, bottom, top)
+ * in degrees and metres, row-major, already made continuous in longitude
+ * (west <= east, as _check_tesseroids leaves them); density in kg/m^3.
+ * field: 0 potential (J/kg) or 3 g_z (mGal, downward).
+ * radial_discretization: nonzero splits along the radius too.
+ * stack_size (<= 100) and max_discretizations: the reference's STACK_SIZE
+ * and MAX_DISCRETIZATIONS (tesseroid_gravity.py:27-28); <= 0 gives 100 and
+ * 100000.
+ * glq_nodes, glq_weights: HOST arrays of 6 (longitude, latitude, radius x 2
+ * nodes), the degree-2 Gauss-Legendre rule (numpy leggauss(2) in the
+ * reference); NULL uses -+1/sqrt(3) and weights 1.
+ * status: optional device int32 OR-ed with 1 when a pair overflows the
+ * stack ("Stack Overflow") and 2 when a pair needs more than
+ * max_discretizations small tesseroids ("Exceeded maximum discretizations"); the
+ * output is then not the reference's (which raises OverflowError).
+ * Stream-ordered; workspace from hg_tesseroid_forward_workspace (NULL: the
+ * call allocates stream-ordered).
+ */
+int hg_tesseroid_forward_workspace(int64_t n_obs, int64_t n_tesseroids, size_t *bytes);
+
+int hg_tesseroid_forward(const double *longitude, const double *latitude, const double *radius,
+                         int64_t n_obs, const double *tesseroids, const double *density,
+                         int64_t n_tesseroids, int32_t field, int32_t radial_discretization,
+                         int32_t stack_size, int64_t max_discretizations,
+                         const double *glq_nodes, const double *glq_weights, double *out,
+                         int32_t *status, void *workspace, size_t workspace_bytes,
+                         void *stream);
+
+/*
+ * Points inside tesseroids (_check_points_outside_tesseroids,
+ * _tesseroid_utils.py:446-468): counts the (point, tesseroid) pairs with the
+ * point strictly inside the tesseroid (longitude compared in [0, 360) and
+ * [-180, 180)) into the device int64 *n_conflicts and stores the first
+ * `capacity` of them as (point, tesseroid) index pairs in the device array
+ * conflicts (2 x capacity int64, unordered).
+ */
+int hg_tesseroid_inside(const double *longitude, const double *latitude, const double *radius,
+                        int64_t n_obs, const double *tesseroids, int64_t n_tesseroids,
+                        int64_t *conflicts, int64_t capacity, int64_t *n_conflicts,
+                        void *stream);
+
 #ifdef __cplusplus
 }
 #endif

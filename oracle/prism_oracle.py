@@ -56,8 +56,9 @@ def _load():
     global _lib
     if _lib is not None:
         return _lib
-    if not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(
-        os.path.join(HERE, "prism_oracle.c")
+    sources = [os.path.join(HERE, f) for f in ("prism_oracle.c", "tesseroid_oracle.c")]
+    if not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < max(
+        os.path.getmtime(f) for f in sources
     ):
         build_oracle()
     lib = ctypes.CDLL(LIB_PATH)
@@ -89,6 +90,25 @@ def _load():
     lib.oracle_is_singular.restype = ctypes.c_int
     lib.oracle_is_singular.argtypes = [
         ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, dp
+    ]
+    lib.oracle_tesseroid_dimensions.restype = None
+    lib.oracle_tesseroid_dimensions.argtypes = [dp, dp]
+    lib.oracle_distance_tesseroid_point.restype = ctypes.c_double
+    lib.oracle_distance_tesseroid_point.argtypes = [
+        ctypes.c_double, ctypes.c_double, ctypes.c_double, dp
+    ]
+    lib.oracle_tesseroid_glq.restype = ctypes.c_double
+    lib.oracle_tesseroid_glq.argtypes = [
+        ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, dp,
+        ctypes.c_double, dp, dp,
+    ]
+    lib.oracle_adaptive_discretization.restype = i64
+    lib.oracle_adaptive_discretization.argtypes = [
+        dp, dp, ctypes.c_double, ctypes.c_int, ctypes.c_int, i64, dp, i64
+    ]
+    lib.oracle_tesseroid_gravity.restype = ctypes.c_int
+    lib.oracle_tesseroid_gravity.argtypes = [
+        ctypes.c_int, ctypes.c_int, i64, dp, dp, dp, i64, dp, dp, dp, dp, dp, ctypes.c_int
     ]
     _lib = lib
     return lib
