@@ -586,9 +586,9 @@ def run_magnetic(args, rank, world, local):
 
 
 # FP64 thread-instructions per tesseroid pair of the tesseroid forward kernel on the
-# Andes layer (ncu sm__sass_thread_inst_executed_op_{dadd,dmul,dfma}_pred_on over the
-# launch / pairs, small case of the same kernel); None until captured.
-FP64_INST_PER_TESS_PAIR = None
+# Andes layer: ncu sm__sass_thread_inst_executed_op_fp64_pred_on.sum of one launch
+# (5.119e10) over its 3825 x 93121 pairs (profiles/tesseroid_forward_andes.md).
+FP64_INST_PER_TESS_PAIR = 143.7
 
 
 def run_tesseroids(args, rank, world, local):
@@ -676,11 +676,13 @@ def run_tesseroids(args, rank, world, local):
             "peak_source": "measured live: hg_fp64_peak_probe (FP64 FMA chains)",
             "traffic": None}
     if FP64_INST_PER_TESS_PAIR:
-        # the FP64 pipe issues one instruction per FMA; the probe's peak counts 2 flops per FMA
+        # the FP64 pipe issues one instruction per FMA; the probe's peak counts 2 flops per
+        # FMA, so FP64 instructions x 2 against it is the pipe's instruction-rate fraction
         achieved = 2.0 * FP64_INST_PER_TESS_PAIR * kernel_rate / 1e12
         roof.update({"achieved": achieved, "frac": achieved / peak,
                      "fp64_inst_per_pair": FP64_INST_PER_TESS_PAIR,
-                     "note": "achieved = FP64 instructions issued x 2 flops, per pair from ncu"})
+                     "note": "achieved = FP64 instructions issued per pair (ncu) x pairs/s x 2 "
+                             "(FMA-equivalent flops), against the FP64 FMA-chain peak"})
     print(json.dumps({
         "metric": "FP64 tesseroid g_z pairs/s (points x tesseroids, adaptive GLQ)",
         "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,

@@ -18,12 +18,17 @@
 // expensive pairs instead of idling behind one of them.  Queued pairs are
 // added to their point's sum in list order: results are deterministic.
 //
-// Arithmetic.  FP64 throughout with the reference's operation order and no
-// contraction into fused multiply-adds (__dmul_rn / __dadd_rn), so results
-// differ from the reference only through the last bits of cos/sin/acos.
-// The split test distance / size < ratio is evaluated exactly; a cheap
-// pre-test distance >= ratio * size * (1 + 2^-40) proves "no split" for most
-// pairs without the division.
+// Arithmetic.  FP64 throughout.  The split decisions and every small
+// tesseroid of a split pair follow the reference's operation order without
+// contraction into fused multiply-adds (__dmul_rn / __dadd_rn), so they
+// differ from the reference only through the last bits of cos/sin/acos.  The
+// split test distance / size < ratio is evaluated exactly whenever it is not
+// settled by a pre-test on the squared distance with a rigorous error margin
+// (distance >= ratio * size * (1 + 2^-40) proves "no split").  Unsplit
+// tesseroids -- nearly all pairs -- are summed by glq_eval_fast: the same 8
+// point masses with cos(lambda_p - lambda) from precomputed cosines and sines
+// and 1 / l from a reciprocal square root, within a few units in the last
+// place of the reference's terms at about half the FP64 instructions.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -31,6 +36,7 @@
 #include <string>
 
 #include "../../include/harmonica_gb300.h"
+#include "lean_math.cuh"
 
 namespace hg {
 
@@ -58,14 +64,17 @@ enum Row : int {
   kCosC,      // cos / sin of the centre latitude
   kSinC,
   kRC,        // centre radius
-  kFarLon,    // ratio * size * (1 + 2^-40) when size > 0, else +inf
-  kFarLat,
-  kFarRad,
+  kCosLonC,   // cos / sin of the centre longitude
+  kSinLonC,
+  kFar2Lon,   // (ratio * size * (1 + 2^-40))^2 when size > 0, else +inf
+  kFar2Lat,
+  kFar2Rad,
   kLLon,      // sizes (_tesseroid_dimensions)
   kLLat,
   kLRad,
-  kNodeLon,   // 2 rows: node longitudes (radians), i = 0, 1
-  kNodeCos = kNodeLon + 2,  // 2 rows: cos of node latitudes, j = 0, 1
+  kNodeCosLon,                    // 2 rows: cos of node longitudes, i = 0, 1
+  kNodeSinLon = kNodeCosLon + 2,  // 2 rows: sin of node longitudes
+  kNodeCos = kNodeSinLon + 2,     // 2 rows: cos of node latitudes, j = 0, 1
   kNodeSin = kNodeCos + 2,  // 2 rows: sin of node latitudes
   kNodeRad = kNodeSin + 2,  // 2 rows: node radii, k = 0, 1
   kMass = kNodeRad + 2,     // 8 rows: masses, index (j * 2 + k) * 2 + i
@@ -92,6 +101,8 @@ struct Station {
   double cphi;  // cos / sin of the latitude
   double sphi;
   double r;
+  double clon;  // cos / sin of the longitude
+  double slon;
 };
 
 __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
@@ -204,11 +215,54 @@ __device__ __forceinline__ double glq_eval(const Station& p, const double* lon_n
   return result;
 }
 
-// distance / size < ratio, exactly as the reference evaluates it; `far` is
-// the pre-test threshold (distance >= far proves the quotient >= ratio).
-__device__ __forceinline__ bool split_axis(double d, double far, double size, double ratio) {
-  if (d >= far) return false;
+// distance / size < ratio, exactly as the reference evaluates it.
+__device__ __forceinline__ bool split_axis(double d, double size, double ratio) {
   return d / size < ratio;
+}
+
+// The 8 point masses of an unsplit tesseroid at one point, rearranged for
+// the FP64 pipe: cos(lambda_p - lambda) from the cosines and sines of both
+// longitudes (cos a cos b + sin a sin b), and 1 / l from a reciprocal square
+// root (FP32 seed, two FP64 Newton steps) instead of a square root and a
+// division.  Same point masses and kernels as glq_eval; each term differs
+// from it by a few units in the last place of cos(psi) and l.
+template <int FIELD>
+__device__ __forceinline__ double glq_eval_fast(const Station& p, const double* clon_n,
+                                                const double* slon_n, const double* cphi_n,
+                                                const double* sphi_n, const double* r_n,
+                                                const double* mass) {
+  double coslambda[2];
+#pragma unroll
+  for (int i = 0; i < 2; i++) coslambda[i] = fma(clon_n[i], p.clon, slon_n[i] * p.slon);
+  const double two_r = 2.0 * p.r;
+  double result = 0.0;
+#pragma unroll
+  for (int j = 0; j < 2; j++) {
+    const double s_term = sphi_n[j] * p.sphi;
+    const double c_term = cphi_n[j] * p.cphi;
+    double cospsi[2];
+#pragma unroll
+    for (int i = 0; i < 2; i++) cospsi[i] = fma(c_term, coslambda[i], s_term);
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+      const double dr = p.r - r_n[k];
+      const double dr2 = dr * dr;
+      const double rr = two_r * r_n[k];
+#pragma unroll
+      for (int i = 0; i < 2; i++) {
+        const double inv = lean::lm_rsqrt(fma(rr, 1.0 - cospsi[i], dr2));
+        const double m = mass[(j * 2 + k) * 2 + i];
+        if (FIELD == 0) {
+          result = fma(m, inv, result);
+        } else {
+          const double delta_z = fma(-r_n[k], cospsi[i], p.r);
+          result = fma(m * delta_z, (inv * inv) * inv, result);
+        }
+      }
+    }
+  }
+  // G (and the sign of gravity_u_spherical) applied once per tesseroid
+  return FIELD == 0 ? result * kG : result * -kG;
 }
 
 // _adaptive_discretization (_tesseroid_utils.py:150-241) for one pair, each
@@ -293,7 +347,8 @@ __global__ void prepare_kernel(const double* __restrict__ aos, const double* __r
 #pragma unroll
   for (int a = 0; a < 3; a++) {
     rec[(kLLon + a) * stride + j] = l[a];
-    rec[(kFarLon + a) * stride + j] = l[a] > 0.0 ? mul(mul(ratio, l[a]), kPreTest) : INFINITY;
+    const double far = mul(mul(ratio, l[a]), kPreTest);
+    rec[(kFar2Lon + a) * stride + j] = l[a] > 0.0 ? far * far : INFINITY;
   }
   double lon_c, cos_c, sin_c, r_c;
   centre(t, lon_c, cos_c, sin_c, r_c);
@@ -301,11 +356,18 @@ __global__ void prepare_kernel(const double* __restrict__ aos, const double* __r
   rec[kCosC * stride + j] = cos_c;
   rec[kSinC * stride + j] = sin_c;
   rec[kRC * stride + j] = r_c;
+  double s_lon_c, c_lon_c;
+  sincos(lon_c, &s_lon_c, &c_lon_c);
+  rec[kCosLonC * stride + j] = c_lon_c;
+  rec[kSinLonC * stride + j] = s_lon_c;
   Nodes nd;
   glq_nodes(t, rho, q, nd);
 #pragma unroll
   for (int a = 0; a < 2; a++) {
-    rec[(kNodeLon + a) * stride + j] = nd.lon[a];
+    double s_lon, c_lon;
+    sincos(nd.lon[a], &s_lon, &c_lon);
+    rec[(kNodeCosLon + a) * stride + j] = c_lon;
+    rec[(kNodeSinLon + a) * stride + j] = s_lon;
     rec[(kNodeCos + a) * stride + j] = nd.cphi[a];
     rec[(kNodeSin + a) * stride + j] = nd.sphi[a];
     rec[(kNodeRad + a) * stride + j] = nd.r[a];
@@ -331,6 +393,8 @@ __device__ __forceinline__ void flush_near(const uint32_t* list, int count, int 
     s.cphi = __shfl_sync(0xffffffffu, mine.cphi, owner);
     s.sphi = __shfl_sync(0xffffffffu, mine.sphi, owner);
     s.r = __shfl_sync(0xffffffffu, mine.r, owner);
+    s.clon = __shfl_sync(0xffffffffu, mine.clon, owner);
+    s.slon = __shfl_sync(0xffffffffu, mine.slon, owner);
     double contrib = 0.0;
     if (has) {
       const int64_t j = p0 + (int64_t)(ent >> 5);
@@ -344,7 +408,7 @@ __device__ __forceinline__ void flush_near(const uint32_t* list, int count, int 
     for (int k = 0; k < n; k++) {
       const double v = __shfl_sync(0xffffffffu, contrib, k);
       const int o = __shfl_sync(0xffffffffu, owner, k);
-      if (lane == o) acc = add(acc, v);
+      if (lane == o) acc += v;
     }
   }
   __syncwarp();
@@ -366,6 +430,7 @@ __global__ void __launch_bounds__(kThreads) forward_kernel(
   Station p;
   p.lon = rad(active ? lon_deg[i] : 0.0);
   sincos(rad(active ? lat_deg[i] : 0.0), &p.sphi, &p.cphi);
+  sincos(p.lon, &p.slon, &p.clon);
   p.r = active ? radius[i] : 1.0;
   const bool rad_split = ad.radial != 0;
   const double ratio = ad.ratio;
@@ -387,22 +452,36 @@ __global__ void __launch_bounds__(kThreads) forward_kernel(
       if (sh[kSkip - kLonC][c] != 0.0) continue;  // same for the whole block
       bool near = false;
       if (active) {
-        double cospsi;
-        const double d = distance_core(p, sh[kLonC - kLonC][c], sh[kCosC - kLonC][c],
-                                       sh[kSinC - kLonC][c], sh[kRC - kLonC][c], cospsi);
-        near = split_axis(d, sh[kFarLon - kLonC][c], sh[kLLon - kLonC][c], ratio) ||
-               split_axis(d, sh[kFarLat - kLonC][c], sh[kLLat - kLonC][c], ratio) ||
-               (rad_split && split_axis(d, sh[kFarRad - kLonC][c], sh[kLRad - kLonC][c], ratio));
+#define S(row) sh[(row) - kLonC][c]
+        // squared distance to the centre from the longitude cosines/sines; it
+        // differs from the reference's by at most `slack`, so d2 - slack >=
+        // far^2 proves distance / size >= ratio on that axis
+        const double r_c = S(kRC);
+        const double clam = fma(S(kCosLonC), p.clon, S(kSinLonC) * p.slon);
+        const double cospsi_c = fma(S(kCosC) * p.cphi, clam, S(kSinC) * p.sphi);
+        const double dr_c = p.r - r_c;
+        const double rr_c = 2.0 * p.r * r_c;
+        const double d2 = fma(rr_c, 1.0 - cospsi_c, dr_c * dr_c);
+        const double lo = d2 - fma(fabs(rr_c), 4e-15, d2 * 4e-15);
+        if (!(lo >= S(kFar2Lon)) || !(lo >= S(kFar2Lat)) || (rad_split && !(lo >= S(kFar2Rad)))) {
+          // undecided: the reference's distance and quotients
+          double cospsi;
+          const double d = distance_core(p, S(kLonC), S(kCosC), S(kSinC), r_c, cospsi);
+          near = split_axis(d, S(kLLon), ratio) || split_axis(d, S(kLLat), ratio) ||
+                 (rad_split && split_axis(d, S(kLRad), ratio));
+        }
         if (!near) {
-          const double lon_n[2] = {sh[kNodeLon - kLonC][c], sh[kNodeLon + 1 - kLonC][c]};
-          const double cphi_n[2] = {sh[kNodeCos - kLonC][c], sh[kNodeCos + 1 - kLonC][c]};
-          const double sphi_n[2] = {sh[kNodeSin - kLonC][c], sh[kNodeSin + 1 - kLonC][c]};
-          const double r_n[2] = {sh[kNodeRad - kLonC][c], sh[kNodeRad + 1 - kLonC][c]};
+          const double clon_n[2] = {S(kNodeCosLon), S(kNodeCosLon + 1)};
+          const double slon_n[2] = {S(kNodeSinLon), S(kNodeSinLon + 1)};
+          const double cphi_n[2] = {S(kNodeCos), S(kNodeCos + 1)};
+          const double sphi_n[2] = {S(kNodeSin), S(kNodeSin + 1)};
+          const double r_n[2] = {S(kNodeRad), S(kNodeRad + 1)};
           double mass[8];
 #pragma unroll
-          for (int a = 0; a < 8; a++) mass[a] = sh[kMass + a - kLonC][c];
-          acc = add(acc, glq_eval<FIELD>(p, lon_n, cphi_n, sphi_n, r_n, mass));
+          for (int a = 0; a < 8; a++) mass[a] = S(kMass + a);
+          acc += glq_eval_fast<FIELD>(p, clon_n, slon_n, cphi_n, sphi_n, r_n, mass);
         }
+#undef S
       }
       const unsigned ball = __ballot_sync(0xffffffffu, near);
       if (ball) {

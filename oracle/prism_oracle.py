@@ -106,6 +106,8 @@ def _load():
     lib.oracle_adaptive_discretization.argtypes = [
         dp, dp, ctypes.c_double, ctypes.c_int, ctypes.c_int, i64, dp, i64
     ]
+    lib.oracle_set_trig_perturbation.restype = None
+    lib.oracle_set_trig_perturbation.argtypes = [ctypes.c_int]
     lib.oracle_tesseroid_gravity.restype = ctypes.c_int
     lib.oracle_tesseroid_gravity.argtypes = [
         ctypes.c_int, ctypes.c_int, i64, dp, dp, dp, i64, dp, dp, dp, dp, dp, ctypes.c_int

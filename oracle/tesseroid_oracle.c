@@ -27,6 +27,7 @@
  */
 #include <math.h>
 #include <stdint.h>
+#include <string.h>
 
 #define TESS_STACK_SIZE 100
 #define TESS_MAX_DISCRETIZATIONS 100000
@@ -39,6 +40,31 @@ static const double G_CONST = 6.6743e-11;
 
 static const double PI_ = 3.141592653589793238462643383279502884;
 
+/*
+ * Conditioning probe (tests only).  When set nonzero, every cos, sin and acos
+ * result of this file is moved by -1, 0 or +1 ulp, chosen by a hash of its
+ * argument: the size of the change in the result measures how much the
+ * reference's own output depends on the last bit of its libm.  Zero (the
+ * default) leaves the functions untouched.
+ */
+static int trig_perturbation = 0;
+
+void oracle_set_trig_perturbation(int on) { trig_perturbation = on; }
+
+static double nudge(double v, double arg, uint64_t salt)
+{
+    if (!trig_perturbation) return v;
+    uint64_t u;
+    memcpy(&u, &arg, sizeof u);
+    u = (u ^ salt) * 0x9E3779B97F4A7C15ull;
+    const int step = (int)((u >> 61) % 3) - 1;
+    return step == 0 ? v : nextafter(v, step > 0 ? INFINITY : -INFINITY);
+}
+
+static double t_cos(double x) { return nudge(cos(x), x, 1); }
+static double t_sin(double x) { return nudge(sin(x), x, 2); }
+static double t_acos(double x) { return nudge(acos(x), x, 3); }
+
 static double radians(double deg) { return deg * (PI_ / 180.0); }
 
 /* distance_spherical_core (utils.py:164-201): distance and cos(psi). */
@@ -46,7 +72,7 @@ static double distance_core(double longitude, double cosphi, double sinphi, doub
                             double longitude_p, double cosphi_p, double sinphi_p,
                             double radius_p, double *cospsi_out)
 {
-    const double coslambda = cos(longitude_p - longitude);
+    const double coslambda = t_cos(longitude_p - longitude);
     const double cospsi = sinphi_p * sinphi + cosphi_p * cosphi * coslambda;
     const double dr = radius - radius_p;
     if (cospsi_out) *cospsi_out = cospsi;
@@ -74,9 +100,9 @@ void oracle_tesseroid_dimensions(const double *t, double *out3)
     const double s = radians(t[2]), n = radians(t[3]);
     const double top = t[5];
     const double latc = (n + s) / 2;
-    const double l_lat = top * acos(sin(n) * sin(s) + cos(n) * cos(s));
-    const double sl = sin(latc), cl = cos(latc);
-    const double l_lon = top * acos(sl * sl + cl * cl * cos(e - w));
+    const double l_lat = top * t_acos(t_sin(n) * t_sin(s) + t_cos(n) * t_cos(s));
+    const double sl = t_sin(latc), cl = t_cos(latc);
+    const double l_lon = top * t_acos(sl * sl + cl * cl * t_cos(e - w));
     out3[0] = l_lon;
     out3[1] = l_lat;
     out3[2] = top - t[4];
@@ -91,8 +117,8 @@ double oracle_distance_tesseroid_point(double longitude, double latitude, double
     const double lat_p = radians((t[2] + t[3]) / 2);
     const double r_p = (t[4] + t[5]) / 2;
     const double lat = radians(latitude);
-    return distance_core(radians(longitude), cos(lat), sin(lat), radius, lon_p, cos(lat_p),
-                         sin(lat_p), r_p, 0);
+    return distance_core(radians(longitude), t_cos(lat), t_sin(lat), radius, lon_p, t_cos(lat_p),
+                         t_sin(lat_p), r_p, 0);
 }
 
 /* gauss_legendre_quadrature (_tesseroid_utils.py:18-115).  nodes/weights:
@@ -106,8 +132,8 @@ double oracle_tesseroid_glq(int field, double longitude_rad, double cosphi, doub
     double result = 0.0;
     for (int j = 0; j < 2; j++) {
         const double latitude_p = radians(0.5 * (n - s) * nodes[2 + j] + 0.5 * (n + s));
-        const double cosphi_p = cos(latitude_p);
-        const double sinphi_p = sin(latitude_p);
+        const double cosphi_p = t_cos(latitude_p);
+        const double sinphi_p = t_sin(latitude_p);
         for (int k = 0; k < 2; k++) {
             const double radius_p = 0.5 * (top - bottom) * nodes[4 + k] + 0.5 * (top + bottom);
             const double kappa = radius_p * radius_p * cosphi_p;
@@ -243,7 +269,7 @@ int oracle_tesseroid_gravity(int field, int radial, int64_t n_obs, const double 
     for (int64_t i = 0; i < n_obs; i++) {
         const double point[3] = {longitude[i], latitude[i], radius[i]};
         const double lat = radians(latitude[i]);
-        glq_ctx g = {field, radians(longitude[i]), cos(lat), sin(lat), radius[i], 0.0,
+        glq_ctx g = {field, radians(longitude[i]), t_cos(lat), t_sin(lat), radius[i], 0.0,
                      nodes, weights, 0.0};
         double acc = 0.0;
         for (int64_t j = 0; j < n_tess; j++) {

@@ -98,8 +98,10 @@ def adaptive_discretization(point, tesseroid, distance_size_ratio, radial_discre
 
 def tesseroid_gravity(coordinates, tesseroids, density, field,
                       radial_adaptive_discretization=False, disable_checks=False,
-                      parallel=True):
-    """Reference result (potential J/kg, g_z mGal) for constant densities."""
+                      parallel=True, trig_perturbation=False):
+    """Reference result (potential J/kg, g_z mGal) for constant densities.
+    ``trig_perturbation`` moves every cos/sin/acos by -1, 0 or +1 ulp (a
+    conditioning probe: how much the result depends on the libm)."""
     if field not in FIELD_CODES:
         msg = f"Gravitational field {field} not recognized"
         raise ValueError(msg)
@@ -113,11 +115,16 @@ def tesseroid_gravity(coordinates, tesseroids, density, field,
     tess, rho = _f64(tess), _f64(rho)
     nodes, weights = glq_nodes_weights()
     result = np.zeros(lon.size)
-    rc = _load().oracle_tesseroid_gravity(
-        FIELD_CODES[field], int(radial_adaptive_discretization), lon.size, _ptr(lon),
-        _ptr(lat), _ptr(rad), tess.shape[0], _ptr(tess), _ptr(rho), _ptr(nodes),
-        _ptr(weights), _ptr(result), int(parallel),
-    )
+    lib = _load()
+    lib.oracle_set_trig_perturbation(int(bool(trig_perturbation)))
+    try:
+        rc = lib.oracle_tesseroid_gravity(
+            FIELD_CODES[field], int(radial_adaptive_discretization), lon.size, _ptr(lon),
+            _ptr(lat), _ptr(rad), tess.shape[0], _ptr(tess), _ptr(rho), _ptr(nodes),
+            _ptr(weights), _ptr(result), int(parallel),
+        )
+    finally:
+        lib.oracle_set_trig_perturbation(0)
     if rc == 1:
         raise OverflowError("Stack Overflow. Try to increase the stack size.")
     if rc == 2:

@@ -128,6 +128,32 @@ def test_oracle_spherical_shell_2d(field):
         npt.assert_allclose(got, expected, rtol=ACCURACY_THRESHOLD)
 
 
+def test_oracle_libm_sensitivity():
+    """How much the reference's own result depends on the last bit of its
+    libm (every cos/sin/acos moved by -1, 0 or +1 ulp): ~1e-13 far above the
+    model, below 1e-8 at 1 km, up to ~1e-3 for points on the face of a 10 m
+    shell.  These bound the agreement any other libm (the GPU's) can have
+    with the reference; the GPU tests use them as tolerances."""
+    def sensitivity(coords, tess, dens, field, radial=False):
+        a = to.tesseroid_gravity(coords, tess, dens, field, radial_adaptive_discretization=radial)
+        b = to.tesseroid_gravity(coords, tess, dens, field, radial_adaptive_discretization=radial,
+                                 trig_perturbation=True)
+        return np.max(np.abs(b / a - 1))
+
+    g = _golden()
+    far = sensitivity(tuple(g["gallery_g_z_coords"]), g["gallery_g_z_tesseroids"],
+                      g["gallery_g_z_density"], "g_z")
+    assert far < 1e-11
+    near = sensitivity([0, 0, MEAN_RADIUS + 1e3], shell((6, 6), MEAN_RADIUS - 1e3, MEAN_RADIUS),
+                       np.full(36, 1000.0), "g_z", radial=True)
+    assert near < 1e-8
+    lon, lat = np.meshgrid(np.arange(0, 351, 10.0), np.arange(-90, 91, 10.0))
+    surface = sensitivity((lon, lat, np.full(lon.shape, MEAN_RADIUS)),
+                          shell((12, 6), MEAN_RADIUS - 10.0, MEAN_RADIUS),
+                          np.full(72, 1000.0), "g_z")
+    assert 1e-5 < surface < ACCURACY_THRESHOLD
+
+
 # ------------------------------------------------------------ host logic
 def test_glq_nodes_weights():
     nodes, weights = ht.glq_nodes_weights((2, 2, 2))
