@@ -587,8 +587,8 @@ def run_magnetic(args, rank, world, local):
 
 # FP64 thread-instructions per tesseroid pair of the tesseroid forward kernel on the
 # Andes layer: ncu sm__sass_thread_inst_executed_op_fp64_pred_on.sum of one launch
-# (5.119e10) over its 3825 x 93121 pairs (profiles/tesseroid_forward_andes.md).
-FP64_INST_PER_TESS_PAIR = 143.7
+# (9.81e8) over its 3825 x 93121 pairs (profiles/tesseroid_forward_andes.md).
+FP64_INST_PER_TESS_PAIR = 2.75
 
 
 def run_tesseroids(args, rank, world, local):

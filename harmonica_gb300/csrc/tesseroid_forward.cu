@@ -18,17 +18,20 @@
 // expensive pairs instead of idling behind one of them.  Queued pairs are
 // added to their point's sum in list order: results are deterministic.
 //
-// Arithmetic.  FP64 throughout.  The split decisions and every small
-// tesseroid of a split pair follow the reference's operation order without
-// contraction into fused multiply-adds (__dmul_rn / __dadd_rn), so they
-// differ from the reference only through the last bits of cos/sin/acos.  The
-// split test distance / size < ratio is evaluated exactly whenever it is not
-// settled by a pre-test on the squared distance with a rigorous error margin
-// (distance >= ratio * size * (1 + 2^-40) proves "no split").  Unsplit
-// tesseroids -- nearly all pairs -- are summed by glq_eval_fast: the same 8
-// point masses with cos(lambda_p - lambda) from precomputed cosines and sines
-// and 1 / l from a reciprocal square root, within a few units in the last
-// place of the reference's terms at about half the FP64 instructions.
+// Arithmetic.  The split decisions and every small tesseroid of a split pair
+// are FP64 in the reference's operation order without contraction into fused
+// multiply-adds (__dmul_rn / __dadd_rn), so they differ from the reference
+// only through the last bits of cos/sin/acos.  The split test
+// distance / size < ratio is evaluated exactly whenever an FP32 pre-test on
+// the Cartesian distance to the centre, with a rigorous error margin, does
+// not already prove "no split".  Unsplit tesseroids -- nearly all pairs --
+// are summed by glq_eval_pairs on float pairs packed two nodes per float2
+// (FFMA2/FADD2/FMUL2): the Cartesian difference of the point and each node
+// (48-bit coordinates), 1 / l from a float-pair reciprocal square root, and
+// for g_z the radial component P . (P - Q) / r, which avoids the
+// 1 - cos(psi) cancellation of the reference's formula; the pair's sum
+// returns to FP64 for the accumulation.  The FP64 pipe, 1/64 of the FP32
+// rate on this GPU, then does almost nothing on the common path.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -36,7 +39,7 @@
 #include <string>
 
 #include "../../include/harmonica_gb300.h"
-#include "lean_math.cuh"
+#include "lean_packed.cuh"
 
 namespace hg {
 
@@ -64,22 +67,19 @@ enum Row : int {
   kCosC,      // cos / sin of the centre latitude
   kSinC,
   kRC,        // centre radius
-  kCosLonC,   // cos / sin of the centre longitude
-  kSinLonC,
-  kFar2Lon,   // (ratio * size * (1 + 2^-40))^2 when size > 0, else +inf
-  kFar2Lat,
-  kFar2Rad,
   kLLon,      // sizes (_tesseroid_dimensions)
   kLLat,
   kLRad,
-  kNodeCosLon,                    // 2 rows: cos of node longitudes, i = 0, 1
-  kNodeSinLon = kNodeCosLon + 2,  // 2 rows: sin of node longitudes
-  kNodeCos = kNodeSinLon + 2,     // 2 rows: cos of node latitudes, j = 0, 1
-  kNodeSin = kNodeCos + 2,  // 2 rows: sin of node latitudes
-  kNodeRad = kNodeSin + 2,  // 2 rows: node radii, k = 0, 1
-  kMass = kNodeRad + 2,     // 8 rows: masses, index (j * 2 + k) * 2 + i
-  kSkip = kMass + 8,        // 1: null tesseroid (zero size or density)
-  kRows
+  kSkip,      // 1: null tesseroid (zero size or density)
+  // float2 rows (two floats in one 8-byte slot):
+  kCentreXY,  // centre, Earth-centred Cartesian, FP32: (x, y)
+  kCentreZ,   // (z, far_lon)
+  kFar,       // (far_lat, far_rad): far = ratio * size * (1 + 2^-40) rounded up, +inf
+              // when the size is not > 0
+  kNodes,     // 24 rows: node (j, k) = jk, coordinate c: row kNodes + (jk * 3 + c) * 2
+              // holds the high floats of nodes i = 0, 1, the next row the low floats
+  kMasses = kNodes + 24,  // 8 rows: masses of nodes (jk, i = 0, 1), high then low floats
+  kRows = kMasses + 8
 };
 constexpr int kSmemRows = kRows - kLonC;
 
@@ -101,8 +101,16 @@ struct Station {
   double cphi;  // cos / sin of the latitude
   double sphi;
   double r;
-  double clon;  // cos / sin of the longitude
-  double slon;
+};
+
+using lean::F2;
+using lean::P2;
+
+// The point in Earth-centred Cartesian coordinates as float pairs, and 1 / r.
+struct StationXYZ {
+  F2 x, y, z;
+  F2 inv_r;
+  float r_f;
 };
 
 __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
@@ -220,49 +228,58 @@ __device__ __forceinline__ bool split_axis(double d, double size, double ratio) 
   return d / size < ratio;
 }
 
-// The 8 point masses of an unsplit tesseroid at one point, rearranged for
-// the FP64 pipe: cos(lambda_p - lambda) from the cosines and sines of both
-// longitudes (cos a cos b + sin a sin b), and 1 / l from a reciprocal square
-// root (FP32 seed, two FP64 Newton steps) instead of a square root and a
-// division.  Same point masses and kernels as glq_eval; each term differs
-// from it by a few units in the last place of cos(psi) and l.
+// 1 / sqrt(x) lane by lane for x > 0 normal: FP32 seed, one Newton step with
+// its second-order term, the residual 1 - x y^2 on float pairs.
+__device__ __forceinline__ P2 p2_rsqrt(P2 x) {
+  using namespace lean;
+  const float2 y = mk2(rsqrt_approx(x.h.x), rsqrt_approx(x.h.y));
+  const P2 xy2 = p2_mul(x, two_prod2(y, y));
+  const float2 r = sub2(sub2(sp2(1.0f), xy2.h), xy2.l);
+  const float2 c = mul2(r, fma2(sp2(0.375f), r, sp2(0.5f)));
+  return P2{y, mul2(y, c)};
+}
+
+__device__ __forceinline__ P2 p2_of(const double* row_h, const double* row_l) {
+  return P2{*reinterpret_cast<const float2*>(row_h), *reinterpret_cast<const float2*>(row_l)};
+}
+
+// The 8 point masses of an unsplit tesseroid at one point, on float pairs two
+// nodes at a time (the lanes hold the nodes of the two longitudes):
+// distance from the Cartesian difference P - Q (no 1 - cos(psi)
+// cancellation), 1 / l by p2_rsqrt, and for g_z the radial component
+// r - r_p cos(psi) = P . (P - Q) / r.  The same point masses and kernels as
+// glq_eval; each term within a few units of 2^-46 of its exact value (the
+// reference's own terms carry the rounding of 1 - cos(psi), which is
+// larger).  `col` is the tesseroid's column in the shared-memory rows.
 template <int FIELD>
-__device__ __forceinline__ double glq_eval_fast(const Station& p, const double* clon_n,
-                                                const double* slon_n, const double* cphi_n,
-                                                const double* sphi_n, const double* r_n,
-                                                const double* mass) {
-  double coslambda[2];
-#pragma unroll
-  for (int i = 0; i < 2; i++) coslambda[i] = fma(clon_n[i], p.clon, slon_n[i] * p.slon);
-  const double two_r = 2.0 * p.r;
-  double result = 0.0;
-#pragma unroll
-  for (int j = 0; j < 2; j++) {
-    const double s_term = sphi_n[j] * p.sphi;
-    const double c_term = cphi_n[j] * p.cphi;
-    double cospsi[2];
-#pragma unroll
-    for (int i = 0; i < 2; i++) cospsi[i] = fma(c_term, coslambda[i], s_term);
-#pragma unroll
-    for (int k = 0; k < 2; k++) {
-      const double dr = p.r - r_n[k];
-      const double dr2 = dr * dr;
-      const double rr = two_r * r_n[k];
-#pragma unroll
-      for (int i = 0; i < 2; i++) {
-        const double inv = lean::lm_rsqrt(fma(rr, 1.0 - cospsi[i], dr2));
-        const double m = mass[(j * 2 + k) * 2 + i];
-        if (FIELD == 0) {
-          result = fma(m, inv, result);
-        } else {
-          const double delta_z = fma(-r_n[k], cospsi[i], p.r);
-          result = fma(m * delta_z, (inv * inv) * inv, result);
-        }
-      }
+__device__ __forceinline__ double glq_eval_pairs(const StationXYZ& q, const double (*rows)[kTile],
+                                                 int col) {
+  using namespace lean;
+  const P2 px{sp2(q.x.h), sp2(q.x.l)}, py{sp2(q.y.h), sp2(q.y.l)}, pz{sp2(q.z.h), sp2(q.z.l)};
+  P2 sum{sp2(0.0f), sp2(0.0f)};
+#pragma unroll 1
+  for (int jk = 0; jk < 4; jk++) {
+    const int r0 = kNodes - kLonC + jk * 6;
+    const P2 dx = p2_sub(px, p2_of(&rows[r0][col], &rows[r0 + 1][col]));
+    const P2 dy = p2_sub(py, p2_of(&rows[r0 + 2][col], &rows[r0 + 3][col]));
+    const P2 dz = p2_sub(pz, p2_of(&rows[r0 + 4][col], &rows[r0 + 5][col]));
+    const P2 l2 = p2_add(p2_add(p2_sq(dx), p2_sq(dy)), p2_sq(dz));
+    const P2 inv = p2_rsqrt(l2);
+    const int rm = kMasses - kLonC + jk * 2;
+    const P2 m = p2_of(&rows[rm][col], &rows[rm + 1][col]);
+    P2 term;
+    if (FIELD == 0) {
+      term = p2_mul(m, inv);
+    } else {
+      const P2 pd = p2_add(p2_add(p2_mul(px, dx), p2_mul(py, dy)), p2_mul(pz, dz));
+      term = p2_mul(p2_mul(m, pd), p2_mul(p2_mul(inv, inv), inv));
     }
+    sum = p2_add(sum, term);
   }
-  // G (and the sign of gravity_u_spherical) applied once per tesseroid
-  return FIELD == 0 ? result * kG : result * -kG;
+  F2 s = f2_add(lane0(sum), lane1(sum));
+  if (FIELD != 0) s = f2_mul(s, q.inv_r);
+  // G (and the sign of gravity_u_spherical) once per tesseroid
+  return f2_to_double(s, 0) * (FIELD == 0 ? kG : -kG);
 }
 
 // _adaptive_discretization (_tesseroid_utils.py:150-241) for one pair, each
@@ -339,41 +356,62 @@ __global__ void prepare_kernel(const double* __restrict__ aos, const double* __r
 #pragma unroll
   for (int c = 0; c < 6; c++) rec[c * stride + j] = t[c];
   rec[kRho * stride + j] = rho;
-  // _discard_null_tesseroids (_tesseroid_utils.py:503-538)
+  // _discard_null_tesseroids (_tesseroid_utils.py:503-538); a tesseroid with a
+  // NaN or infinite bound or density that is not null makes the reference's
+  // result NaN: flag 2
   const bool null = t[0] == t[1] || t[2] == t[3] || t[4] == t[5] || rho == 0.0;
-  rec[kSkip * stride + j] = null ? 1.0 : 0.0;
+  bool finite = isfinite(rho);
+#pragma unroll
+  for (int c = 0; c < 6; c++) finite = finite && isfinite(t[c]);
+  rec[kSkip * stride + j] = null ? 1.0 : (finite ? 0.0 : 2.0);
   double l[3];
   dimensions(t, l[0], l[1], l[2]);
-#pragma unroll
-  for (int a = 0; a < 3; a++) {
-    rec[(kLLon + a) * stride + j] = l[a];
-    const double far = mul(mul(ratio, l[a]), kPreTest);
-    rec[(kFar2Lon + a) * stride + j] = l[a] > 0.0 ? far * far : INFINITY;
-  }
   double lon_c, cos_c, sin_c, r_c;
   centre(t, lon_c, cos_c, sin_c, r_c);
   rec[kLonC * stride + j] = lon_c;
   rec[kCosC * stride + j] = cos_c;
   rec[kSinC * stride + j] = sin_c;
   rec[kRC * stride + j] = r_c;
+  float far[3];
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    rec[(kLLon + a) * stride + j] = l[a];
+    far[a] = l[a] > 0.0 ? __double2float_ru(mul(mul(ratio, l[a]), kPreTest)) : INFINITY;
+  }
   double s_lon_c, c_lon_c;
   sincos(lon_c, &s_lon_c, &c_lon_c);
-  rec[kCosLonC * stride + j] = c_lon_c;
-  rec[kSinLonC * stride + j] = s_lon_c;
+  const double rcc = r_c * cos_c;
+  float2* f2row = reinterpret_cast<float2*>(rec);
+  f2row[kCentreXY * stride + j] = make_float2((float)(rcc * c_lon_c), (float)(rcc * s_lon_c));
+  f2row[kCentreZ * stride + j] = make_float2((float)(r_c * sin_c), far[0]);
+  f2row[kFar * stride + j] = make_float2(far[1], far[2]);
   Nodes nd;
   glq_nodes(t, rho, q, nd);
+  double c_lon[2], s_lon[2];
 #pragma unroll
-  for (int a = 0; a < 2; a++) {
-    double s_lon, c_lon;
-    sincos(nd.lon[a], &s_lon, &c_lon);
-    rec[(kNodeCosLon + a) * stride + j] = c_lon;
-    rec[(kNodeSinLon + a) * stride + j] = s_lon;
-    rec[(kNodeCos + a) * stride + j] = nd.cphi[a];
-    rec[(kNodeSin + a) * stride + j] = nd.sphi[a];
-    rec[(kNodeRad + a) * stride + j] = nd.r[a];
-  }
+  for (int i = 0; i < 2; i++) sincos(nd.lon[i], &s_lon[i], &c_lon[i]);
 #pragma unroll
-  for (int a = 0; a < 8; a++) rec[(kMass + a) * stride + j] = nd.mass[a];
+  for (int jj = 0; jj < 2; jj++)
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+      const int jk = jj * 2 + k;
+      const double rc = nd.r[k] * nd.cphi[jj];
+      lean::F2 xyz[3][2], m[2];
+#pragma unroll
+      for (int i = 0; i < 2; i++) {
+        xyz[0][i] = lean::double_to_f2(rc * c_lon[i]);
+        xyz[1][i] = lean::double_to_f2(rc * s_lon[i]);
+        xyz[2][i] = lean::double_to_f2(nd.r[k] * nd.sphi[jj]);
+        m[i] = lean::double_to_f2(nd.mass[jk * 2 + i]);
+      }
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        f2row[(kNodes + (jk * 3 + c) * 2) * stride + j] = make_float2(xyz[c][0].h, xyz[c][1].h);
+        f2row[(kNodes + (jk * 3 + c) * 2 + 1) * stride + j] = make_float2(xyz[c][0].l, xyz[c][1].l);
+      }
+      f2row[(kMasses + jk * 2) * stride + j] = make_float2(m[0].h, m[1].h);
+      f2row[(kMasses + jk * 2 + 1) * stride + j] = make_float2(m[0].l, m[1].l);
+    }
 }
 
 // Run the queued split pairs of this warp, 32 at a time (one per lane), and
@@ -393,8 +431,6 @@ __device__ __forceinline__ void flush_near(const uint32_t* list, int count, int 
     s.cphi = __shfl_sync(0xffffffffu, mine.cphi, owner);
     s.sphi = __shfl_sync(0xffffffffu, mine.sphi, owner);
     s.r = __shfl_sync(0xffffffffu, mine.r, owner);
-    s.clon = __shfl_sync(0xffffffffu, mine.clon, owner);
-    s.slon = __shfl_sync(0xffffffffu, mine.slon, owner);
     double contrib = 0.0;
     if (has) {
       const int64_t j = p0 + (int64_t)(ent >> 5);
@@ -430,8 +466,18 @@ __global__ void __launch_bounds__(kThreads) forward_kernel(
   Station p;
   p.lon = rad(active ? lon_deg[i] : 0.0);
   sincos(rad(active ? lat_deg[i] : 0.0), &p.sphi, &p.cphi);
-  sincos(p.lon, &p.slon, &p.clon);
   p.r = active ? radius[i] : 1.0;
+  StationXYZ q3;
+  {
+    double slon, clon;
+    sincos(p.lon, &slon, &clon);
+    const double rc = p.r * p.cphi;
+    q3.x = lean::double_to_f2(rc * clon);
+    q3.y = lean::double_to_f2(rc * slon);
+    q3.z = lean::double_to_f2(p.r * p.sphi);
+    q3.inv_r = lean::double_to_f2(1.0 / p.r);
+    q3.r_f = (float)p.r;
+  }
   const bool rad_split = ad.radial != 0;
   const double ratio = ad.ratio;
 
@@ -449,38 +495,36 @@ __global__ void __launch_bounds__(kThreads) forward_kernel(
     }
     __syncthreads();
     for (int c = 0; c < cnt; c++) {
-      if (sh[kSkip - kLonC][c] != 0.0) continue;  // same for the whole block
+      const double skip = sh[kSkip - kLonC][c];  // same for the whole block
+      if (skip != 0.0) {
+        if (skip == 2.0) acc += NAN;
+        continue;
+      }
       bool near = false;
       if (active) {
 #define S(row) sh[(row) - kLonC][c]
-        // squared distance to the centre from the longitude cosines/sines; it
-        // differs from the reference's by at most `slack`, so d2 - slack >=
-        // far^2 proves distance / size >= ratio on that axis
-        const double r_c = S(kRC);
-        const double clam = fma(S(kCosLonC), p.clon, S(kSinLonC) * p.slon);
-        const double cospsi_c = fma(S(kCosC) * p.cphi, clam, S(kSinC) * p.sphi);
-        const double dr_c = p.r - r_c;
-        const double rr_c = 2.0 * p.r * r_c;
-        const double d2 = fma(rr_c, 1.0 - cospsi_c, dr_c * dr_c);
-        const double lo = d2 - fma(fabs(rr_c), 4e-15, d2 * 4e-15);
-        if (!(lo >= S(kFar2Lon)) || !(lo >= S(kFar2Lat)) || (rad_split && !(lo >= S(kFar2Rad)))) {
+#define F(row) (*reinterpret_cast<const float2*>(&sh[(row) - kLonC][c]))
+        // FP32 distance to the centre in Cartesian coordinates.  Its error
+        // against the reference's distance is below 2^-22 (r + r_c) from the
+        // coordinates' rounding, ~0.1 m from the reference's own rounding at
+        // d >= 1 m and 2^-21 relative from the arithmetic, so
+        // d2 (1 - 2^-19) >= (far + 2^-21 (r + r_c) + 1 m)^2 proves
+        // distance / size >= ratio on that axis.
+        const float2 cxy = F(kCentreXY), cz = F(kCentreZ), fl = F(kFar);
+        const float ddx = q3.x.h - cxy.x, ddy = q3.y.h - cxy.y, ddz = q3.z.h - cz.x;
+        const float d2 = fmaf(ddx, ddx, fmaf(ddy, ddy, ddz * ddz)) * (1.0f - 0x1p-19f);
+        const float slack = fmaf(0x1p-21f, q3.r_f + (float)S(kRC), 1.0f);
+        const float t_lon = cz.y + slack, t_lat = fl.x + slack, t_rad = fl.y + slack;
+        if (!(d2 >= t_lon * t_lon) || !(d2 >= t_lat * t_lat) ||
+            (rad_split && !(d2 >= t_rad * t_rad))) {
           // undecided: the reference's distance and quotients
           double cospsi;
-          const double d = distance_core(p, S(kLonC), S(kCosC), S(kSinC), r_c, cospsi);
+          const double d = distance_core(p, S(kLonC), S(kCosC), S(kSinC), S(kRC), cospsi);
           near = split_axis(d, S(kLLon), ratio) || split_axis(d, S(kLLat), ratio) ||
                  (rad_split && split_axis(d, S(kLRad), ratio));
         }
-        if (!near) {
-          const double clon_n[2] = {S(kNodeCosLon), S(kNodeCosLon + 1)};
-          const double slon_n[2] = {S(kNodeSinLon), S(kNodeSinLon + 1)};
-          const double cphi_n[2] = {S(kNodeCos), S(kNodeCos + 1)};
-          const double sphi_n[2] = {S(kNodeSin), S(kNodeSin + 1)};
-          const double r_n[2] = {S(kNodeRad), S(kNodeRad + 1)};
-          double mass[8];
-#pragma unroll
-          for (int a = 0; a < 8; a++) mass[a] = S(kMass + a);
-          acc += glq_eval_fast<FIELD>(p, clon_n, slon_n, cphi_n, sphi_n, r_n, mass);
-        }
+        if (!near) acc += glq_eval_pairs<FIELD>(q3, sh, c);
+#undef F
 #undef S
       }
       const unsigned ball = __ballot_sync(0xffffffffu, near);
