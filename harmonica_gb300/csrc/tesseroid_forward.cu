@@ -25,7 +25,7 @@
 // distance / size < ratio is evaluated exactly whenever an FP32 pre-test on
 // the Cartesian distance to the centre, with a rigorous error margin, does
 // not already prove "no split".  Unsplit tesseroids -- nearly all pairs --
-// are summed by glq_eval_pairs on float pairs packed two nodes per float2
+// are summed by glq_sum_pairs on float pairs packed two nodes per float2
 // (FFMA2/FADD2/FMUL2): the Cartesian difference of the point and each node
 // (48-bit coordinates), 1 / l from a float-pair reciprocal square root, and
 // for g_z the radial component P . (P - Q) / r, which avoids the
@@ -79,7 +79,8 @@ enum Row : int {
   kNodes,     // 24 rows: node (j, k) = jk, coordinate c: row kNodes + (jk * 3 + c) * 2
               // holds the high floats of nodes i = 0, 1, the next row the low floats
   kMasses = kNodes + 24,  // 8 rows: masses of nodes (jk, i = 0, 1), high then low floats
-  kRows = kMasses + 8
+  kNodeR = kMasses + 8,   // 2 rows: node radii (k = 0, 1), high then low floats
+  kRows = kNodeR + 2
 };
 constexpr int kSmemRows = kRows - kLonC;
 
@@ -109,7 +110,7 @@ using lean::P2;
 // The point in Earth-centred Cartesian coordinates as float pairs, and 1 / r.
 struct StationXYZ {
   F2 x, y, z;
-  F2 inv_r;
+  F2 r, inv_r;
   float r_f;
 };
 
@@ -243,43 +244,146 @@ __device__ __forceinline__ P2 p2_of(const double* row_h, const double* row_l) {
   return P2{*reinterpret_cast<const float2*>(row_h), *reinterpret_cast<const float2*>(row_l)};
 }
 
-// The 8 point masses of an unsplit tesseroid at one point, on float pairs two
+// Node sources for glq_sum_pairs: node (j, k) = jk of both longitudes as
+// float pairs (lanes i = 0, 1) -- Cartesian coordinates and masses.
+struct SmemNodes {  // prepared records staged in shared memory
+  const double (*rows)[kTile];
+  int col;
+  __device__ __forceinline__ P2 radii() const {
+    return p2_of(&rows[kNodeR - kLonC][col], &rows[kNodeR + 1 - kLonC][col]);
+  }
+  __device__ __forceinline__ void get(int jk, P2& x, P2& y, P2& z, P2& m) const {
+    const int r0 = kNodes - kLonC + jk * 6;
+    x = p2_of(&rows[r0][col], &rows[r0 + 1][col]);
+    y = p2_of(&rows[r0 + 2][col], &rows[r0 + 3][col]);
+    z = p2_of(&rows[r0 + 4][col], &rows[r0 + 5][col]);
+    const int rm = kMasses - kLonC + jk * 2;
+    m = p2_of(&rows[rm][col], &rows[rm + 1][col]);
+  }
+};
+
+struct RegNodes {  // computed per small tesseroid of a split pair (thread-local)
+  P2 x[4], y[4], z[4], m[4], r;
+  __device__ __forceinline__ P2 radii() const { return r; }
+  __device__ __forceinline__ void get(int jk, P2& xo, P2& yo, P2& zo, P2& mo) const {
+    xo = x[jk];
+    yo = y[jk];
+    zo = z[jk];
+    mo = m[jk];
+  }
+};
+
+// a - b lane by lane: the rounded difference of the high parts, its exact
+// rounding error plus the low parts, renormalised (the low parts of 6e6 m
+// coordinates are up to 0.5 m, hundreds of ulps of a 30 km difference: left
+// unnormalised, the squares below would lose their (lo)^2 terms).
+__device__ __forceinline__ P2 p2_diff(P2 a, P2 b) {
+  using namespace lean;
+  const P2 s = two_sum2(a.h, neg2(b.h));
+  return quick_two_sum2(s.h, add2(s.l, sub2(a.l, b.l)));
+}
+
+// x^2 + y^2 + z^2 lane by lane: exact squares of the high parts, their sum
+// by two-sums, every low-order term added once, one renormalisation.
+__device__ __forceinline__ P2 p2_norm2(P2 x, P2 y, P2 z) {
+  using namespace lean;
+  const P2 px = two_prod2(x.h, x.h), py = two_prod2(y.h, y.h), pz = two_prod2(z.h, z.h);
+  const P2 s = two_sum2(px.h, py.h);
+  const P2 t = two_sum2(s.h, pz.h);
+  float2 lo = add2(add2(px.l, py.l), add2(pz.l, add2(s.l, t.l)));
+  lo = fma2(x.h, add2(x.l, x.l), lo);
+  lo = fma2(y.h, add2(y.l, y.l), lo);
+  lo = fma2(z.h, add2(z.l, z.l), lo);
+  return quick_two_sum2(t.h, lo);
+}
+
+// The 8 point masses of one tesseroid at one point, on float pairs two
 // nodes at a time (the lanes hold the nodes of the two longitudes):
-// distance from the Cartesian difference P - Q (no 1 - cos(psi)
+// l^2 = |P - Q|^2 from the Cartesian difference (no 1 - cos(psi)
 // cancellation), 1 / l by p2_rsqrt, and for g_z the radial component
-// r - r_p cos(psi) = P . (P - Q) / r.  The same point masses and kernels as
-// glq_eval; each term within a few units of 2^-46 of its exact value (the
-// reference's own terms carry the rounding of 1 - cos(psi), which is
-// larger).  `col` is the tesseroid's column in the shared-memory rows.
-template <int FIELD>
-__device__ __forceinline__ double glq_eval_pairs(const StationXYZ& q, const double (*rows)[kTile],
-                                                 int col) {
+// r - r_p cos(psi) = P . (P - Q) / r = (l^2 + (r - r_p)(r + r_p)) / (2 r).
+// The same point masses and kernels as glq_eval; each term within a few
+// units of 2^-46 of its exact value (the reference's own terms carry the
+// rounding of 1 - cos(psi), which is larger).  UNROLL: loop unrolling (1
+// keeps the code small).
+template <int FIELD, int UNROLL, class Src>
+__device__ __forceinline__ double glq_sum_pairs(const StationXYZ& q, const Src& src) {
   using namespace lean;
   const P2 px{sp2(q.x.h), sp2(q.x.l)}, py{sp2(q.y.h), sp2(q.y.l)}, pz{sp2(q.z.h), sp2(q.z.l)};
+  // (r - r_k)(r + r_k) for the two node radii, lanes k = 0, 1
+  P2 rr{sp2(0.0f), sp2(0.0f)};
+  if (FIELD != 0) {
+    const P2 pr{sp2(q.r.h), sp2(q.r.l)}, rk = src.radii();
+    const P2 dif = p2_diff(pr, rk);
+    const P2 sum_r = p2_diff(pr, p2_neg(rk));
+    rr = p2_mul(dif, sum_r);
+  }
   P2 sum{sp2(0.0f), sp2(0.0f)};
-#pragma unroll 1
+#pragma unroll UNROLL
   for (int jk = 0; jk < 4; jk++) {
-    const int r0 = kNodes - kLonC + jk * 6;
-    const P2 dx = p2_sub(px, p2_of(&rows[r0][col], &rows[r0 + 1][col]));
-    const P2 dy = p2_sub(py, p2_of(&rows[r0 + 2][col], &rows[r0 + 3][col]));
-    const P2 dz = p2_sub(pz, p2_of(&rows[r0 + 4][col], &rows[r0 + 5][col]));
-    const P2 l2 = p2_add(p2_add(p2_sq(dx), p2_sq(dy)), p2_sq(dz));
+    P2 nx, ny, nz, m;
+    src.get(jk, nx, ny, nz, m);
+    const P2 l2 = p2_norm2(p2_diff(px, nx), p2_diff(py, ny), p2_diff(pz, nz));
     const P2 inv = p2_rsqrt(l2);
-    const int rm = kMasses - kLonC + jk * 2;
-    const P2 m = p2_of(&rows[rm][col], &rows[rm + 1][col]);
     P2 term;
     if (FIELD == 0) {
       term = p2_mul(m, inv);
     } else {
-      const P2 pd = p2_add(p2_add(p2_mul(px, dx), p2_mul(py, dy)), p2_mul(pz, dz));
-      term = p2_mul(p2_mul(m, pd), p2_mul(p2_mul(inv, inv), inv));
+      const int k = jk & 1;
+      const P2 rrk{sp2(k ? rr.h.y : rr.h.x), sp2(k ? rr.l.y : rr.l.x)};
+      const P2 pd2 = p2_add(l2, rrk);  // 2 r (r - r_p cos(psi))
+      term = p2_mul(p2_mul(m, pd2), p2_mul(p2_mul(inv, inv), inv));
     }
-    sum = p2_add(sum, term);
+    // running sum: two-sum of the high parts, low parts gathered unnormalised
+    const P2 t = two_sum2(sum.h, term.h);
+    sum = P2{t.h, add2(sum.l, add2(t.l, term.l))};
   }
-  F2 s = f2_add(lane0(sum), lane1(sum));
+  F2 s = f2_add(F2{sum.h.x, sum.l.x}, F2{sum.h.y, sum.l.y});
   if (FIELD != 0) s = f2_mul(s, q.inv_r);
-  // G (and the sign of gravity_u_spherical) once per tesseroid
-  return f2_to_double(s, 0) * (FIELD == 0 ? kG : -kG);
+  // G, the sign of gravity_u_spherical and the 1/2 of pd2, once per tesseroid
+  return f2_to_double(s, 0) * (FIELD == 0 ? kG : -0.5 * kG);
+}
+
+// Cartesian float-pair nodes of gauss_legendre_quadrature's point masses.
+__device__ __forceinline__ void cartesian_nodes(const Nodes& nd, lean::F2 (*xyz)[3][2],
+                                                lean::F2 (*m)[2], lean::F2* r) {
+  r[0] = lean::double_to_f2(nd.r[0]);
+  r[1] = lean::double_to_f2(nd.r[1]);
+  double c_lon[2], s_lon[2];
+#pragma unroll
+  for (int i = 0; i < 2; i++) sincos(nd.lon[i], &s_lon[i], &c_lon[i]);
+#pragma unroll
+  for (int jj = 0; jj < 2; jj++)
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+      const int jk = jj * 2 + k;
+      const double rc = nd.r[k] * nd.cphi[jj];
+#pragma unroll
+      for (int i = 0; i < 2; i++) {
+        xyz[jk][0][i] = lean::double_to_f2(rc * c_lon[i]);
+        xyz[jk][1][i] = lean::double_to_f2(rc * s_lon[i]);
+        xyz[jk][2][i] = lean::double_to_f2(nd.r[k] * nd.sphi[jj]);
+        m[jk][i] = lean::double_to_f2(nd.mass[jk * 2 + i]);
+      }
+    }
+}
+
+// A small tesseroid of a split pair: its point masses (the reference's
+// positions and masses) summed on float pairs.
+template <int FIELD>
+__device__ __forceinline__ double glq_leaf_pairs(const StationXYZ& q3, const Nodes& nd) {
+  lean::F2 xyz[4][3][2], m[4][2], r[2];
+  cartesian_nodes(nd, xyz, m, r);
+  RegNodes src;
+  src.r = lean::pk(r[0], r[1]);
+#pragma unroll
+  for (int jk = 0; jk < 4; jk++) {
+    src.x[jk] = lean::pk(xyz[jk][0][0], xyz[jk][0][1]);
+    src.y[jk] = lean::pk(xyz[jk][1][0], xyz[jk][1][1]);
+    src.z[jk] = lean::pk(xyz[jk][2][0], xyz[jk][2][1]);
+    src.m[jk] = lean::pk(m[jk][0], m[jk][1]);
+  }
+  return glq_sum_pairs<FIELD, 1>(q3, src);
 }
 
 // _adaptive_discretization (_tesseroid_utils.py:150-241) for one pair, each
@@ -287,8 +391,9 @@ __device__ __forceinline__ double glq_eval_pairs(const StationXYZ& q, const doub
 // stores and then integrates them).  status: 1 stack overflow, 2 more than
 // MAX_DISCRETIZATIONS small tesseroids.
 template <int FIELD>
-__device__ __noinline__ double adaptive_pair(const Station& p, const double* root, double density,
-                                             const Adapt& ad, const GlqRule& q, int& status) {
+__device__ __noinline__ double adaptive_pair(const Station& p, const StationXYZ& q3,
+                                             const double* root, double density, const Adapt& ad,
+                                             const GlqRule& q, int& status) {
   double stack[kStackSize][6];
 #pragma unroll
   for (int c = 0; c < 6; c++) stack[0][c] = root[c];
@@ -338,7 +443,7 @@ __device__ __noinline__ double adaptive_pair(const Station& p, const double* roo
       leaves++;
       Nodes nd;
       glq_nodes(t, density, q, nd);
-      acc = add(acc, glq_eval<FIELD>(p, nd.lon, nd.cphi, nd.sphi, nd.r, nd.mass));
+      acc += glq_leaf_pairs<FIELD>(q3, nd);
     }
   }
   return acc;
@@ -387,58 +492,58 @@ __global__ void prepare_kernel(const double* __restrict__ aos, const double* __r
   f2row[kFar * stride + j] = make_float2(far[1], far[2]);
   Nodes nd;
   glq_nodes(t, rho, q, nd);
-  double c_lon[2], s_lon[2];
+  lean::F2 xyz[4][3][2], mass[4][2], nr[2];
+  cartesian_nodes(nd, xyz, mass, nr);
+  f2row[kNodeR * stride + j] = make_float2(nr[0].h, nr[1].h);
+  f2row[(kNodeR + 1) * stride + j] = make_float2(nr[0].l, nr[1].l);
 #pragma unroll
-  for (int i = 0; i < 2; i++) sincos(nd.lon[i], &s_lon[i], &c_lon[i]);
+  for (int jk = 0; jk < 4; jk++) {
 #pragma unroll
-  for (int jj = 0; jj < 2; jj++)
-#pragma unroll
-    for (int k = 0; k < 2; k++) {
-      const int jk = jj * 2 + k;
-      const double rc = nd.r[k] * nd.cphi[jj];
-      lean::F2 xyz[3][2], m[2];
-#pragma unroll
-      for (int i = 0; i < 2; i++) {
-        xyz[0][i] = lean::double_to_f2(rc * c_lon[i]);
-        xyz[1][i] = lean::double_to_f2(rc * s_lon[i]);
-        xyz[2][i] = lean::double_to_f2(nd.r[k] * nd.sphi[jj]);
-        m[i] = lean::double_to_f2(nd.mass[jk * 2 + i]);
-      }
-#pragma unroll
-      for (int c = 0; c < 3; c++) {
-        f2row[(kNodes + (jk * 3 + c) * 2) * stride + j] = make_float2(xyz[c][0].h, xyz[c][1].h);
-        f2row[(kNodes + (jk * 3 + c) * 2 + 1) * stride + j] = make_float2(xyz[c][0].l, xyz[c][1].l);
-      }
-      f2row[(kMasses + jk * 2) * stride + j] = make_float2(m[0].h, m[1].h);
-      f2row[(kMasses + jk * 2 + 1) * stride + j] = make_float2(m[0].l, m[1].l);
+    for (int c = 0; c < 3; c++) {
+      f2row[(kNodes + (jk * 3 + c) * 2) * stride + j] =
+          make_float2(xyz[jk][c][0].h, xyz[jk][c][1].h);
+      f2row[(kNodes + (jk * 3 + c) * 2 + 1) * stride + j] =
+          make_float2(xyz[jk][c][0].l, xyz[jk][c][1].l);
     }
+    f2row[(kMasses + jk * 2) * stride + j] = make_float2(mass[jk][0].h, mass[jk][1].h);
+    f2row[(kMasses + jk * 2 + 1) * stride + j] = make_float2(mass[jk][0].l, mass[jk][1].l);
+  }
 }
 
-// Run the queued split pairs of this warp, 32 at a time (one per lane), and
-// add each result to its point's sum in list order.
+// A point's data for the lane that runs one of its split pairs.
+struct StationSh {
+  Station p;
+  StationXYZ q;
+};
+
+// Split pair `ent` of a chunk's list: (tesseroid index in the chunk) << 5 | lane.
 template <int FIELD>
-__device__ __forceinline__ void flush_near(const uint32_t* list, int count, int lane,
-                                           const Station& mine, const double* __restrict__ rec,
-                                           int64_t stride, int64_t p0, const Adapt& ad,
-                                           const GlqRule& q, double& acc, int& status) {
+__device__ __forceinline__ double run_entry(uint32_t ent, const StationSh& st,
+                                            const double* __restrict__ rec, int64_t stride,
+                                            int64_t p0, const Adapt& ad, const GlqRule& q,
+                                            int& status) {
+  const int64_t j = p0 + (int64_t)(ent >> 5);
+  double root[6];
+#pragma unroll
+  for (int c = 0; c < 6; c++) root[c] = rec[c * stride + j];
+  return adaptive_pair<FIELD>(st.p, st.q, root, rec[kRho * stride + j], ad, q, status);
+}
+
+// A warp's list is full: run it, 32 pairs at a time (one per lane), and add
+// each result to its point's sum in list order.
+template <int FIELD>
+__device__ __forceinline__ void flush_warp(const uint32_t* list, int count, int lane,
+                                           const StationSh* warp_st,
+                                           const double* __restrict__ rec, int64_t stride,
+                                           int64_t p0, const Adapt& ad, const GlqRule& q,
+                                           double& acc, int& status) {
   for (int r0 = 0; r0 < count; r0 += 32) {
     const int e = r0 + lane;
     const bool has = e < count;
     const uint32_t ent = has ? list[e] : 0u;
     const int owner = has ? (int)(ent & 31u) : lane;
-    Station s;
-    s.lon = __shfl_sync(0xffffffffu, mine.lon, owner);
-    s.cphi = __shfl_sync(0xffffffffu, mine.cphi, owner);
-    s.sphi = __shfl_sync(0xffffffffu, mine.sphi, owner);
-    s.r = __shfl_sync(0xffffffffu, mine.r, owner);
     double contrib = 0.0;
-    if (has) {
-      const int64_t j = p0 + (int64_t)(ent >> 5);
-      double root[6];
-#pragma unroll
-      for (int c = 0; c < 6; c++) root[c] = rec[c * stride + j];
-      contrib = adaptive_pair<FIELD>(s, root, rec[kRho * stride + j], ad, q, status);
-    }
+    if (has) contrib = run_entry<FIELD>(ent, warp_st[owner], rec, stride, p0, ad, q, status);
     __syncwarp();
     const int n = min(32, count - r0);
     for (int k = 0; k < n; k++) {
@@ -451,7 +556,7 @@ __device__ __forceinline__ void flush_near(const uint32_t* list, int count, int 
 }
 
 template <int FIELD>
-__global__ void __launch_bounds__(kThreads) forward_kernel(
+__global__ void __launch_bounds__(kThreads, 4) forward_kernel(
     const double* __restrict__ lon_deg, const double* __restrict__ lat_deg,
     const double* __restrict__ radius, int64_t n_obs, const double* __restrict__ rec,
     int64_t stride, int64_t n_tess, int64_t chunk, Adapt ad, GlqRule q,
@@ -459,6 +564,9 @@ __global__ void __launch_bounds__(kThreads) forward_kernel(
     int32_t* __restrict__ status_out) {
   __shared__ double sh[kSmemRows][kTile];
   __shared__ uint32_t near_list[kWarps][kNearCap];
+  __shared__ int near_count[kWarps];
+  __shared__ double contrib[kWarps * kNearCap];
+  __shared__ StationSh st[kThreads];
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
   const int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x;
@@ -475,9 +583,11 @@ __global__ void __launch_bounds__(kThreads) forward_kernel(
     q3.x = lean::double_to_f2(rc * clon);
     q3.y = lean::double_to_f2(rc * slon);
     q3.z = lean::double_to_f2(p.r * p.sphi);
+    q3.r = lean::double_to_f2(p.r);
     q3.inv_r = lean::double_to_f2(1.0 / p.r);
     q3.r_f = (float)p.r;
   }
+  st[threadIdx.x] = StationSh{p, q3};  // read after the first barrier below
   const bool rad_split = ad.radial != 0;
   const double ratio = ad.ratio;
 
@@ -523,7 +633,7 @@ __global__ void __launch_bounds__(kThreads) forward_kernel(
           near = split_axis(d, S(kLLon), ratio) || split_axis(d, S(kLLat), ratio) ||
                  (rad_split && split_axis(d, S(kLRad), ratio));
         }
-        if (!near) acc += glq_eval_pairs<FIELD>(q3, sh, c);
+        if (!near) acc += glq_sum_pairs<FIELD, 1>(q3, SmemNodes{sh, c});
 #undef F
 #undef S
       }
@@ -531,8 +641,8 @@ __global__ void __launch_bounds__(kThreads) forward_kernel(
       if (ball) {
         const int add_n = __popc(ball);
         if (n_near + add_n > kNearCap) {
-          flush_near<FIELD>(near_list[warp], n_near, lane, p, rec, stride, p0, ad, q, acc,
-                            status);
+          flush_warp<FIELD>(near_list[warp], n_near, lane, &st[warp * 32], rec, stride, p0, ad,
+                            q, acc, status);
           n_near = 0;
         }
         if (near)
@@ -543,8 +653,27 @@ __global__ void __launch_bounds__(kThreads) forward_kernel(
       }
     }
   }
-  if (n_near > 0)
-    flush_near<FIELD>(near_list[warp], n_near, lane, p, rec, stride, p0, ad, q, acc, status);
+  // the split pairs left in the four lists run on all the block's lanes
+  // together; each point then adds its results in its list's order
+  if (lane == 0) near_count[warp] = n_near;
+  __syncthreads();
+  int offs[kWarps], total = 0;
+#pragma unroll
+  for (int w = 0; w < kWarps; w++) {
+    offs[w] = total;
+    total += near_count[w];
+  }
+  for (int e = threadIdx.x; e < total; e += kThreads) {
+    int w = 0;
+#pragma unroll
+    for (int v = 1; v < kWarps; v++) w += e >= offs[v] ? 1 : 0;
+    const uint32_t ent = near_list[w][e - offs[w]];
+    contrib[e] = run_entry<FIELD>(ent, st[w * 32 + (int)(ent & 31u)], rec, stride, p0, ad, q,
+                                  status);
+  }
+  __syncthreads();
+  for (int k = 0; k < n_near; k++)
+    if ((int)(near_list[warp][k] & 31u) == lane) acc += contrib[offs[warp] + k];
   if (status && status_out) atomicOr(status_out, status);
   if (active) dst[(int64_t)blockIdx.y * dst_chunk_stride + i] = mul(acc, out_scale);
 }
@@ -620,7 +749,9 @@ Plan make_plan(int64_t n_obs, int64_t m) {
   if (p.n_tiles < 1) p.n_tiles = 1;
   int64_t m_tiles = (m + kTile - 1) / kTile;
   if (m_tiles < 1) m_tiles = 1;
-  const int64_t target = (int64_t)kSms * 8;
+  // about 8 waves of 4 resident CTAs per SM: the last, partial wave then
+  // costs at most an eighth of the launch
+  const int64_t target = (int64_t)kSms * 4 * 8;
   int64_t want = (target + p.n_tiles - 1) / p.n_tiles;
   // the per-warp list keeps the index within the chunk in 27 bits
   const int64_t min_chunks = (m_tiles * kTile + (1ll << 26) - 1) >> 26;
