@@ -693,7 +693,7 @@ def run_tesseroids(args, rank, world, local):
                                f"{n_obs} points 10 km above the WGS84 reference",
                    "l2": "flushed between timed steps (256 MB write)"},
         "roofline": roof, "cpu_baseline": base, "e2e": e2e,
-        "gpu_launches": 3 * args.steps, "clocks": clocks, "step_ms": step_ms,
+        "gpu_launches": 4 * args.steps, "clocks": clocks, "step_ms": step_ms,
     }))
 
 

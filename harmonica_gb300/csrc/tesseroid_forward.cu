@@ -36,6 +36,7 @@
 
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 #include <string>
 
 #include "../../include/harmonica_gb300.h"
@@ -555,10 +556,34 @@ __device__ __forceinline__ void flush_warp(const uint32_t* list, int count, int 
   __syncwarp();
 }
 
+// Per point, once per launch: the reference's radians, cos/sin of the
+// latitude and radius, and the Cartesian float pairs of the fast path.
+__global__ void stations_kernel(const double* __restrict__ lon_deg,
+                                const double* __restrict__ lat_deg,
+                                const double* __restrict__ radius, int64_t n_obs,
+                                StationSh* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_obs) return;
+  Station p;
+  p.lon = rad(lon_deg[i]);
+  sincos(rad(lat_deg[i]), &p.sphi, &p.cphi);
+  p.r = radius[i];
+  StationXYZ q3;
+  double slon, clon;
+  sincos(p.lon, &slon, &clon);
+  const double rc = p.r * p.cphi;
+  q3.x = lean::double_to_f2(rc * clon);
+  q3.y = lean::double_to_f2(rc * slon);
+  q3.z = lean::double_to_f2(p.r * p.sphi);
+  q3.r = lean::double_to_f2(p.r);
+  q3.inv_r = lean::double_to_f2(1.0 / p.r);
+  q3.r_f = (float)p.r;
+  out[i] = StationSh{p, q3};
+}
+
 template <int FIELD>
 __global__ void __launch_bounds__(kThreads, 4) forward_kernel(
-    const double* __restrict__ lon_deg, const double* __restrict__ lat_deg,
-    const double* __restrict__ radius, int64_t n_obs, const double* __restrict__ rec,
+    const StationSh* __restrict__ stations, int64_t n_obs, const double* __restrict__ rec,
     int64_t stride, int64_t n_tess, int64_t chunk, Adapt ad, GlqRule q,
     double* __restrict__ dst, int64_t dst_chunk_stride, double out_scale,
     int32_t* __restrict__ status_out) {
@@ -571,23 +596,10 @@ __global__ void __launch_bounds__(kThreads, 4) forward_kernel(
   const int warp = threadIdx.x >> 5;
   const int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x;
   const bool active = i < n_obs;
-  Station p;
-  p.lon = rad(active ? lon_deg[i] : 0.0);
-  sincos(rad(active ? lat_deg[i] : 0.0), &p.sphi, &p.cphi);
-  p.r = active ? radius[i] : 1.0;
-  StationXYZ q3;
-  {
-    double slon, clon;
-    sincos(p.lon, &slon, &clon);
-    const double rc = p.r * p.cphi;
-    q3.x = lean::double_to_f2(rc * clon);
-    q3.y = lean::double_to_f2(rc * slon);
-    q3.z = lean::double_to_f2(p.r * p.sphi);
-    q3.r = lean::double_to_f2(p.r);
-    q3.inv_r = lean::double_to_f2(1.0 / p.r);
-    q3.r_f = (float)p.r;
-  }
-  st[threadIdx.x] = StationSh{p, q3};  // read after the first barrier below
+  const StationSh me = stations[active ? i : 0];
+  const Station p = me.p;
+  const StationXYZ q3 = me.q;
+  st[threadIdx.x] = me;  // read after the first barrier below
   const bool rad_split = ad.radial != 0;
   const double ratio = ad.ratio;
 
@@ -633,7 +645,7 @@ __global__ void __launch_bounds__(kThreads, 4) forward_kernel(
           near = split_axis(d, S(kLLon), ratio) || split_axis(d, S(kLLat), ratio) ||
                  (rad_split && split_axis(d, S(kLRad), ratio));
         }
-        if (!near) acc += glq_sum_pairs<FIELD, 1>(q3, SmemNodes{sh, c});
+        if (!near) acc += glq_sum_pairs<FIELD, 4>(q3, SmemNodes{sh, c});
 #undef F
 #undef S
       }
@@ -740,7 +752,7 @@ __global__ void __launch_bounds__(kThreads) inside_kernel(
 
 struct Plan {
   int64_t n_tiles, n_chunks, chunk;
-  size_t rec_bytes, part_bytes;
+  size_t rec_bytes, station_bytes, part_bytes;
 };
 
 Plan make_plan(int64_t n_obs, int64_t m) {
@@ -749,9 +761,18 @@ Plan make_plan(int64_t n_obs, int64_t m) {
   if (p.n_tiles < 1) p.n_tiles = 1;
   int64_t m_tiles = (m + kTile - 1) / kTile;
   if (m_tiles < 1) m_tiles = 1;
-  // about 8 waves of 4 resident CTAs per SM: the last, partial wave then
-  // costs at most an eighth of the launch
-  const int64_t target = (int64_t)kSms * 4 * 8;
+  // about 96 waves of 4 resident CTAs per SM (HG_TESS_WAVES overrides),
+  // which on the layer workloads means one 64-tesseroid tile per CTA: the
+  // split pairs, which cost ~100x an unsplit one, then spread over many
+  // short CTAs instead of lengthening a few (measured on the 93,121-
+  // tesseroid layer: 8 waves 2.2e10 pairs/s, 24 2.8e10, 96 3.1e10).  The
+  // chunk partials stay below target x 128 points x 8 bytes (60 MB).
+  static const int64_t waves = [] {
+    const char* v = std::getenv("HG_TESS_WAVES");
+    const long w = v ? std::strtol(v, nullptr, 10) : 96;
+    return (int64_t)(w >= 1 && w <= 256 ? w : 96);
+  }();
+  const int64_t target = (int64_t)kSms * 4 * waves;
   int64_t want = (target + p.n_tiles - 1) / p.n_tiles;
   // the per-warp list keeps the index within the chunk in 27 bits
   const int64_t min_chunks = (m_tiles * kTile + (1ll << 26) - 1) >> 26;
@@ -764,6 +785,7 @@ Plan make_plan(int64_t n_obs, int64_t m) {
   p.n_chunks = (m + p.chunk - 1) / p.chunk;
   if (p.n_chunks < 1) p.n_chunks = 1;
   p.rec_bytes = ((size_t)kRows * (size_t)(m > 0 ? m : 1) * sizeof(double) + 255) & ~(size_t)255;
+  p.station_bytes = ((size_t)(n_obs > 0 ? n_obs : 1) * sizeof(StationSh) + 255) & ~(size_t)255;
   p.part_bytes = p.n_chunks > 1 ? (size_t)p.n_chunks * n_obs * sizeof(double) : 0;
   return p;
 }
@@ -791,7 +813,7 @@ int hg_tesseroid_forward_workspace(int64_t n_obs, int64_t n_tesseroids, size_t* 
   if (!bytes) return set_error(HG_ERR_INVALID, "null pointer");
   if (n_obs < 0 || n_tesseroids < 0) return set_error(HG_ERR_INVALID, "bad sizes");
   const tess::Plan p = tess::make_plan(n_obs, n_tesseroids);
-  *bytes = p.rec_bytes + p.part_bytes;
+  *bytes = p.rec_bytes + p.station_bytes + p.part_bytes;
   return HG_OK;
 }
 
@@ -817,7 +839,7 @@ int hg_tesseroid_forward(const double* longitude, const double* latitude, const 
     return cuda_check(cudaMemsetAsync(out, 0, sizeof(double) * n_obs, st), "cudaMemsetAsync");
   const tess::Plan plan = tess::make_plan(n_obs, n_tesseroids);
   if (plan.n_tiles > 2147483647LL) return set_error(HG_ERR_INVALID, "too many points");
-  const size_t need = plan.rec_bytes + plan.part_bytes;
+  const size_t need = plan.rec_bytes + plan.station_bytes + plan.part_bytes;
   bool own = false;
   if (workspace == nullptr) {
     cudaError_t e = cudaMallocAsync(&workspace, need, st);
@@ -827,7 +849,10 @@ int hg_tesseroid_forward(const double* longitude, const double* latitude, const 
     return set_error(HG_ERR_INVALID, "workspace too small");
   }
   double* rec = static_cast<double*>(workspace);
-  double* part = reinterpret_cast<double*>(static_cast<char*>(workspace) + plan.rec_bytes);
+  tess::StationSh* stations =
+      reinterpret_cast<tess::StationSh*>(static_cast<char*>(workspace) + plan.rec_bytes);
+  double* part = reinterpret_cast<double*>(static_cast<char*>(workspace) + plan.rec_bytes +
+                                           plan.station_bytes);
   const tess::GlqRule q = tess::make_rule(glq_nodes, glq_weights);
   tess::Adapt ad;
   ad.ratio = field == 3 ? 2.5 : 1.0;  // DISTANCE_SIZE_RATII, tesseroid_gravity.py:30
@@ -839,17 +864,22 @@ int hg_tesseroid_forward(const double* longitude, const double* latitude, const 
       tesseroids, density, n_tesseroids, rec, n_tesseroids, ad.ratio, q);
   int rc = cuda_check(cudaGetLastError(), "tesseroid prepare_kernel launch");
   if (rc == HG_OK) {
+    tess::stations_kernel<<<(unsigned)((n_obs + threads - 1) / threads), threads, 0, st>>>(
+        longitude, latitude, radius, n_obs, stations);
+    rc = cuda_check(cudaGetLastError(), "tesseroid stations_kernel launch");
+  }
+  if (rc == HG_OK) {
     const bool direct = plan.n_chunks == 1;
     double* dst = direct ? out : part;
     const dim3 grid((unsigned)plan.n_tiles, (unsigned)plan.n_chunks);
     if (field == 0)
       tess::forward_kernel<0><<<grid, tess::kThreads, 0, st>>>(
-          longitude, latitude, radius, n_obs, rec, n_tesseroids, n_tesseroids, plan.chunk, ad, q,
-          dst, n_obs, direct ? scale : 1.0, status);
+          stations, n_obs, rec, n_tesseroids, n_tesseroids, plan.chunk, ad, q, dst, n_obs,
+          direct ? scale : 1.0, status);
     else
       tess::forward_kernel<1><<<grid, tess::kThreads, 0, st>>>(
-          longitude, latitude, radius, n_obs, rec, n_tesseroids, n_tesseroids, plan.chunk, ad, q,
-          dst, n_obs, direct ? scale : 1.0, status);
+          stations, n_obs, rec, n_tesseroids, n_tesseroids, plan.chunk, ad, q, dst, n_obs,
+          direct ? scale : 1.0, status);
     rc = cuda_check(cudaGetLastError(), "tesseroid forward_kernel launch");
     if (rc == HG_OK && !direct) {
       tess::reduce_kernel<<<(unsigned)((n_obs + threads - 1) / threads), threads, 0, st>>>(
