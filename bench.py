@@ -585,10 +585,13 @@ def run_magnetic(args, rank, world, local):
                           "gpu_launches": 2 * args.steps}))
 
 
-# FP64 thread-instructions per tesseroid pair of the tesseroid forward kernel on the
-# Andes layer: ncu sm__sass_thread_inst_executed_op_fp64_pred_on.sum of one launch
-# (9.81e8) over its 3825 x 93121 pairs (profiles/tesseroid_forward_andes.md).
-FP64_INST_PER_TESS_PAIR = 2.75
+# Per-pair instruction counts of the tesseroid forward kernel on the Andes layer, from
+# ncu on one bench launch (smsp__inst_executed.sum and
+# sm__sass_thread_inst_executed_op_fp64_pred_on.sum over its 3825 x 93121 pairs;
+# profiles/tesseroid_forward_andes.md), and the DRAM bytes of that launch.
+WARP_INST_PER_TESS_PAIR = 20.4
+FP64_INST_PER_TESS_PAIR = 2.56
+TRAFFIC_BYTES_TESS_STEP = 46889728 + 35952384
 
 
 def run_tesseroids(args, rank, world, local):
@@ -672,17 +675,22 @@ def run_tesseroids(args, rank, world, local):
     if rank != 0:
         return
     kernel_rate = n_obs * m / (dev_time / args.steps)
-    roof = {"bound": "fp64", "peak": peak, "unit": "TFLOP/s",
-            "peak_source": "measured live: hg_fp64_peak_probe (FP64 FMA chains)",
-            "traffic": None}
-    if FP64_INST_PER_TESS_PAIR:
-        # the FP64 pipe issues one instruction per FMA; the probe's peak counts 2 flops per
-        # FMA, so FP64 instructions x 2 against it is the pipe's instruction-rate fraction
-        achieved = 2.0 * FP64_INST_PER_TESS_PAIR * kernel_rate / 1e12
-        roof.update({"achieved": achieved, "frac": achieved / peak,
-                     "fp64_inst_per_pair": FP64_INST_PER_TESS_PAIR,
-                     "note": "achieved = FP64 instructions issued per pair (ncu) x pairs/s x 2 "
-                             "(FMA-equivalent flops), against the FP64 FMA-chain peak"})
+    # the binding resource is instruction issue (the far path runs on packed FP32
+    # float pairs): warp instructions per pair x pairs/s against 4 per clock per SM
+    n_sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    sm_hz = (clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 0.0) * 1e6
+    issue_peak = 4 * n_sms * sm_hz
+    issue_rate = WARP_INST_PER_TESS_PAIR * kernel_rate
+    roof = {"bound": "instruction issue", "achieved": issue_rate / 1e9,
+            "peak": issue_peak / 1e9 if issue_peak else None, "unit": "G warp-instructions/s",
+            "frac": issue_rate / issue_peak if issue_peak else None,
+            "warp_inst_per_pair": WARP_INST_PER_TESS_PAIR,
+            "peak_source": "4 warp instructions per clock per SM x SMs x sampled SM clock",
+            "traffic": TRAFFIC_BYTES_TESS_STEP,
+            "fp64": {"inst_per_pair": FP64_INST_PER_TESS_PAIR,
+                     "pipe_frac": FP64_INST_PER_TESS_PAIR * kernel_rate / (peak * 1e12 / 2.0),
+                     "peak": peak, "unit": "TFLOP/s",
+                     "peak_source": "measured live: hg_fp64_peak_probe (FP64 FMA chains)"}}
     print(json.dumps({
         "metric": "FP64 tesseroid g_z pairs/s (points x tesseroids, adaptive GLQ)",
         "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,

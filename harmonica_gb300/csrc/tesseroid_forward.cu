@@ -690,13 +690,28 @@ __global__ void __launch_bounds__(kThreads, 4) forward_kernel(
   if (active) dst[(int64_t)blockIdx.y * dst_chunk_stride + i] = mul(acc, out_scale);
 }
 
-__global__ void reduce_kernel(const double* __restrict__ part, int64_t n_chunks, int64_t n_obs,
-                              double scale, double* __restrict__ out) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n_obs) return;
+// Sum of the chunk partials of 32 points per block: thread (x, y) adds the
+// chunks y, y + 16, ... of point x (coalesced rows), then the 16 group sums
+// are added in order of y.  Fixed order for a given number of chunks:
+// deterministic.
+constexpr int kReduceGroups = 16;
+
+__global__ void __launch_bounds__(32 * kReduceGroups) reduce_kernel(
+    const double* __restrict__ part, int64_t n_chunks, int64_t n_obs, double scale,
+    double* __restrict__ out) {
+  __shared__ double group[kReduceGroups][32];
+  const int64_t i = (int64_t)blockIdx.x * 32 + threadIdx.x;
   double s = 0.0;
-  for (int64_t c = 0; c < n_chunks; c++) s = add(s, part[c * n_obs + i]);
-  out[i] = mul(s, scale);
+  if (i < n_obs)
+    for (int64_t c = threadIdx.y; c < n_chunks; c += kReduceGroups) s += part[c * n_obs + i];
+  group[threadIdx.y][threadIdx.x] = s;
+  __syncthreads();
+  if (threadIdx.y == 0 && i < n_obs) {
+    double t = 0.0;
+#pragma unroll
+    for (int g = 0; g < kReduceGroups; g++) t += group[g][threadIdx.x];
+    out[i] = mul(t, scale);
+  }
 }
 
 // Python's float modulo (x % 360, result in [0, 360)).
@@ -882,8 +897,8 @@ int hg_tesseroid_forward(const double* longitude, const double* latitude, const 
           direct ? scale : 1.0, status);
     rc = cuda_check(cudaGetLastError(), "tesseroid forward_kernel launch");
     if (rc == HG_OK && !direct) {
-      tess::reduce_kernel<<<(unsigned)((n_obs + threads - 1) / threads), threads, 0, st>>>(
-          part, plan.n_chunks, n_obs, scale, out);
+      tess::reduce_kernel<<<(unsigned)((n_obs + 31) / 32), dim3(32, tess::kReduceGroups), 0,
+                            st>>>(part, plan.n_chunks, n_obs, scale, out);
       rc = cuda_check(cudaGetLastError(), "tesseroid reduce_kernel launch");
     }
   }
