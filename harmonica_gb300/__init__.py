@@ -8,8 +8,9 @@ harmonica):
 * :func:`prism_gravity` -- ``harmonica.prism_gravity``
 * :func:`prism_layer` and the ``prism_layer`` accessor
   (:class:`DatasetAccessorPrismLayer`) -- ``harmonica.prism_layer``
-* :func:`point_gravity`, :func:`prism_magnetic`, :func:`tesseroid_gravity`
-  -- the point-mass, magnetic-prism and tesseroid forward models
+* :func:`point_gravity`, :func:`prism_magnetic`, :func:`tesseroid_gravity`,
+  :func:`tesseroid_layer` -- the point-mass, magnetic-prism and tesseroid
+  forward models
 
 The all-pairs sums run in hand-written CUDA kernels behind the C ABI declared
 in ``include/harmonica_gb300.h``; :func:`build` compiles them in-tree.
@@ -25,6 +26,7 @@ from .layer import DatasetAccessorPrismLayer, PrismLayer, prism_layer
 from .magnetic import prism_magnetic
 from .point import point_gravity
 from .tesseroid import tesseroid_gravity
+from .tesseroid_layer import DatasetAccessorTesseroidLayer, TesseroidLayer, tesseroid_layer
 
 __all__ = [
     "DevicePrismLayer",
@@ -45,4 +47,7 @@ __all__ = [
     "point_gravity",
     "prism_magnetic",
     "tesseroid_gravity",
+    "tesseroid_layer",
+    "TesseroidLayer",
+    "DatasetAccessorTesseroidLayer",
 ]
