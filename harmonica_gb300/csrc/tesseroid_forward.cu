@@ -732,6 +732,7 @@ __global__ void __launch_bounds__(kThreads) inside_kernel(
     int64_t chunk, long long* __restrict__ conflicts, int64_t cap,
     unsigned long long* __restrict__ count) {
   __shared__ double sh[6][kTile];
+  __shared__ double bound[4];  // tile: lowest bottom, highest top, lowest south, highest north
   const int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x;
   const bool active = i < n_obs;
   const double lo = active ? lon[i] : 0.0;
@@ -749,7 +750,35 @@ __global__ void __launch_bounds__(kThreads) inside_kernel(
       if (c < cnt) sh[k][c] = aos[6 * (base + c) + k];
     }
     __syncthreads();
+    if (threadIdx.x < 32) {
+      // the tile's radial and latitudinal extent (fmin/fmax skip NaN bounds,
+      // whose tesseroids contain no point)
+      double lo_b = INFINITY, hi_t = -INFINITY, lo_s = INFINITY, hi_n = -INFINITY;
+      for (int c = threadIdx.x; c < cnt; c += 32) {
+        lo_b = fmin(lo_b, sh[4][c]);
+        hi_t = fmax(hi_t, sh[5][c]);
+        lo_s = fmin(lo_s, sh[2][c]);
+        hi_n = fmax(hi_n, sh[3][c]);
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        lo_b = fmin(lo_b, __shfl_xor_sync(0xffffffffu, lo_b, o));
+        hi_t = fmax(hi_t, __shfl_xor_sync(0xffffffffu, hi_t, o));
+        lo_s = fmin(lo_s, __shfl_xor_sync(0xffffffffu, lo_s, o));
+        hi_n = fmax(hi_n, __shfl_xor_sync(0xffffffffu, hi_n, o));
+      }
+      if (threadIdx.x == 0) {
+        bound[0] = lo_b;
+        bound[1] = hi_t;
+        bound[2] = lo_s;
+        bound[3] = hi_n;
+      }
+    }
+    __syncthreads();
     if (!active) continue;
+    // a point outside the tile's extent is in none of its tesseroids (points
+    // above a layer skip every tile)
+    if (!(bound[0] < r && r < bound[1] && bound[2] < la && la < bound[3])) continue;
     for (int c = 0; c < cnt; c++) {
       const double w = sh[0][c], e = sh[1][c], s = sh[2][c], n = sh[3][c];
       const double b = sh[4][c], t = sh[5][c];

@@ -50,7 +50,9 @@ def test_layer_gravity(field):
     npt.assert_allclose(layer.tesseroid_layer.gravity(grid, field=field), expected)
     ref = to.tesseroid_gravity(grid, layer.tesseroid_layer._to_tesseroids(), density.ravel(),
                                field)
-    npt.assert_allclose(expected, ref, rtol=1e-11)
+    # points 10 km above 4-5 degree tesseroids that are split: the near class
+    # of test_gpu_tesseroid.py
+    npt.assert_allclose(expected, ref, rtol=1e-8)
 
 
 @pytest.mark.parametrize("field", ["potential", "g_z"])
