@@ -13,6 +13,7 @@
 
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -83,16 +84,29 @@ struct RowFields {
 };
 
 // out[row][i] = scale(field of row) * sum_c part[c][row][i], chunks in order.
-__global__ void reduce_chunks_kernel(const double* __restrict__ part, int64_t n_chunks,
-                                     int64_t chunk_stride, int64_t n_obs, int n_rows,
-                                     RowFields row_field, double* __restrict__ out) {
-  int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  int64_t total = (int64_t)n_rows * n_obs;
-  if (idx >= total) return;
-  int row = (int)(idx / n_obs);
+// 32 outputs per block: thread (x, y) adds chunks y, y + 16, ... of output x
+// (coalesced rows), then the 16 group sums are added in order of y -- a
+// fixed order for a given chunk count (deterministic), and 16x the memory
+// parallelism of one thread walking all chunks.
+constexpr int kReduceGroups = 16;
+
+__global__ void __launch_bounds__(32 * kReduceGroups) reduce_chunks_kernel(
+    const double* __restrict__ part, int64_t n_chunks, int64_t chunk_stride, int64_t n_obs,
+    int n_rows, RowFields row_field, double* __restrict__ out) {
+  __shared__ double group[kReduceGroups][32];
+  const int64_t idx = (int64_t)blockIdx.x * 32 + threadIdx.x;
+  const int64_t total = (int64_t)n_rows * n_obs;
   double s = 0.0;
-  for (int64_t c = 0; c < n_chunks; c++) s += part[c * chunk_stride + idx];
-  out[idx] = s * field_scale(row_field.f[row]);
+  if (idx < total)
+    for (int64_t c = threadIdx.y; c < n_chunks; c += kReduceGroups) s += part[c * chunk_stride + idx];
+  group[threadIdx.y][threadIdx.x] = s;
+  __syncthreads();
+  if (threadIdx.y == 0 && idx < total) {
+    double t = 0.0;
+#pragma unroll
+    for (int g = 0; g < kReduceGroups; g++) t += group[g][threadIdx.x];
+    out[idx] = t * field_scale(row_field.f[(int)(idx / n_obs)]);
+  }
 }
 
 // top/bottom of a layer from surface and reference (layer.py:264-312): the
@@ -146,9 +160,20 @@ Plan make_plan(int64_t n_obs, int64_t n_prisms, uint32_t mask) {
     for (int f = 0; f < kNumFields; f++)
       if ((mask >> f) & 1u) p.single_field = f;
   p.n_tiles = (n_obs + kThreads - 1) / kThreads;
-  // Enough CTAs for several waves over all SMs; split the prisms when the
-  // observation tiles alone cannot fill the GPU.
-  const int64_t target = (int64_t)kSmCount * 8;
+  // Enough CTAs for many full waves of the resident CTAs on every SM
+  // (HG_FWD_WAVES overrides the default 32); split the prisms when the
+  // observation tiles alone cannot fill the GPU.  Measured on the g_z bench
+  // step (5000 stations x 1e6 prisms): 1 wave 1.09e10 pairs/s, 2 1.14e10,
+  // 4 1.18e10, 16 1.20e10, 32 1.21e10 (the old fixed 8 CTAs per SM was
+  // 1.6 waves): short CTAs even out the SMs' progress and the tail.
+  static const int64_t waves = [] {
+    const char* v = std::getenv("HG_FWD_WAVES");
+    const long w = v ? std::strtol(v, nullptr, 10) : 32;
+    return (int64_t)(w >= 1 && w <= 256 ? w : 32);
+  }();
+  const bool wide = p.all || p.single_field == kPotential;
+  const int64_t resident = wide ? HG_FWD_MIN_BLOCKS_ALL : HG_FWD_MIN_BLOCKS;
+  const int64_t target = (int64_t)kSmCount * resident * waves;
   int64_t n_prism_tiles = (n_prisms + kTile - 1) / kTile;
   if (n_prism_tiles < 1) n_prism_tiles = 1;
   int64_t want = (target + p.n_tiles - 1) / p.n_tiles;
@@ -218,9 +243,8 @@ int launch_forward(const Plan& plan, const double* oe, const double* on, const d
     for (int f = 0; f < kNumFields; f++)
       if ((mask >> f) & 1u) rf.f[r++] = f;
     int64_t total = (int64_t)plan.n_rows * n_obs;
-    int threads = 256;
-    int64_t blocks = (total + threads - 1) / threads;
-    reduce_chunks_kernel<<<(unsigned)blocks, threads, 0, stream>>>(
+    int64_t blocks = (total + 31) / 32;
+    reduce_chunks_kernel<<<(unsigned)blocks, dim3(32, kReduceGroups), 0, stream>>>(
         dst, plan.n_chunks, chunk_stride, n_obs, plan.n_rows, rf, out);
     rc = cuda_check(cudaGetLastError(), "reduce_chunks_kernel launch");
     if (own_ws) cudaFreeAsync(workspace, stream);
