@@ -113,15 +113,6 @@ __global__ void __launch_bounds__(kThreads) point_kernel(
   dst[(int64_t)blockIdx.y * dst_chunk_stride + i] = scale_output ? acc * field_scale(F) : acc;
 }
 
-__global__ void point_reduce_kernel(const double* __restrict__ part, int64_t n_chunks,
-                                    int64_t n_obs, double scale, double* __restrict__ out) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n_obs) return;
-  double s = 0.0;
-  for (int64_t c = 0; c < n_chunks; c++) s += part[c * n_obs + i];
-  out[i] = s * scale;
-}
-
 struct PointPlan {
   int64_t tiles, n_chunks, chunk;
   size_t bytes;
@@ -130,7 +121,7 @@ struct PointPlan {
 PointPlan point_plan(int64_t n_obs, int64_t n_points) {
   PointPlan p;
   p.tiles = (n_obs + kThreads - 1) / kThreads;
-  const int64_t target = (int64_t)kSmCount * 8;
+  const int64_t target = (int64_t)kSmCount * 4 * launch_waves();
   int64_t pt = (n_points + kTile - 1) / kTile;
   if (pt < 1) pt = 1;
   int64_t want = (target + (p.tiles > 0 ? p.tiles : 1) - 1) / (p.tiles > 0 ? p.tiles : 1);
@@ -168,9 +159,8 @@ int launch_point(int field, const double* c1, const double* c2, const double* c3
   }
   int rc = cuda_check(cudaGetLastError(), "point_kernel launch");
   if (rc != HG_OK || direct) return rc;
-  point_reduce_kernel<<<(unsigned)((n_obs + 255) / 256), 256, 0, st>>>(
-      dst, plan.n_chunks, n_obs, field_scale(field), out);
-  return cuda_check(cudaGetLastError(), "point_reduce_kernel launch");
+  launch_chunk_sum(dst, plan.n_chunks, n_obs, n_obs, field_scale(field), out, st);
+  return cuda_check(cudaGetLastError(), "chunk_sum_kernel launch");
 }
 
 }  // namespace

@@ -126,7 +126,7 @@ struct AdjPlan {
 AdjPlan adj_plan(int64_t n_obs, int64_t n_prisms) {
   AdjPlan p;
   p.tiles = (n_prisms + kThreads - 1) / kThreads;
-  const int64_t target = (int64_t)kSmCount * 8;
+  const int64_t target = (int64_t)kSmCount * HG_ADJ_MIN_BLOCKS * launch_waves();
   int64_t point_tiles = (n_obs + kTile - 1) / kTile;
   if (point_tiles < 1) point_tiles = 1;
   int64_t want = (target + p.tiles - 1) / (p.tiles > 0 ? p.tiles : 1);

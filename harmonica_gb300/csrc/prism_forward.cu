@@ -161,19 +161,13 @@ Plan make_plan(int64_t n_obs, int64_t n_prisms, uint32_t mask) {
       if ((mask >> f) & 1u) p.single_field = f;
   p.n_tiles = (n_obs + kThreads - 1) / kThreads;
   // Enough CTAs for many full waves of the resident CTAs on every SM
-  // (HG_FWD_WAVES overrides the default 32); split the prisms when the
-  // observation tiles alone cannot fill the GPU.  Measured on the g_z bench
-  // step (5000 stations x 1e6 prisms): 1 wave 1.09e10 pairs/s, 2 1.14e10,
-  // 4 1.18e10, 16 1.20e10, 32 1.21e10 (the old fixed 8 CTAs per SM was
-  // 1.6 waves): short CTAs even out the SMs' progress and the tail.
-  static const int64_t waves = [] {
-    const char* v = std::getenv("HG_FWD_WAVES");
-    const long w = v ? std::strtol(v, nullptr, 10) : 32;
-    return (int64_t)(w >= 1 && w <= 256 ? w : 32);
-  }();
+  // (launch_waves()); split the prisms when the observation tiles alone
+  // cannot fill the GPU.  Measured on the g_z bench step (5000 stations x
+  // 1e6 prisms): 1 wave 1.09e10 pairs/s, 2 1.14e10, 4 1.18e10, 16 1.20e10,
+  // 32 1.21e10 (the old fixed 8 CTAs per SM was 1.6 waves).
   const bool wide = p.all || p.single_field == kPotential;
   const int64_t resident = wide ? HG_FWD_MIN_BLOCKS_ALL : HG_FWD_MIN_BLOCKS;
-  const int64_t target = (int64_t)kSmCount * resident * waves;
+  const int64_t target = (int64_t)kSmCount * resident * launch_waves();
   int64_t n_prism_tiles = (n_prisms + kTile - 1) / kTile;
   if (n_prism_tiles < 1) n_prism_tiles = 1;
   int64_t want = (target + p.n_tiles - 1) / p.n_tiles;

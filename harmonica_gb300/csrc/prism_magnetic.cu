@@ -102,15 +102,6 @@ __global__ void __launch_bounds__(kThreads, HG_MAG_MIN_BLOCKS) magnetic_kernel(
   }
 }
 
-__global__ void mag_reduce_kernel(const double* __restrict__ part, int64_t n_chunks,
-                                  int64_t chunk_stride, int64_t total, double* __restrict__ out) {
-  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= total) return;
-  double s = 0.0;
-  for (int64_t c = 0; c < n_chunks; c++) s += part[c * chunk_stride + idx];
-  out[idx] = s * (kMu0Over4Pi * 1e9);
-}
-
 __global__ void pack_magnetic_kernel(const double* __restrict__ aos, const double* __restrict__ me,
                                      const double* __restrict__ mn, const double* __restrict__ mu,
                                      int64_t n, double* __restrict__ soa, int64_t stride) {
@@ -133,7 +124,7 @@ MagPlan mag_plan(int64_t n_obs, int64_t n_prisms, int comp) {
   MagPlan p;
   p.rows = comp == 3 ? 3 : 1;
   p.tiles = (n_obs + kThreads - 1) / kThreads;
-  const int64_t target = (int64_t)kSmCount * 8;
+  const int64_t target = (int64_t)kSmCount * HG_MAG_MIN_BLOCKS * launch_waves();
   int64_t pt = (n_prisms + kTile - 1) / kTile;
   if (pt < 1) pt = 1;
   int64_t want = (target + (p.tiles > 0 ? p.tiles : 1) - 1) / (p.tiles > 0 ? p.tiles : 1);
@@ -203,9 +194,8 @@ int hg_prism_magnetic(const double* obs_e, const double* obs_n, const double* ob
   int rc = cuda_check(cudaGetLastError(), "magnetic_kernel launch");
   if (rc != HG_OK || direct) return rc;
   const int64_t total = cstride;
-  mag_reduce_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(dst, plan.n_chunks, cstride,
-                                                                     total, out);
-  return cuda_check(cudaGetLastError(), "mag_reduce_kernel launch");
+  launch_chunk_sum(dst, plan.n_chunks, cstride, total, kMu0Over4Pi * 1e9, out, st);
+  return cuda_check(cudaGetLastError(), "chunk_sum_kernel launch");
 }
 
 }  // extern "C"
