@@ -58,9 +58,9 @@ ALGO_FLOP_PER_PAIR_GZ = 720.0
 # FP64 thread-instructions per pair (sm__sass_thread_inst_executed_op_fp64_pred_on / pairs),
 # warp instructions issued per pair (smsp__inst_executed / pairs) and DRAM read+write bytes of
 # one default step's launch (5000 stations x 1e6 prisms).
-FP64_INST_PER_PAIR_GZ = 9.14
-WARP_INST_PER_PAIR_GZ = 64.15
-TRAFFIC_BYTES_GZ_STEP = 24918272 + 1273344
+FP64_INST_PER_PAIR_GZ = 9.37
+WARP_INST_PER_PAIR_GZ = 65.9
+TRAFFIC_BYTES_GZ_STEP = 25041664 + 18485760
 ISSUE_PER_SM_PER_CLOCK = 4  # one warp instruction per clock per SM sub-partition, 4 per SM
 METRIC = "FP64 g_z prism-station pairs/s"
 WORKLOAD = "layer_topography_1e6: 1000x1000 prisms (200 m grid), 500x500 stations, g_z"
