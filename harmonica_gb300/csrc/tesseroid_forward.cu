@@ -63,7 +63,9 @@ constexpr double kPreTest = 1.0 + 0x1p-40;
 // Rows of the prepared tesseroid records (structure of arrays, `stride`
 // doubles per row).  Rows from kLonC on are staged in shared memory.
 enum Row : int {
-  kW, kE, kS, kN, kBot, kTop, kRho,
+  kW, kE, kS, kN, kBot, kTop,
+  kRho,       // density at the radial nodes k = 0 and 1 (equal for a constant
+  kRho1,      // density; a density function evaluated at the node radii)
   kLonC,      // centre longitude (radians)
   kCosC,      // cos / sin of the centre latitude
   kSinC,
@@ -157,8 +159,11 @@ struct Nodes {
   double lon[2], cphi[2], sphi[2], r[2], mass[8];
 };
 
-__device__ __forceinline__ void glq_nodes(const double* t, double density, const GlqRule& q,
-                                          Nodes& nd) {
+// density[k]: the density at radial node k (gauss_legendre_quadrature uses one
+// value; gauss_legendre_quadrature_variable_density, _tesseroid_variable_
+// density.py:18-107, the density function at radius_p of node k).
+__device__ __forceinline__ void glq_nodes(const double* t, const double* density,
+                                          const GlqRule& q, Nodes& nd) {
   const double w = t[0], e = t[1], s = t[2], n = t[3], bottom = t[4], top = t[5];
   const double a_factor =
       mul(mul(mul(0.125, rad(sub(e, w))), rad(sub(n, s))), sub(top, bottom));
@@ -181,7 +186,7 @@ __device__ __forceinline__ void glq_nodes(const double* t, double density, const
 #pragma unroll
       for (int i = 0; i < 2; i++)
         nd.mass[(j * 2 + k) * 2 + i] =
-            mul(mul(mul(mul(mul(density, a_factor), kappa), q.weight[i]), q.weight[2 + j]),
+            mul(mul(mul(mul(mul(density[k], a_factor), kappa), q.weight[i]), q.weight[2 + j]),
                 q.weight[4 + k]);
     }
 }
@@ -393,7 +398,8 @@ __device__ __forceinline__ double glq_leaf_pairs(const StationXYZ& q3, const Nod
 // MAX_DISCRETIZATIONS small tesseroids.
 template <int FIELD>
 __device__ __noinline__ double adaptive_pair(const Station& p, const StationXYZ& q3,
-                                             const double* root, double density, const Adapt& ad,
+                                             const double* root, const double* density,
+                                             const Adapt& ad,
                                              const GlqRule& q, int& status) {
   double stack[kStackSize][6];
 #pragma unroll
@@ -451,22 +457,26 @@ __device__ __noinline__ double adaptive_pair(const Station& p, const StationXYZ&
 }
 
 __global__ void prepare_kernel(const double* __restrict__ aos, const double* __restrict__ density,
-                               int64_t m, double* __restrict__ rec, int64_t stride, double ratio,
-                               GlqRule q) {
+                               int per_node, int64_t m, double* __restrict__ rec, int64_t stride,
+                               double ratio, GlqRule q) {
   const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= m) return;
   double t[6];
 #pragma unroll
   for (int c = 0; c < 6; c++) t[c] = aos[6 * j + c];
-  const double rho = density[j];
+  double rho[2];
+  rho[0] = per_node ? density[2 * j] : density[j];
+  rho[1] = per_node ? density[2 * j + 1] : rho[0];
 #pragma unroll
   for (int c = 0; c < 6; c++) rec[c * stride + j] = t[c];
-  rec[kRho * stride + j] = rho;
+  rec[kRho * stride + j] = rho[0];
+  rec[kRho1 * stride + j] = rho[1];
   // _discard_null_tesseroids (_tesseroid_utils.py:503-538); a tesseroid with a
   // NaN or infinite bound or density that is not null makes the reference's
   // result NaN: flag 2
-  const bool null = t[0] == t[1] || t[2] == t[3] || t[4] == t[5] || rho == 0.0;
-  bool finite = isfinite(rho);
+  const bool null =
+      t[0] == t[1] || t[2] == t[3] || t[4] == t[5] || (rho[0] == 0.0 && rho[1] == 0.0);
+  bool finite = isfinite(rho[0]) && isfinite(rho[1]);
 #pragma unroll
   for (int c = 0; c < 6; c++) finite = finite && isfinite(t[c]);
   rec[kSkip * stride + j] = null ? 1.0 : (finite ? 0.0 : 2.0);
@@ -527,7 +537,8 @@ __device__ __forceinline__ double run_entry(uint32_t ent, const StationSh& st,
   double root[6];
 #pragma unroll
   for (int c = 0; c < 6; c++) root[c] = rec[c * stride + j];
-  return adaptive_pair<FIELD>(st.p, st.q, root, rec[kRho * stride + j], ad, q, status);
+  const double rho[2] = {rec[kRho * stride + j], rec[kRho1 * stride + j]};
+  return adaptive_pair<FIELD>(st.p, st.q, root, rho, ad, q, status);
 }
 
 // A warp's list is full: run it, 32 pairs at a time (one per lane), and add
@@ -863,7 +874,8 @@ int hg_tesseroid_forward_workspace(int64_t n_obs, int64_t n_tesseroids, size_t* 
 
 int hg_tesseroid_forward(const double* longitude, const double* latitude, const double* radius,
                          int64_t n_obs, const double* tesseroids, const double* density,
-                         int64_t n_tesseroids, int32_t field, int32_t radial_discretization,
+                         int32_t density_per_node, int64_t n_tesseroids, int32_t field,
+                         int32_t radial_discretization,
                          int32_t stack_size, int64_t max_discretizations,
                          const double* glq_nodes, const double* glq_weights, double* out,
                          int32_t* status, void* workspace, size_t workspace_bytes,
@@ -905,7 +917,7 @@ int hg_tesseroid_forward(const double* longitude, const double* latitude, const 
   ad.max_leaves = max_discretizations > 0 ? max_discretizations : tess::kMaxLeaves;
   const int threads = 256;
   tess::prepare_kernel<<<(unsigned)((n_tesseroids + threads - 1) / threads), threads, 0, st>>>(
-      tesseroids, density, n_tesseroids, rec, n_tesseroids, ad.ratio, q);
+      tesseroids, density, density_per_node ? 1 : 0, n_tesseroids, rec, n_tesseroids, ad.ratio, q);
   int rc = cuda_check(cudaGetLastError(), "tesseroid prepare_kernel launch");
   if (rc == HG_OK) {
     tess::stations_kernel<<<(unsigned)((n_obs + threads - 1) / threads), threads, 0, st>>>(

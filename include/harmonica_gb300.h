@@ -327,7 +327,13 @@ int hg_point_forward(const double *obs_1, const double *obs_2, const double *obs
  * longitude, latitude (degrees), radius (m): n_obs computation points.
  * tesseroids: n_tesseroids rows of (west, east, south, north, bottom, top)
  * in degrees and metres, row-major, already made continuous in longitude
- * (west <= east, as _check_tesseroids leaves them); density in kg/m^3.
+ * (west <= east, as _check_tesseroids leaves them); density in kg/m^3: one
+ * value per tesseroid (density_per_node = 0), or (density_per_node = 1) two
+ * per tesseroid, the density at its two radial Gauss-Legendre nodes -- a
+ * density function evaluated at radius_p as
+ * gauss_legendre_quadrature_variable_density does
+ * (_tesseroid_variable_density.py:18-107); valid only without radial
+ * discretization, where every small tesseroid keeps its root's radii.
  * field: 0 potential (J/kg) or 3 g_z (mGal, downward).
  * radial_discretization: nonzero splits along the radius too.
  * stack_size (<= 100) and max_discretizations: the reference's STACK_SIZE
@@ -347,7 +353,8 @@ int hg_tesseroid_forward_workspace(int64_t n_obs, int64_t n_tesseroids, size_t *
 
 int hg_tesseroid_forward(const double *longitude, const double *latitude, const double *radius,
                          int64_t n_obs, const double *tesseroids, const double *density,
-                         int64_t n_tesseroids, int32_t field, int32_t radial_discretization,
+                         int32_t density_per_node, int64_t n_tesseroids, int32_t field,
+                         int32_t radial_discretization,
                          int32_t stack_size, int64_t max_discretizations,
                          const double *glq_nodes, const double *glq_weights, double *out,
                          int32_t *status, void *workspace, size_t workspace_bytes,

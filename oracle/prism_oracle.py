@@ -100,7 +100,7 @@ def _load():
     lib.oracle_tesseroid_glq.restype = ctypes.c_double
     lib.oracle_tesseroid_glq.argtypes = [
         ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, dp,
-        ctypes.c_double, dp, dp,
+        dp, dp, dp,
     ]
     lib.oracle_adaptive_discretization.restype = i64
     lib.oracle_adaptive_discretization.argtypes = [
@@ -110,7 +110,8 @@ def _load():
     lib.oracle_set_trig_perturbation.argtypes = [ctypes.c_int]
     lib.oracle_tesseroid_gravity.restype = ctypes.c_int
     lib.oracle_tesseroid_gravity.argtypes = [
-        ctypes.c_int, ctypes.c_int, i64, dp, dp, dp, i64, dp, dp, dp, dp, dp, ctypes.c_int
+        ctypes.c_int, ctypes.c_int, i64, dp, dp, dp, i64, dp, dp, ctypes.c_int, dp, dp, dp,
+        ctypes.c_int,
     ]
     _lib = lib
     return lib

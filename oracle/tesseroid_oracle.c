@@ -124,9 +124,13 @@ double oracle_distance_tesseroid_point(double longitude, double latitude, double
 /* gauss_legendre_quadrature (_tesseroid_utils.py:18-115).  nodes/weights:
  * [lon(2), lat(2), rad(2)] from numpy.polynomial.legendre.leggauss(2). */
 double oracle_tesseroid_glq(int field, double longitude_rad, double cosphi, double sinphi,
-                            double radius, const double *t, double density,
+                            double radius, const double *t, const double *density,
                             const double *nodes, const double *weights)
 {
+    /* density[k]: the density at radial node k -- one value twice for
+     * gauss_legendre_quadrature, the density function at radius_p for
+     * gauss_legendre_quadrature_variable_density
+     * (_tesseroid_variable_density.py:18-107) */
     const double w = t[0], e = t[1], s = t[2], n = t[3], bottom = t[4], top = t[5];
     const double a_factor = 1.0 / 8 * radians(e - w) * radians(n - s) * (top - bottom);
     double result = 0.0;
@@ -140,7 +144,7 @@ double oracle_tesseroid_glq(int field, double longitude_rad, double cosphi, doub
             for (int i = 0; i < 2; i++) {
                 const double longitude_p = radians(0.5 * (e - w) * nodes[i] + 0.5 * (e + w));
                 const double mass =
-                    density * a_factor * kappa * weights[i] * weights[2 + j] * weights[4 + k];
+                    density[k] * a_factor * kappa * weights[i] * weights[2 + j] * weights[4 + k];
                 result += mass * point_kernel(field, longitude_rad, cosphi, sinphi, radius,
                                               longitude_p, cosphi_p, sinphi_p, radius_p);
             }
@@ -237,7 +241,8 @@ int64_t oracle_adaptive_discretization(const double *point, const double *tess, 
 
 typedef struct {
     int field;
-    double longitude_rad, cosphi, sinphi, radius, density;
+    double longitude_rad, cosphi, sinphi, radius;
+    double density[2];
     const double *nodes, *weights;
     double acc;
 } glq_ctx;
@@ -260,20 +265,23 @@ static void glq_leaf(const double *t, void *vctx)
 int oracle_tesseroid_gravity(int field, int radial, int64_t n_obs, const double *longitude,
                              const double *latitude, const double *radius, int64_t n_tess,
                              const double *tesseroids, const double *density,
-                             const double *nodes, const double *weights, double *result,
-                             int parallel)
+                             int density_per_node, const double *nodes, const double *weights,
+                             double *result, int parallel)
 {
+    /* density: one value per tesseroid, or (density_per_node, 2D
+     * discretization only) the density at its two radial nodes */
     const double ratio = field == 0 ? 1.0 : 2.5;
     int status = TESS_OK;
 #pragma omp parallel for schedule(dynamic, 1) if (parallel)
     for (int64_t i = 0; i < n_obs; i++) {
         const double point[3] = {longitude[i], latitude[i], radius[i]};
         const double lat = radians(latitude[i]);
-        glq_ctx g = {field, radians(longitude[i]), t_cos(lat), t_sin(lat), radius[i], 0.0,
+        glq_ctx g = {field, radians(longitude[i]), t_cos(lat), t_sin(lat), radius[i], {0.0, 0.0},
                      nodes, weights, 0.0};
         double acc = 0.0;
         for (int64_t j = 0; j < n_tess; j++) {
-            g.density = density[j];
+            g.density[0] = density_per_node ? density[2 * j] : density[j];
+            g.density[1] = density_per_node ? density[2 * j + 1] : density[j];
             /* result[i] += glq(leaf) leaf by leaf, as the reference does */
             g.acc = acc;
             const int64_t rc = adaptive(point, tesseroids + 6 * j, ratio, radial, 0, 0, glq_leaf, &g);

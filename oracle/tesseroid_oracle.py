@@ -98,10 +98,15 @@ def adaptive_discretization(point, tesseroid, distance_size_ratio, radial_discre
 
 def tesseroid_gravity(coordinates, tesseroids, density, field,
                       radial_adaptive_discretization=False, disable_checks=False,
-                      parallel=True, trig_perturbation=False):
-    """Reference result (potential J/kg, g_z mGal) for constant densities.
-    ``trig_perturbation`` moves every cos/sin/acos by -1, 0 or +1 ulp (a
-    conditioning probe: how much the result depends on the libm)."""
+                      parallel=True, trig_perturbation=False, node_density=None):
+    """Reference result (potential J/kg, g_z mGal).  ``density``: one value
+    per tesseroid; or ``node_density`` (M, 2): the density at the two radial
+    nodes of each tesseroid, as gauss_legendre_quadrature_variable_density
+    evaluates a density function (2D discretization only; the tesseroids are
+    then used as given, without the null discard, like the reference's
+    variable-density loop).  ``trig_perturbation`` moves every cos/sin/acos by
+    -1, 0 or +1 ulp (a conditioning probe: how much the result depends on the
+    libm)."""
     if field not in FIELD_CODES:
         msg = f"Gravitational field {field} not recognized"
         raise ValueError(msg)
@@ -110,9 +115,15 @@ def tesseroid_gravity(coordinates, tesseroids, density, field,
     tess = np.atleast_2d(np.asarray(tesseroids, dtype=np.float64))
     if not disable_checks and (tess[:, 0] > tess[:, 1]).any():
         tess = longitude_continuity(tess)
-    rho = np.atleast_1d(np.asarray(density, dtype=np.float64)).ravel()
-    tess, rho = discard_null_tesseroids(tess, rho)
-    tess, rho = _f64(tess), _f64(rho)
+    if node_density is not None:
+        if radial_adaptive_discretization:
+            raise ValueError("node densities need the 2D discretization")
+        rho = _f64(np.asarray(node_density, dtype=np.float64).reshape(-1, 2))
+        tess = _f64(tess)
+    else:
+        rho = np.atleast_1d(np.asarray(density, dtype=np.float64)).ravel()
+        tess, rho = discard_null_tesseroids(tess, rho)
+        tess, rho = _f64(tess), _f64(rho)
     nodes, weights = glq_nodes_weights()
     result = np.zeros(lon.size)
     lib = _load()
@@ -120,8 +131,9 @@ def tesseroid_gravity(coordinates, tesseroids, density, field,
     try:
         rc = lib.oracle_tesseroid_gravity(
             FIELD_CODES[field], int(radial_adaptive_discretization), lon.size, _ptr(lon),
-            _ptr(lat), _ptr(rad), tess.shape[0], _ptr(tess), _ptr(rho), _ptr(nodes),
-            _ptr(weights), _ptr(result), int(parallel),
+            _ptr(lat), _ptr(rad), tess.shape[0], _ptr(tess), _ptr(rho),
+            int(node_density is not None), _ptr(nodes), _ptr(weights), _ptr(result),
+            int(parallel),
         )
     finally:
         lib.oracle_set_trig_perturbation(0)

@@ -1,7 +1,9 @@
 """
-Generate ``reference_tesseroid.npz``: outputs of harmonica's own tesseroid
-forward model (src/harmonica/_forward/tesseroid_gravity.py and
-_tesseroid_utils.py, run from the reference sources) on small cases.
+Generate ``reference_tesseroid.npz`` and ``reference_tesseroid_variable.npz``:
+outputs of harmonica's own tesseroid forward model
+(src/harmonica/_forward/tesseroid_gravity.py, _tesseroid_utils.py and
+_tesseroid_variable_density.py, run from the reference sources) on small
+cases, constant densities and density functions.
 
 numba and choclo are not installed here, so the reference functions are run
 as plain Python: ``numba.jit`` is replaced by the identity decorator and
@@ -121,8 +123,78 @@ def cases():
     return out
 
 
+# density functions of the variable-density cases (test/test_tesseroid_variable_density.py
+# fixtures); tests/test_gpu_tesseroid.py defines the same functions
+def quadratic_density(radius):
+    return 1e-3 * (radius - 3e3) ** 2 + 1900.0
+
+
+def linear_shell_density(top, bottom):
+    slope = (2500.0 - 3300.0) / (top - bottom)
+    constant = 2500.0 - slope * top
+    return lambda radius: slope * radius + constant
+
+
+def exponential_shell_density(top, bottom, b_factor):
+    thickness = top - bottom
+    a_factor = (3300.0 - 2670.0) / (1 - np.exp(-b_factor))
+    constant = 3300.0 - a_factor
+    return lambda radius: a_factor * np.exp(-b_factor * (radius - bottom) / thickness) + constant
+
+
+def variable_shell(bottom, top, shape=(6, 12)):
+    n_lat, n_lon = shape
+    longitude = np.linspace(-180, 180, n_lon + 1)
+    latitude = np.linspace(-90, 90, n_lat + 1)
+    return np.array([[w, e, s, n, bottom, top]
+                     for w, e in zip(longitude[:-1], longitude[1:])
+                     for s, n in zip(latitude[:-1], latitude[1:])])
+
+
+def variable_cases():
+    """(name, coordinates, tesseroids, density function)."""
+    top = 6371e3
+    bottom = top - 1e3
+    shell = variable_shell(bottom, top)
+    pts = np.array([[10.0, -35.0, 120.0, 10.0, -35.0, 120.0],
+                    [5.0, 42.0, -61.0, 5.0, 42.0, -61.0],
+                    [top + 1e3, top + 5e3, top + 20e3, top, top, top]])
+    single = np.array([[-3.0, 3.0, -2.0, 2.0, 5400e3, 6300e3]])
+    spts = np.array([[0.0, 2.5, -4.0], [0.0, 1.0, 3.5], [6300e3, 6300e3 + 1e3, 6300e3 + 50e3]])
+    return [
+        ("linear_shell", pts, shell, linear_shell_density(top, bottom)),
+        ("exponential_shell", pts, shell, exponential_shell_density(top, bottom, 5)),
+        ("single_constant_fn", spts, single, lambda radius: 2900.0),
+    ]
+
+
 def main(root):
     tg, tu = load_reference(root)
+    import importlib  # noqa: PLC0415
+
+    tv = importlib.import_module("harmonica._forward._tesseroid_variable_density")
+    var = {}
+    var_names = []
+    for name, coords, tess, fn in variable_cases():
+        for field in ("potential", "g_z"):
+            t0 = time.time()
+            res = tg.tesseroid_gravity(tuple(coords), tess, fn, field=field, parallel=False)
+            key = f"{name}_{field}"
+            var_names.append(key)
+            var[f"{key}_coords"] = coords
+            var[f"{key}_tesseroids"] = tess
+            var[f"{key}_result"] = np.asarray(res, dtype=np.float64).ravel()
+            print(f"{key}: {time.time() - t0:.2f} s", file=sys.stderr)
+    # density-based discretization of single tesseroids
+    var["split_quadratic"] = np.array(
+        tv._density_based_discretization((-3, 2, -4, 5, 2e3, 5e3), quadratic_density), dtype=float)
+    for b in (5, 100):
+        t = (0.0, 30.0, 0.0, 30.0, 6371e3 - 1e3, 6371e3)
+        var[f"split_exponential_{b}"] = np.array(
+            tv._density_based_discretization(t, exponential_shell_density(t[5], t[4], b)),
+            dtype=float)
+    var["names"] = np.array(var_names)
+    np.savez_compressed(os.path.join(HERE, "reference_tesseroid_variable.npz"), **var)
     store = {}
     names = []
     for name, coords, tess, dens, radial, disable in cases():

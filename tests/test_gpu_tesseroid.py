@@ -34,9 +34,18 @@ from oracle import tesseroid_oracle as to  # noqa: E402
 from test_tesseroid_host import (  # noqa: E402
     ACCURACY_THRESHOLD,
     MEAN_RADIUS,
+    _var_golden,
+    analytic_shell_exponential,
+    analytic_shell_linear,
+    exponential_shell_density,
     golden_case,
     golden_keys,
+    linear_shell_density,
     shell,
+    shell_surface_points,
+    variable_density_fn,
+    variable_keys,
+    variable_shell,
 )
 
 pytestmark = pytest.mark.gpu
@@ -176,10 +185,67 @@ def test_gpu_invalid_density_array():
         hg.tesseroid_gravity([0, 0, 250], tess, [1000, 2000], field="potential")
 
 
-def test_gpu_callable_density_not_supported():
-    with pytest.raises(NotImplementedError, match="Variable-density"):
+def test_gpu_variable_density_radial_not_supported():
+    with pytest.raises(NotImplementedError, match="radial_adaptive_discretization"):
         hg.tesseroid_gravity([0, 0, 250], [-10, 10, -10, 10, 100, 200], lambda r: 1.0,
-                             field="potential")
+                             field="potential", radial_adaptive_discretization=True)
+
+
+@pytest.mark.parametrize("key", variable_keys())
+def test_gpu_variable_density_matches_reference(key):
+    """Density functions (density-based discretization on the host, density
+    per radial node on the GPU) against harmonica's own results; points on
+    the shell's top face take the on-face tolerance."""
+    g = _var_golden()
+    name = key.rsplit("_", 2)[0] if key.endswith("g_z") else key.rsplit("_", 1)[0]
+    field = "g_z" if key.endswith("g_z") else "potential"
+    coords = tuple(g[f"{key}_coords"])
+    tess = g[f"{key}_tesseroids"]
+    got = hg.tesseroid_gravity(coords, tess, variable_density_fn(name), field=field).ravel()
+    expected = g[f"{key}_result"]
+    on_face = np.isin(coords[2], tess[:, 5])
+    npt.assert_allclose(got[~on_face], expected[~on_face], rtol=NEAR_RTOL)
+    npt.assert_allclose(got[on_face], expected[on_face], rtol=SURFACE_RTOL)
+
+
+@pytest.mark.parametrize("field", ["potential", "g_z"])
+def test_gpu_single_tesseroid_against_constant_density(field):
+    """test/test_tesseroid_variable_density.py:321-355."""
+    bottom, top = 5400e3, 6300e3
+    tess = [-3, 3, -2, 2, bottom, top]
+    lon, lat = np.meshgrid(np.arange(-5, 5.1, 1.0), np.arange(-5, 5.1, 1.0))
+    coords = (lon, lat, np.full(lon.shape, top))
+    npt.assert_allclose(hg.tesseroid_gravity(coords, [tess], [2900.0], field=field),
+                        hg.tesseroid_gravity(coords, [tess], lambda r: 2900.0, field=field))
+
+
+@pytest.mark.parametrize("field", ["potential", "g_z"])
+@pytest.mark.parametrize("thickness", [1e2, 1e3, 1e6])
+def test_gpu_shell_linear_density(field, thickness):
+    """test/test_tesseroid_variable_density.py:441-479."""
+    top = 6371e3
+    bottom = top - thickness
+    slope = (2500.0 - 3300.0) / (top - bottom)
+    constant = 2500.0 - slope * top
+    got = hg.tesseroid_gravity(shell_surface_points(top), variable_shell(bottom, top),
+                               linear_shell_density(top, bottom), field=field)
+    npt.assert_allclose(got, analytic_shell_linear(top, bottom, top, slope, constant)[field],
+                        rtol=ACCURACY_THRESHOLD)
+
+
+@pytest.mark.parametrize("field", ["potential", "g_z"])
+@pytest.mark.parametrize("thickness", [1e2, 1e3, 1e6])
+@pytest.mark.parametrize("b_factor", [5, 100])
+def test_gpu_shell_exponential_density(field, thickness, b_factor):
+    """test/test_tesseroid_variable_density.py:482-525."""
+    top = 6371e3
+    bottom = top - thickness
+    a_factor = (3300.0 - 2670.0) / (1 - np.exp(-b_factor))
+    constant = 3300.0 - a_factor
+    got = hg.tesseroid_gravity(shell_surface_points(top), variable_shell(bottom, top),
+                               exponential_shell_density(top, bottom, b_factor), field=field)
+    expected = analytic_shell_exponential(top, bottom, top, a_factor, b_factor, constant)[field]
+    npt.assert_allclose(got, expected, rtol=ACCURACY_THRESHOLD)
 
 
 INSIDE = re.escape("Found computation point(s) inside tesseroid(s)")

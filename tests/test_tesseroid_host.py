@@ -246,3 +246,161 @@ def test_discard_null_tesseroids_oracle():
     t, d = to.discard_null_tesseroids(tess, dens)
     npt.assert_allclose(t, tess[[0, 5, 7]])
     npt.assert_allclose(d, [2400, 2800, 3000])
+
+
+# ------------------------------------------------------ variable density
+GOLDEN_VAR = os.path.join(os.path.dirname(__file__), "golden",
+                          "reference_tesseroid_variable.npz")
+
+
+def _var_golden():
+    return np.load(GOLDEN_VAR)
+
+
+def quadratic_density(radius):
+    """test/test_tesseroid_variable_density.py:59-109 (factor 1e-3, vertex
+    (3e3, 1900))."""
+    return 1e-3 * (radius - 3e3) ** 2 + 1900.0
+
+
+def linear_shell_density(top, bottom):
+    slope = (2500.0 - 3300.0) / (top - bottom)
+    constant = 2500.0 - slope * top
+    return lambda radius: slope * radius + constant
+
+
+def exponential_shell_density(top, bottom, b_factor):
+    thickness = top - bottom
+    a_factor = (3300.0 - 2670.0) / (1 - np.exp(-b_factor))
+    constant = 3300.0 - a_factor
+    return lambda radius: a_factor * np.exp(-b_factor * (radius - bottom) / thickness) + constant
+
+
+def variable_density_fn(name):
+    top = 6371e3
+    return {"linear_shell": linear_shell_density(top, top - 1e3),
+            "exponential_shell": exponential_shell_density(top, top - 1e3, 5),
+            "single_constant_fn": lambda radius: 2900.0}[name]
+
+
+def variable_keys():
+    return [str(k) for k in _var_golden()["names"]]
+
+
+def node_densities(tesseroids, fn):
+    """The density function at radius_p of the two radial nodes
+    (_tesseroid_variable_density.py:87-90), written out independently."""
+    x = np.polynomial.legendre.leggauss(2)[0]
+    return np.array([[fn(0.5 * (t - b) * x[k] + 0.5 * (t + b)) for k in range(2)]
+                     for b, t in tesseroids[:, 4:6]])
+
+
+def test_density_based_discretization_matches_reference():
+    g = _var_golden()
+    got = np.array(ht._density_based_discretization((-3, 2, -4, 5, 2e3, 5e3), quadratic_density),
+                   dtype=float)
+    npt.assert_array_equal(got, g["split_quadratic"])
+    # test/test_tesseroid_variable_density.py:223-248: two tesseroids, split at
+    # the analytic radius of the largest departure from the chord
+    slope = (quadratic_density(5e3) - quadratic_density(2e3)) / 3e3
+    npt.assert_allclose(got[0, 4], 0.5 * slope / 1e-3 + 3e3)
+    for b in (5, 100):
+        t = (0.0, 30.0, 0.0, 30.0, 6371e3 - 1e3, 6371e3)
+        got = np.array(ht._density_based_discretization(
+            t, exponential_shell_density(t[5], t[4], b)), dtype=float)
+        npt.assert_array_equal(got, g[f"split_exponential_{b}"])
+
+
+def test_density_based_discretization_cases(monkeypatch):
+    """test/test_tesseroid_variable_density.py:251-318."""
+    tess = [-3, 2, -4, 5, 30, 50]
+    assert len(ht._density_based_discretization(tess, lambda r: 3 * r + 2)) == 1
+    assert len(ht._density_based_discretization(tess, lambda r: 3)) == 1
+    splits = []
+    for delta in (1e-3, 1e-2, 1e-1, 1e0):
+        monkeypatch.setattr(ht, "DELTA_RATIO", delta)
+        splits.append(len(ht._density_based_discretization((-3, 2, -4, 5, 2e3, 5e3),
+                                                           quadratic_density)))
+    assert (np.diff(splits) < 0).all()
+
+
+@pytest.mark.parametrize("key", variable_keys())
+def test_oracle_variable_density_matches_reference(key):
+    """The oracle on the host discretization reproduces harmonica's
+    variable-density results bit for bit."""
+    g = _var_golden()
+    name = key.rsplit("_", 2)[0] if key.endswith("g_z") else key.rsplit("_", 1)[0]
+    field = "g_z" if key.endswith("g_z") else "potential"
+    fn = variable_density_fn(name)
+    tess = ht.density_based_discretization(g[f"{key}_tesseroids"], fn)
+    got = to.tesseroid_gravity(tuple(g[f"{key}_coords"]), tess, None, field,
+                               node_density=node_densities(tess, fn))
+    npt.assert_allclose(got.ravel(), g[f"{key}_result"], rtol=1e-14, atol=0)
+
+
+def analytic_shell_linear(radius, bottom, top, slope, constant):
+    """test/test_tesseroid_variable_density.py:358-372."""
+    g = 6.6743e-11
+    c = np.pi * g * slope * (top**4 - bottom**4) + 4 / 3 * np.pi * g * constant * (
+        top**3 - bottom**3)
+    potential = c / radius
+    return {"potential": potential, "g_z": 1e5 * potential / radius}
+
+
+def analytic_shell_exponential(radius, bottom, top, a_factor, b_factor, constant):
+    """test/test_tesseroid_variable_density.py:375-409."""
+    g = 6.6743e-11
+    thickness = top - bottom
+    k = b_factor / thickness
+    potential = (4 * np.pi * g * a_factor / k**3 / radius * (
+        ((bottom * k) ** 2 + 2 * bottom * k + 2)
+        - ((top * k) ** 2 + 2 * top * k + 2) * np.exp(-k * thickness))
+        + 4 / 3 * np.pi * g * constant * (top**3 - bottom**3) / radius)
+    return {"potential": potential, "g_z": 1e5 * potential / radius}
+
+
+def variable_shell(bottom, top, shape=(6, 12)):
+    n_lat, n_lon = shape
+    longitude = np.linspace(-180, 180, n_lon + 1)
+    latitude = np.linspace(-90, 90, n_lat + 1)
+    return np.array([[w, e, s, n, bottom, top]
+                     for w, e in zip(longitude[:-1], longitude[1:], strict=True)
+                     for s, n in zip(latitude[:-1], latitude[1:], strict=True)])
+
+
+def shell_surface_points(top):
+    lon, lat = np.meshgrid(np.linspace(-180, 180, 13), np.linspace(-90, 90, 19))
+    return (lon, lat, np.full(lon.shape, top))
+
+
+@pytest.mark.parametrize("field", ["potential", "g_z"])
+@pytest.mark.parametrize("thickness", [1e2, 1e3, 1e6])
+def test_oracle_shell_linear_density(field, thickness):
+    """test/test_tesseroid_variable_density.py:441-479 on the oracle."""
+    top = 6371e3
+    bottom = top - thickness
+    slope = (2500.0 - 3300.0) / (top - bottom)
+    constant = 2500.0 - slope * top
+    fn = linear_shell_density(top, bottom)
+    tess = ht.density_based_discretization(variable_shell(bottom, top), fn)
+    coords = shell_surface_points(top)
+    got = to.tesseroid_gravity(coords, tess, None, field, node_density=node_densities(tess, fn))
+    npt.assert_allclose(got, analytic_shell_linear(top, bottom, top, slope, constant)[field],
+                        rtol=ACCURACY_THRESHOLD)
+
+
+@pytest.mark.parametrize("field", ["potential", "g_z"])
+@pytest.mark.parametrize("thickness", [1e2, 1e3, 1e6])
+@pytest.mark.parametrize("b_factor", [5, 100])
+def test_oracle_shell_exponential_density(field, thickness, b_factor):
+    """test/test_tesseroid_variable_density.py:482-525 on the oracle."""
+    top = 6371e3
+    bottom = top - thickness
+    a_factor = (3300.0 - 2670.0) / (1 - np.exp(-b_factor))
+    constant = 3300.0 - a_factor
+    fn = exponential_shell_density(top, bottom, b_factor)
+    tess = ht.density_based_discretization(variable_shell(bottom, top), fn)
+    coords = shell_surface_points(top)
+    got = to.tesseroid_gravity(coords, tess, None, field, node_density=node_densities(tess, fn))
+    expected = analytic_shell_exponential(top, bottom, top, a_factor, b_factor, constant)[field]
+    npt.assert_allclose(got, expected, rtol=ACCURACY_THRESHOLD)
