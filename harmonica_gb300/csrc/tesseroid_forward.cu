@@ -18,20 +18,21 @@
 // expensive pairs instead of idling behind one of them.  Queued pairs are
 // added to their point's sum in list order: results are deterministic.
 //
-// Arithmetic.  The split decisions and every small tesseroid of a split pair
-// are FP64 in the reference's operation order without contraction into fused
-// multiply-adds (__dmul_rn / __dadd_rn), so they differ from the reference
-// only through the last bits of cos/sin/acos.  The split test
-// distance / size < ratio is evaluated exactly whenever an FP32 pre-test on
-// the Cartesian distance to the centre, with a rigorous error margin, does
-// not already prove "no split".  Unsplit tesseroids -- nearly all pairs --
-// are summed by glq_sum_pairs on float pairs packed two nodes per float2
-// (FFMA2/FADD2/FMUL2): the Cartesian difference of the point and each node
-// (48-bit coordinates), 1 / l from a float-pair reciprocal square root, and
-// for g_z the radial component P . (P - Q) / r, which avoids the
-// 1 - cos(psi) cancellation of the reference's formula; the pair's sum
-// returns to FP64 for the accumulation.  The FP64 pipe, 1/64 of the FP32
-// rate on this GPU, then does almost nothing on the common path.
+// Arithmetic.  The split decisions follow the reference's operation order
+// in FP64 without contraction into fused multiply-adds (__dmul_rn /
+// __dadd_rn), so they differ from the reference only through the last bits
+// of cos/sin/acos; so do the point-mass positions and masses of every
+// tesseroid (glq_nodes).  The split test distance / size < ratio is
+// evaluated exactly whenever an FP32 pre-test on the Cartesian distance to
+// the centre, with a rigorous error margin, does not already prove "no
+// split".  The point masses are summed by glq_sum_pairs on float pairs
+// packed two nodes per float2 (FFMA2/FADD2/FMUL2): the Cartesian difference
+// of the point and each node (48-bit coordinates), 1 / l from a float-pair
+// reciprocal square root, and for g_z the radial component
+// (l^2 + (r - r_p)(r + r_p)) / (2 r), which avoids the 1 - cos(psi)
+// cancellation of the reference's formula; each tesseroid's sum returns to
+// FP64 for the accumulation.  The FP64 pipe, 1/64 of the FP32 rate on this
+// GPU, then does almost nothing on the common path.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -191,45 +192,6 @@ __device__ __forceinline__ void glq_nodes(const double* t, const double* density
     }
 }
 
-// Sum of the 8 point masses at one point (the loop of
-// gauss_legendre_quadrature with potential_spherical / gravity_u_spherical,
-// point.py:323-354).  FIELD 0: potential; 1: radial (upward) acceleration, SI.
-template <int FIELD>
-__device__ __forceinline__ double glq_eval(const Station& p, const double* lon_n,
-                                           const double* cphi_n, const double* sphi_n,
-                                           const double* r_n, const double* mass) {
-  double coslambda[2];
-#pragma unroll
-  for (int i = 0; i < 2; i++) coslambda[i] = cos(sub(lon_n[i], p.lon));
-  const double two_r = mul(2.0, p.r);
-  double result = 0.0;
-#pragma unroll
-  for (int j = 0; j < 2; j++) {
-    const double s_term = mul(sphi_n[j], p.sphi);
-    const double c_term = mul(cphi_n[j], p.cphi);
-#pragma unroll
-    for (int k = 0; k < 2; k++) {
-      const double dr = sub(p.r, r_n[k]);
-      const double dr2 = mul(dr, dr);
-      const double rr = mul(two_r, r_n[k]);
-#pragma unroll
-      for (int i = 0; i < 2; i++) {
-        const double cospsi = add(s_term, mul(c_term, coslambda[i]));
-        const double dist = sqrt(add(dr2, mul(rr, sub(1.0, cospsi))));
-        double kern;
-        if (FIELD == 0) {
-          kern = mul(1.0 / dist, kG);
-        } else {
-          const double delta_z = sub(p.r, mul(r_n[k], cospsi));
-          kern = mul(-kG, delta_z) / mul(mul(dist, dist), dist);
-        }
-        result = add(result, mul(mass[(j * 2 + k) * 2 + i], kern));
-      }
-    }
-  }
-  return result;
-}
-
 // distance / size < ratio, exactly as the reference evaluates it.
 __device__ __forceinline__ bool split_axis(double d, double size, double ratio) {
   return d / size < ratio;
@@ -308,7 +270,8 @@ __device__ __forceinline__ P2 p2_norm2(P2 x, P2 y, P2 z) {
 // l^2 = |P - Q|^2 from the Cartesian difference (no 1 - cos(psi)
 // cancellation), 1 / l by p2_rsqrt, and for g_z the radial component
 // r - r_p cos(psi) = P . (P - Q) / r = (l^2 + (r - r_p)(r + r_p)) / (2 r).
-// The same point masses and kernels as glq_eval; each term within a few
+// The point masses of gauss_legendre_quadrature with the kernels
+// potential_spherical / gravity_u_spherical (point.py:323-354); each term within a few
 // units of 2^-46 of its exact value (the reference's own terms carry the
 // rounding of 1 - cos(psi), which is larger).  UNROLL: loop unrolling (1
 // keeps the code small).
