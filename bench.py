@@ -608,6 +608,9 @@ def run_tesseroids(args, rank, world, local):
     dev = torch.device("cuda", local)
     L = synthetic.tesseroid_layer_andes()
     tess, dens, coords = L["tesseroids"], L["density"], L["coordinates"]
+    if world > 1:  # each rank takes a contiguous share of the points (no collective)
+        lo, hi = rank * coords[0].size // world, (rank + 1) * coords[0].size // world
+        coords = tuple(c[lo:hi] for c in coords)
     n_obs, m = coords[0].size, tess.shape[0]
     T = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).to(dev)  # noqa: E731
     c = [T(x) for x in coords]
@@ -641,6 +644,13 @@ def run_tesseroids(args, rank, world, local):
     step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
     dev_time = sum(step_ms) * 1e-3
     pairs = n_obs * m * args.steps
+    if world > 1:
+        t = torch.tensor([dev_time, float(pairs)], dtype=torch.float64, device=dev)
+        if not torch.distributed.is_initialized():
+            torch.distributed.init_process_group("nccl", device_id=dev)
+        torch.distributed.all_reduce(t[:1], op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(t[1:])
+        dev_time, pairs = float(t[0].item()), int(t[1].item())
     value = pairs / dev_time
 
     e2e = None
