@@ -20,6 +20,7 @@ from ._native import build
 from .adjoint import layer_gravity_torch, prism_gravity_torch
 from .batch import PrismBatch, autotune, prism_gravity_batch
 from .device_layer import DevicePrismLayer, prism_layer_device
+from .equivalent_sources import EquivalentSources, EquivalentSourcesSph
 from .fields import FIELDS
 from .gravity import check_prisms, prism_gravity, prism_gravity_fields
 from .layer import DatasetAccessorPrismLayer, PrismLayer, prism_layer
@@ -30,6 +31,8 @@ from .tesseroid_layer import DatasetAccessorTesseroidLayer, TesseroidLayer, tess
 
 __all__ = [
     "DevicePrismLayer",
+    "EquivalentSources",
+    "EquivalentSourcesSph",
     "prism_layer_device",
     "FIELDS",
     "PrismBatch",

@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(kThreads) point_kernel(
     const double* __restrict__ c1, const double* __restrict__ c2, const double* __restrict__ c3,
     int64_t n_obs, const double* __restrict__ p1, const double* __restrict__ p2,
     const double* __restrict__ p3, const double* __restrict__ mass, int64_t n_points,
-    int64_t chunk, double* __restrict__ dst, int64_t dst_chunk_stride, int scale_output) {
+    int64_t chunk, double* __restrict__ dst, int64_t dst_chunk_stride, double out_scale) {
   __shared__ PointTile sh;
   const int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x;
   const bool active = i < n_obs;
@@ -110,7 +110,50 @@ __global__ void __launch_bounds__(kThreads) point_kernel(
     }
   }
   if (!active) return;
-  dst[(int64_t)blockIdx.y * dst_chunk_stride + i] = scale_output ? acc * field_scale(F) : acc;
+  dst[(int64_t)blockIdx.y * dst_chunk_stride + i] = acc * out_scale;
+}
+
+// One row block of the equivalent-source Jacobian: jac[i][j] = 1 / l(i, j),
+// greens_func_cartesian / greens_func_spherical (src/harmonica/
+// _equivalent_sources/cartesian.py:635-644, spherical.py:413-424) filled by
+// the loop of jacobian (_equivalent_sources/utils.py:54-74).  Threads run
+// along the sources, so each row is written in coalesced 256-byte pieces;
+// a block covers kJacRows points.
+constexpr int kJacRows = 8;
+
+template <int SPH>
+__global__ void __launch_bounds__(kThreads) jacobian_kernel(
+    const double* __restrict__ c1, const double* __restrict__ c2, const double* __restrict__ c3,
+    int64_t n_obs, const double* __restrict__ p1, const double* __restrict__ p2,
+    const double* __restrict__ p3, int64_t n_points, double* __restrict__ jac) {
+  const int64_t j = (int64_t)blockIdx.x * kThreads + threadIdx.x;
+  if (j >= n_points) return;
+  double a = p1[j], b = p2[j], c = p3[j];
+  if (SPH) {
+    double sp, cp;
+    sincos(b * kDeg, &sp, &cp);
+    a *= kDeg;
+    b = cp;
+    c = sp;
+  }
+  const double rp = SPH ? p3[j] : 0.0;
+  const int64_t i0 = (int64_t)blockIdx.y * kJacRows;
+  const int64_t i1 = min(i0 + kJacRows, n_obs);
+  for (int64_t i = i0; i < i1; i++) {
+    double l2;
+    if (SPH) {
+      double sphi, cphi;
+      sincos(c2[i] * kDeg, &sphi, &cphi);
+      const double r = c3[i];
+      const double cospsi = c * sphi + b * cphi * cos(a - c1[i] * kDeg);
+      const double dr = r - rp;
+      l2 = dr * dr + 2.0 * r * rp * (1.0 - cospsi);
+    } else {
+      const double dx = c1[i] - a, dy = c2[i] - b, dz = c3[i] - c;
+      l2 = fma(dx, dx, fma(dy, dy, dz * dz));
+    }
+    jac[i * n_points + j] = lean::lm_rsqrt(l2);
+  }
 }
 
 struct PointPlan {
@@ -133,10 +176,13 @@ PointPlan point_plan(int64_t n_obs, int64_t n_points) {
   return p;
 }
 
+// unit: the sum of m / l without G (the equivalent-source prediction,
+// _equivalent_sources/utils.py:77-96); only for the potential kernel.
 template <int SPH>
 int launch_point(int field, const double* c1, const double* c2, const double* c3, int64_t n_obs,
                  const double* p1, const double* p2, const double* p3, const double* m,
-                 int64_t n_points, double* out, void* ws, size_t ws_bytes, cudaStream_t st) {
+                 int64_t n_points, double* out, void* ws, size_t ws_bytes, cudaStream_t st,
+                 bool unit = false) {
   const PointPlan plan = point_plan(n_obs, n_points);
   if (n_obs == 0) return HG_OK;
   if (n_points == 0)
@@ -145,13 +191,14 @@ int launch_point(int field, const double* c1, const double* c2, const double* c3
   if (!direct && (!ws || ws_bytes < plan.bytes))
     return set_error(HG_ERR_INVALID, "workspace missing or too small");
   double* dst = direct ? out : static_cast<double*>(ws);
+  const double scale = unit ? 1.0 : field_scale(field);
   dim3 grid((unsigned)plan.tiles, (unsigned)plan.n_chunks);
   switch (field) {
 #define HG_PT(FF)                                                                              \
   case FF:                                                                                     \
     point_kernel<FF, SPH><<<grid, kThreads, 0, st>>>(c1, c2, c3, n_obs, p1, p2, p3, m,        \
                                                       n_points, plan.chunk, dst, n_obs,        \
-                                                      direct ? 1 : 0);                         \
+                                                      direct ? scale : 1.0);                   \
     break;
     HG_PT(0) HG_PT(1) HG_PT(2) HG_PT(3) HG_PT(4) HG_PT(5) HG_PT(6) HG_PT(7) HG_PT(8) HG_PT(9)
 #undef HG_PT
@@ -159,7 +206,7 @@ int launch_point(int field, const double* c1, const double* c2, const double* c3
   }
   int rc = cuda_check(cudaGetLastError(), "point_kernel launch");
   if (rc != HG_OK || direct) return rc;
-  launch_chunk_sum(dst, plan.n_chunks, n_obs, n_obs, field_scale(field), out, st);
+  launch_chunk_sum(dst, plan.n_chunks, n_obs, n_obs, scale, out, st);
   return cuda_check(cudaGetLastError(), "chunk_sum_kernel launch");
 }
 
@@ -195,6 +242,54 @@ int hg_point_forward(const double* obs_1, const double* obs_2, const double* obs
                            n_points, out, workspace, workspace_bytes, st);
   return launch_point<0>(field, obs_1, obs_2, obs_3, n_obs, pts_1, pts_2, pts_3, masses,
                          n_points, out, workspace, workspace_bytes, st);
+}
+
+int hg_eqs_jacobian(const double* obs_1, const double* obs_2, const double* obs_3, int64_t n_obs,
+                    const double* pts_1, const double* pts_2, const double* pts_3,
+                    int64_t n_points, int32_t spherical, double* jac, void* stream) {
+  if (n_obs < 0 || n_points < 0) return set_error(HG_ERR_INVALID, "bad sizes");
+  if (n_obs == 0 || n_points == 0) return HG_OK;
+  if (!obs_1 || !obs_2 || !obs_3 || !pts_1 || !pts_2 || !pts_3 || !jac)
+    return set_error(HG_ERR_INVALID, "null pointer");
+  const int64_t col_blocks = (n_points + kThreads - 1) / kThreads;
+  const int64_t row_blocks = (n_obs + kJacRows - 1) / kJacRows;
+  if (col_blocks > 2147483647LL || row_blocks > 65535LL * 65535LL)
+    return set_error(HG_ERR_INVALID, "Jacobian too large for one launch");
+  cudaStream_t st = (cudaStream_t)stream;
+  // rows in launches of at most 65535 row blocks (the grid's y limit)
+  for (int64_t r0 = 0; r0 < row_blocks; r0 += 65535) {
+    const int64_t nb = min(row_blocks - r0, (int64_t)65535);
+    const int64_t first = r0 * kJacRows;
+    const dim3 grid((unsigned)col_blocks, (unsigned)nb);
+    if (spherical)
+      jacobian_kernel<1><<<grid, kThreads, 0, st>>>(obs_1 + first, obs_2 + first, obs_3 + first,
+                                                    n_obs - first, pts_1, pts_2, pts_3, n_points,
+                                                    jac + first * n_points);
+    else
+      jacobian_kernel<0><<<grid, kThreads, 0, st>>>(obs_1 + first, obs_2 + first, obs_3 + first,
+                                                    n_obs - first, pts_1, pts_2, pts_3, n_points,
+                                                    jac + first * n_points);
+    const int rc = cuda_check(cudaGetLastError(), "jacobian_kernel launch");
+    if (rc != HG_OK) return rc;
+  }
+  return HG_OK;
+}
+
+int hg_eqs_predict(const double* obs_1, const double* obs_2, const double* obs_3, int64_t n_obs,
+                   const double* pts_1, const double* pts_2, const double* pts_3,
+                   const double* coefs, int64_t n_points, int32_t spherical, double* out,
+                   void* workspace, size_t workspace_bytes, void* stream) {
+  if (n_obs < 0 || n_points < 0) return set_error(HG_ERR_INVALID, "bad sizes");
+  if (n_obs > 0 && (!obs_1 || !obs_2 || !obs_3 || !out))
+    return set_error(HG_ERR_INVALID, "null pointer");
+  if (n_points > 0 && (!pts_1 || !pts_2 || !pts_3 || !coefs))
+    return set_error(HG_ERR_INVALID, "null points pointer");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (spherical)
+    return launch_point<1>(kPotential, obs_1, obs_2, obs_3, n_obs, pts_1, pts_2, pts_3, coefs,
+                           n_points, out, workspace, workspace_bytes, st, true);
+  return launch_point<0>(kPotential, obs_1, obs_2, obs_3, n_obs, pts_1, pts_2, pts_3, coefs,
+                         n_points, out, workspace, workspace_bytes, st, true);
 }
 
 }  // extern "C"

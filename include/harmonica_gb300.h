@@ -317,6 +317,27 @@ int hg_point_forward(const double *obs_1, const double *obs_2, const double *obs
 
 /*
  * ---------------------------------------------------------------------------
+ * Equivalent sources (point sources with the Green's function 1 / distance).
+ * hg_eqs_jacobian replaces jacobian_numba_parallel/serial
+ * (src/harmonica/_equivalent_sources/utils.py:54-74) with
+ * greens_func_cartesian (cartesian.py:635-644) or greens_func_spherical
+ * (spherical.py:413-424): jac is n_obs x n_points, row-major, on the device.
+ * hg_eqs_predict replaces predict_numba_parallel/serial (utils.py:77-96):
+ * out[i] = sum_j coefs[j] / distance(i, j); workspace from
+ * hg_point_forward_workspace (NULL when it returns 0).  spherical = 0:
+ * easting, northing, upward (m); 1: longitude, latitude (degrees), radius (m).
+ */
+int hg_eqs_jacobian(const double *obs_1, const double *obs_2, const double *obs_3, int64_t n_obs,
+                    const double *pts_1, const double *pts_2, const double *pts_3,
+                    int64_t n_points, int32_t spherical, double *jac, void *stream);
+
+int hg_eqs_predict(const double *obs_1, const double *obs_2, const double *obs_3, int64_t n_obs,
+                   const double *pts_1, const double *pts_2, const double *pts_3,
+                   const double *coefs, int64_t n_points, int32_t spherical, double *out,
+                   void *workspace, size_t workspace_bytes, void *stream);
+
+/*
+ * ---------------------------------------------------------------------------
  * Tesseroids (spherical prisms) of constant density.  Replaces
  * jit_tesseroid_gravity_parallel/serial (src/harmonica/_forward/
  * tesseroid_gravity.py:236-333) with the adaptive discretisation and
