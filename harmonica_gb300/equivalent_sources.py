@@ -38,8 +38,7 @@ def _device(device):
 def _tensors(arrays, dev):
     import torch  # noqa: PLC0415
 
-    return [torch.from_numpy(np.ascontiguousarray(np.ravel(a), dtype=np.float64)).to(dev)
-            for a in arrays]
+    return [torch.from_numpy(np.array(np.ravel(a), dtype=np.float64)).to(dev) for a in arrays]
 
 
 def greens_jacobian(coordinates, points, spherical=False, device=None, as_tensor=False):

@@ -44,10 +44,12 @@ def test_jacobian_and_predict_vs_oracle(spherical):
     coords, pts, coefs = spherical_case() if spherical else cartesian_case()
     jac = greens_jacobian(coords, pts, spherical=spherical)
     ref = eqs_oracle.jacobian(coords, pts, spherical)
-    npt.assert_allclose(jac, ref, rtol=1e-13 if spherical else 1e-14)
+    # spherical: the distance formula's 1 - cos(psi) turns last-bit differences
+    # of cos into relative ones of up to 2e-16 / (1 - cos(psi)) (~1e-10 here)
+    npt.assert_allclose(jac, ref, rtol=1e-9 if spherical else 1e-14)
     pred = greens_predict(coords, pts, coefs, spherical=spherical)
-    npt.assert_allclose(pred, eqs_oracle.predict(coords, pts, coefs, spherical), rtol=1e-12,
-                        atol=1e-12 * np.abs(pred).max())
+    npt.assert_allclose(pred, eqs_oracle.predict(coords, pts, coefs, spherical),
+                        rtol=1e-9 if spherical else 1e-12, atol=1e-12 * np.abs(pred).max())
 
 
 def test_jacobian_many_rows_and_empty():
