@@ -44,3 +44,39 @@ def test_version_and_error_without_gpu():
     assert b"bad sizes" in lib.hg_last_error()
     assert lib.hg_prism_forward_workspace(10, 10, 0, ctypes.byref(size)) < 0
     assert lib.hg_prism_forward_workspace(2500, 10000, 1 << 3, ctypes.byref(size)) == 0
+
+
+def test_tesseroid_and_eqs_validation_without_gpu():
+    """Argument checks of the tesseroid and equivalent-source entry points
+    (they return before any CUDA call)."""
+    from harmonica_gb300 import _native
+
+    lib = _native.lib()
+    size = ctypes.c_size_t(0)
+    assert lib.hg_tesseroid_forward_workspace(-1, 10, ctypes.byref(size)) < 0
+    assert b"bad sizes" in lib.hg_last_error()
+    assert lib.hg_tesseroid_forward_workspace(100, 1000, ctypes.byref(size)) == 0
+    assert size.value >= 52 * 1000 * 8  # the prepared tesseroid records
+    args = [None, None, None, 1, None, None, 0, 1]
+    # radial, stack size, max discretizations, nodes, weights, out, status,
+    # workspace, workspace bytes, stream
+    tail = [0, 100, 0, None, None, None, None, None, 0, None]
+    # field other than potential (0) or g_z (3)
+    assert lib.hg_tesseroid_forward(*args, 5, *tail) < 0
+    assert b"tesseroid field" in lib.hg_last_error()
+    # stack larger than the kernels' 100 entries
+    tail_big_stack = [0, 101, 0, None, None, None, None, None, 0, None]
+    assert lib.hg_tesseroid_forward(*args, 3, *tail_big_stack) < 0
+    assert b"stack size above 100" in lib.hg_last_error()
+    # null pointers with work to do
+    assert lib.hg_tesseroid_forward(*args, 3, *tail) < 0
+    assert b"null pointer" in lib.hg_last_error()
+    assert lib.hg_tesseroid_inside(None, None, None, 1, None, 1, None, 0, None, None) < 0
+    assert b"null pointer" in lib.hg_last_error()
+    assert lib.hg_eqs_jacobian(None, None, None, -1, None, None, None, 1, 0, None, None) < 0
+    assert b"bad sizes" in lib.hg_last_error()
+    assert lib.hg_eqs_jacobian(None, None, None, 2, None, None, None, 3, 0, None, None) < 0
+    assert b"null pointer" in lib.hg_last_error()
+    assert lib.hg_eqs_predict(None, None, None, 2, None, None, None, None, 3, 0, None, None, 0,
+                              None) < 0
+    assert b"null pointer" in lib.hg_last_error()
