@@ -20,6 +20,7 @@ from ._native import build
 from .adjoint import layer_gravity_torch, prism_gravity_torch
 from .batch import PrismBatch, autotune, prism_gravity_batch
 from .device_layer import DevicePrismLayer, prism_layer_device
+from .dipole import dipole_magnetic
 from .equivalent_sources import EquivalentSources, EquivalentSourcesSph
 from .fields import FIELDS
 from .gravity import check_prisms, prism_gravity, prism_gravity_fields
@@ -31,6 +32,7 @@ from .tesseroid_layer import DatasetAccessorTesseroidLayer, TesseroidLayer, tess
 
 __all__ = [
     "DevicePrismLayer",
+    "dipole_magnetic",
     "EquivalentSources",
     "EquivalentSourcesSph",
     "prism_layer_device",

@@ -113,6 +113,65 @@ __global__ void __launch_bounds__(kThreads) point_kernel(
   dst[(int64_t)blockIdx.y * dst_chunk_stride + i] = acc * out_scale;
 }
 
+// Magnetic field of dipoles (src/harmonica/_forward/dipole.py:23-130,
+// 292-360, with choclo.dipole's closed form): with r = P - Q,
+// b = mu0/(4 pi) (3 (m . r) r / l^5 - m / l^3); the kernel sums
+// (3 (m . r) r_a - m_a l^2) / l^5 and the reduction applies mu0/(4 pi) and
+// nT.  COMP 0/1/2: b_e, b_n, b_u; 3: all three (rows e, n, u).
+struct DipoleTile {
+  double e[kTile], n[kTile], u[kTile], me[kTile], mn[kTile], mu[kTile];
+};
+
+template <int COMP>
+__global__ void __launch_bounds__(kThreads) dipole_kernel(
+    const double* __restrict__ oe, const double* __restrict__ on, const double* __restrict__ ou,
+    int64_t n_obs, const double* __restrict__ de, const double* __restrict__ dn,
+    const double* __restrict__ du, const double* __restrict__ me, const double* __restrict__ mn,
+    const double* __restrict__ mu, int64_t n_dip, int64_t chunk, double* __restrict__ dst,
+    int64_t dst_chunk_stride, double out_scale) {
+  __shared__ DipoleTile sh;
+  const int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x;
+  const bool active = i < n_obs;
+  const double pe = active ? oe[i] : 0.0, pn = active ? on[i] : 0.0, pu = active ? ou[i] : 0.0;
+  double be = 0.0, bn = 0.0, bu = 0.0;
+  const int64_t q0 = (int64_t)blockIdx.y * chunk;
+  const int64_t q1 = min(q0 + chunk, n_dip);
+  for (int64_t base = q0; base < q1; base += kTile) {
+    const int cnt = (int)min((int64_t)kTile, q1 - base);
+    __syncthreads();
+    if ((int)threadIdx.x < cnt) {
+      const int64_t j = base + threadIdx.x;
+      sh.e[threadIdx.x] = de[j];
+      sh.n[threadIdx.x] = dn[j];
+      sh.u[threadIdx.x] = du[j];
+      sh.me[threadIdx.x] = me[j];
+      sh.mn[threadIdx.x] = mn[j];
+      sh.mu[threadIdx.x] = mu[j];
+    }
+    __syncthreads();
+    for (int k = 0; k < cnt; k++) {
+      const double rx = pe - sh.e[k], ry = pn - sh.n[k], rz = pu - sh.u[k];
+      const double l2 = fma(rx, rx, fma(ry, ry, rz * rz));
+      const double inv = lean::lm_rsqrt(l2);
+      const double inv2 = inv * inv;
+      const double inv5 = (inv2 * inv2) * inv;
+      const double mdr3 = 3.0 * fma(sh.me[k], rx, fma(sh.mn[k], ry, sh.mu[k] * rz));
+      if (COMP == 0 || COMP == 3) be = fma(fma(mdr3, rx, -sh.me[k] * l2), inv5, be);
+      if (COMP == 1 || COMP == 3) bn = fma(fma(mdr3, ry, -sh.mn[k] * l2), inv5, bn);
+      if (COMP == 2 || COMP == 3) bu = fma(fma(mdr3, rz, -sh.mu[k] * l2), inv5, bu);
+    }
+  }
+  if (!active) return;
+  double* d = dst + (int64_t)blockIdx.y * dst_chunk_stride;
+  if (COMP == 3) {
+    d[i] = be * out_scale;
+    d[n_obs + i] = bn * out_scale;
+    d[2 * n_obs + i] = bu * out_scale;
+  } else {
+    d[i] = (COMP == 0 ? be : (COMP == 1 ? bn : bu)) * out_scale;
+  }
+}
+
 // One row block of the equivalent-source Jacobian: jac[i][j] = 1 / l(i, j),
 // greens_func_cartesian / greens_func_spherical (src/harmonica/
 // _equivalent_sources/cartesian.py:635-644, spherical.py:413-424) filled by
@@ -242,6 +301,53 @@ int hg_point_forward(const double* obs_1, const double* obs_2, const double* obs
                            n_points, out, workspace, workspace_bytes, st);
   return launch_point<0>(field, obs_1, obs_2, obs_3, n_obs, pts_1, pts_2, pts_3, masses,
                          n_points, out, workspace, workspace_bytes, st);
+}
+
+int hg_dipole_workspace(int64_t n_obs, int64_t n_dipoles, int32_t component, size_t* bytes) {
+  if (!bytes || n_obs < 0 || n_dipoles < 0 || component < 0 || component > 3)
+    return set_error(HG_ERR_INVALID, "bad arguments");
+  const PointPlan p = point_plan(n_obs, n_dipoles);
+  *bytes = p.n_chunks > 1 ? p.bytes * (component == 3 ? 3 : 1) : 0;
+  return HG_OK;
+}
+
+int hg_dipole_magnetic(const double* obs_e, const double* obs_n, const double* obs_u,
+                       int64_t n_obs, const double* dip_e, const double* dip_n,
+                       const double* dip_u, const double* m_e, const double* m_n,
+                       const double* m_u, int64_t n_dipoles, int32_t component, double* out,
+                       void* workspace, size_t workspace_bytes, void* stream) {
+  if (n_obs < 0 || n_dipoles < 0 || component < 0 || component > 3)
+    return set_error(HG_ERR_INVALID, "bad sizes or component");
+  if (n_obs == 0) return HG_OK;
+  if (!obs_e || !obs_n || !obs_u || !out) return set_error(HG_ERR_INVALID, "null pointer");
+  if (n_dipoles > 0 && (!dip_e || !dip_n || !dip_u || !m_e || !m_n || !m_u))
+    return set_error(HG_ERR_INVALID, "null dipole pointer");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int rows = component == 3 ? 3 : 1;
+  if (n_dipoles == 0)
+    return cuda_check(cudaMemsetAsync(out, 0, sizeof(double) * rows * n_obs, st),
+                      "cudaMemsetAsync");
+  const PointPlan plan = point_plan(n_obs, n_dipoles);
+  const bool direct = plan.n_chunks == 1;
+  const size_t need = direct ? 0 : plan.bytes * rows;
+  if (!direct && (!workspace || workspace_bytes < need))
+    return set_error(HG_ERR_INVALID, "workspace missing or too small");
+  // mu0 / (4 pi) = 1e-7 H/m, results in nT (dipole.py:193-195)
+  const double scale = 1e-7 * 1e9;
+  double* dst = direct ? out : static_cast<double*>(workspace);
+  const int64_t cstride = (int64_t)rows * n_obs;
+  const dim3 grid((unsigned)plan.tiles, (unsigned)plan.n_chunks);
+  const double sc = direct ? scale : 1.0;
+  switch (component) {
+    case 0: dipole_kernel<0><<<grid, kThreads, 0, st>>>(obs_e, obs_n, obs_u, n_obs, dip_e, dip_n, dip_u, m_e, m_n, m_u, n_dipoles, plan.chunk, dst, cstride, sc); break;
+    case 1: dipole_kernel<1><<<grid, kThreads, 0, st>>>(obs_e, obs_n, obs_u, n_obs, dip_e, dip_n, dip_u, m_e, m_n, m_u, n_dipoles, plan.chunk, dst, cstride, sc); break;
+    case 2: dipole_kernel<2><<<grid, kThreads, 0, st>>>(obs_e, obs_n, obs_u, n_obs, dip_e, dip_n, dip_u, m_e, m_n, m_u, n_dipoles, plan.chunk, dst, cstride, sc); break;
+    default: dipole_kernel<3><<<grid, kThreads, 0, st>>>(obs_e, obs_n, obs_u, n_obs, dip_e, dip_n, dip_u, m_e, m_n, m_u, n_dipoles, plan.chunk, dst, cstride, sc); break;
+  }
+  int rc = cuda_check(cudaGetLastError(), "dipole_kernel launch");
+  if (rc != HG_OK || direct) return rc;
+  launch_chunk_sum(dst, plan.n_chunks, cstride, cstride, scale, out, st);
+  return cuda_check(cudaGetLastError(), "chunk_sum_kernel launch");
 }
 
 int hg_eqs_jacobian(const double* obs_1, const double* obs_2, const double* obs_3, int64_t n_obs,

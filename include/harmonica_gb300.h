@@ -317,6 +317,22 @@ int hg_point_forward(const double *obs_1, const double *obs_2, const double *obs
 
 /*
  * ---------------------------------------------------------------------------
+ * Magnetic dipoles.  Replaces the loops behind dipole_magnetic
+ * (src/harmonica/_forward/dipole.py:23-130, 292-360): b = mu0/(4 pi)
+ * (3 (m . r) r / |r|^5 - m / |r|^3), r = point - dipole, in nT.
+ * Coordinates in m (easting, northing, upward), moments in A m^2.
+ * component: 0 b_e, 1 b_n, 2 b_u, 3 all three (out: rows e, n, u of n_obs).
+ */
+int hg_dipole_workspace(int64_t n_obs, int64_t n_dipoles, int32_t component, size_t *bytes);
+
+int hg_dipole_magnetic(const double *obs_e, const double *obs_n, const double *obs_u,
+                       int64_t n_obs, const double *dip_e, const double *dip_n,
+                       const double *dip_u, const double *m_e, const double *m_n,
+                       const double *m_u, int64_t n_dipoles, int32_t component, double *out,
+                       void *workspace, size_t workspace_bytes, void *stream);
+
+/*
+ * ---------------------------------------------------------------------------
  * Equivalent sources (point sources with the Green's function 1 / distance).
  * hg_eqs_jacobian replaces jacobian_numba_parallel/serial
  * (src/harmonica/_equivalent_sources/utils.py:54-74) with
