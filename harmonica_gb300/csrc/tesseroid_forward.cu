@@ -197,17 +197,6 @@ __device__ __forceinline__ bool split_axis(double d, double size, double ratio) 
   return d / size < ratio;
 }
 
-// 1 / sqrt(x) lane by lane for x > 0 normal: FP32 seed, one Newton step with
-// its second-order term, the residual 1 - x y^2 on float pairs.
-__device__ __forceinline__ P2 p2_rsqrt(P2 x) {
-  using namespace lean;
-  const float2 y = mk2(rsqrt_approx(x.h.x), rsqrt_approx(x.h.y));
-  const P2 xy2 = p2_mul(x, two_prod2(y, y));
-  const float2 r = sub2(sub2(sp2(1.0f), xy2.h), xy2.l);
-  const float2 c = mul2(r, fma2(sp2(0.375f), r, sp2(0.5f)));
-  return P2{y, mul2(y, c)};
-}
-
 __device__ __forceinline__ P2 p2_of(const double* row_h, const double* row_l) {
   return P2{*reinterpret_cast<const float2*>(row_h), *reinterpret_cast<const float2*>(row_l)};
 }
@@ -240,30 +229,6 @@ struct RegNodes {  // computed per small tesseroid of a split pair (thread-local
     mo = m[jk];
   }
 };
-
-// a - b lane by lane: the rounded difference of the high parts, its exact
-// rounding error plus the low parts, renormalised (the low parts of 6e6 m
-// coordinates are up to 0.5 m, hundreds of ulps of a 30 km difference: left
-// unnormalised, the squares below would lose their (lo)^2 terms).
-__device__ __forceinline__ P2 p2_diff(P2 a, P2 b) {
-  using namespace lean;
-  const P2 s = two_sum2(a.h, neg2(b.h));
-  return quick_two_sum2(s.h, add2(s.l, sub2(a.l, b.l)));
-}
-
-// x^2 + y^2 + z^2 lane by lane: exact squares of the high parts, their sum
-// by two-sums, every low-order term added once, one renormalisation.
-__device__ __forceinline__ P2 p2_norm2(P2 x, P2 y, P2 z) {
-  using namespace lean;
-  const P2 px = two_prod2(x.h, x.h), py = two_prod2(y.h, y.h), pz = two_prod2(z.h, z.h);
-  const P2 s = two_sum2(px.h, py.h);
-  const P2 t = two_sum2(s.h, pz.h);
-  float2 lo = add2(add2(px.l, py.l), add2(pz.l, add2(s.l, t.l)));
-  lo = fma2(x.h, add2(x.l, x.l), lo);
-  lo = fma2(y.h, add2(y.l, y.l), lo);
-  lo = fma2(z.h, add2(z.l, z.l), lo);
-  return quick_two_sum2(t.h, lo);
-}
 
 // The 8 point masses of one tesseroid at one point, on float pairs two
 // nodes at a time (the lanes hold the nodes of the two longitudes):
