@@ -121,10 +121,12 @@ __global__ void __launch_bounds__(kThreads) point_kernel(
 // difference d = P - Q, l^2 = |d|^2, 1 / l by a float-pair reciprocal square
 // root and m / l or m d_a / l^3 (the quantities of point_cart) on
 // FFMA2/FADD2/FMUL2, summed on float pairs over a tile and added to the FP64
-// accumulator per tile.  Each term is within a few units of 2^-46 of its
-// exact value (for d of 10 m and more at 1e5 m from the first point: 1e-11
-// relative; the tolerance of the parity tests is 1e-8); the FP64 pipe, 1/64
-// of the FP32 rate here, only sees the per-tile sums.
+// accumulator per tile.  Each term's relative error is the 48-bit rounding
+// of the coordinates, ~2^-48 x (distance of the points from the first point)
+// / d, plus a few 2^-46: 4e-11 for d = 10 m at 1e5 m from the first point,
+// 1e-13 at 10 km (tests/test_float_pairs.py; the parity tests' tolerance is
+// 1e-10); the FP64 pipe, 1/64 of the FP32 rate here, only sees the per-tile
+// sums.
 struct PointTileF2 {
   float xh[kTile], xl[kTile], yh[kTile], yl[kTile], zh[kTile], zl[kTile], mh[kTile], ml[kTile];
 };

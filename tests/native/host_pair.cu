@@ -5,6 +5,7 @@
 #include <cstdint>
 
 #include "../../harmonica_gb300/csrc/prism_math.cuh"
+#include "../../harmonica_gb300/csrc/lean_packed.cuh"
 
 using namespace hg;
 
@@ -76,6 +77,32 @@ void host_lean(int kind, int64_t n, const double* a, const double* b, const doub
       case 5: out[i] = lean::lm_arg_near(a[i], b[i], (float)c[i], T); break;
       default: out[i] = lean::lm_rsqrt(a[i]); break;
     }
+  }
+}
+
+}
+
+extern "C" {
+
+// The float-pair point-mass terms of the tesseroid and point kernels, lane 0
+// of the packed helpers (lean_packed.cuh), for the CPU precision tests.
+// For each i: P = (a[i], b[i], c[i]), Q = (d[3i], d[3i+1], d[3i+2]) as
+// float pairs; kind 0: 1 / |P - Q| (p2_diff, p2_norm2, p2_rsqrt); kind 1:
+// (P_z - Q_z) / |P - Q|^3.
+void host_pairs(int kind, int64_t n, const double* a, const double* b, const double* c,
+                const double* d, double* out) {
+  using namespace lean;
+  for (int64_t i = 0; i < n; i++) {
+    const auto two = [](double v) {
+      const F2 f = double_to_f2(v);
+      return P2{mk2(f.h, f.h), mk2(f.l, f.l)};
+    };
+    const P2 dx = p2_diff(two(a[i]), two(d[3 * i]));
+    const P2 dy = p2_diff(two(b[i]), two(d[3 * i + 1]));
+    const P2 dz = p2_diff(two(c[i]), two(d[3 * i + 2]));
+    const P2 inv = p2_rsqrt(p2_norm2(dx, dy, dz));
+    const P2 v = kind == 0 ? inv : p2_mul(dz, p2_mul(p2_mul(inv, inv), inv));
+    out[i] = f2_to_double(f2_add(lane0(v), F2{0.0f, 0.0f}), 0);
   }
 }
 
