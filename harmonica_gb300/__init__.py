@@ -26,6 +26,7 @@ from .fields import FIELDS
 from .gravity import check_prisms, prism_gravity, prism_gravity_fields
 from .layer import DatasetAccessorPrismLayer, PrismLayer, prism_layer
 from .magnetic import prism_magnetic
+from .magnetic_utils import magnetic_angles_to_vec, magnetic_vec_to_angles, total_field_anomaly
 from .point import point_gravity
 from .tesseroid import tesseroid_gravity
 from .tesseroid_layer import DatasetAccessorTesseroidLayer, TesseroidLayer, tesseroid_layer
@@ -51,6 +52,9 @@ __all__ = [
     "prism_layer",
     "point_gravity",
     "prism_magnetic",
+    "magnetic_angles_to_vec",
+    "magnetic_vec_to_angles",
+    "total_field_anomaly",
     "tesseroid_gravity",
     "tesseroid_layer",
     "TesseroidLayer",
