@@ -28,5 +28,7 @@ def test_total_field_anomaly():
     perpendicular one to zero."""
     b = magnetic_angles_to_vec(50.0, 30.0, -20.0)
     npt.assert_allclose(total_field_anomaly(b, 30.0, -20.0), 50.0, rtol=1e-14)
-    perp = magnetic_angles_to_vec(7.0, -60.0, 160.0)
-    npt.assert_allclose(total_field_anomaly(perp, 30.0, -20.0), 0.0, atol=1e-13)
+    f_hat = np.array(magnetic_angles_to_vec(1.0, 30.0, -20.0))
+    other = np.array([0.3, -1.2, 0.7])
+    perp = other - (other @ f_hat) * f_hat
+    npt.assert_allclose(total_field_anomaly(perp, 30.0, -20.0), 0.0, atol=1e-14)
