@@ -46,6 +46,34 @@ def test_version_and_error_without_gpu():
     assert lib.hg_prism_forward_workspace(2500, 10000, 1 << 3, ctypes.byref(size)) == 0
 
 
+def test_header_compiles_and_links_as_c(tmp_path):
+    """include/harmonica_gb300.h is a C header: a C99 program that includes
+    it builds with -Wall -Wextra -pedantic -Werror, links against the
+    library and passes its GPU-free checks (tests/native/abi_consumer.c)."""
+    import shutil
+    import subprocess
+
+    import pytest
+
+    from harmonica_gb300 import _native
+
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("gcc not available")
+    _native.build()
+    exe = str(tmp_path / "abi_consumer")
+    subprocess.run(
+        [gcc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror",
+         "-I", os.path.join(ROOT, "include"),
+         os.path.join(ROOT, "tests", "native", "abi_consumer.c"),
+         "-L", _native.BUILD_DIR, "-lharmonica_gb300",
+         "-Wl,-rpath," + _native.BUILD_DIR, "-o", exe],
+        check=True, capture_output=True, text=True)
+    run = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    assert run.returncode == 0, run.stderr
+    assert "all checks passed" in run.stdout
+
+
 def test_tesseroid_and_eqs_validation_without_gpu():
     """Argument checks of the tesseroid and equivalent-source entry points
     (they return before any CUDA call)."""
