@@ -34,6 +34,6 @@ def magnetic_vec_to_angles(magnetic_e, magnetic_n, magnetic_u, degrees=True):
 def total_field_anomaly(magnetic_field, inclination, declination):
     """B . F_hat: the anomalous field projected on the unit vector of the
     regional field (inclination, declination in degrees)."""
-    b_e, b_n, b_u = magnetic_field[:3]
+    b_e, b_n, b_u = (np.asarray(component) for component in magnetic_field)
     f_e, f_n, f_u = magnetic_angles_to_vec(1, inclination, declination)
     return b_e * f_e + b_n * f_n + b_u * f_u
