@@ -14,9 +14,9 @@ sources ``relative_depth`` below the data).  The Jacobian
 Jacobian's columns are scaled by their standard deviations, the (weighted)
 least-squares or ridge problem with damping ``damping`` is solved, and the
 solution is unscaled -- the algorithm of the reference's least-squares step
-(verde's ``least_squares``, a dependency that is not installed here, so the
-fitted coefficients are checked by the reference tests' criterion: the fit
-reproduces the data it was fitted on and predicts the field elsewhere).
+(verde's ``least_squares``: scikit-learn's standard scaler without centring,
+then ordinary least squares or ridge regression without intercept, with the
+sample weights; the coefficients divided by the scales).
 ``block_size`` (block-averaging with verde's ``BlockReduce``), ``grid``,
 ``scatter`` and ``profile`` (verde gridding) are outside the GPU path and
 raise ``NotImplementedError``.

@@ -60,3 +60,69 @@ def test_unsupported_options():
 def test_predict_before_fit():
     with pytest.raises(ValueError, match="not fitted yet"):
         EquivalentSources().predict((np.zeros(1), np.zeros(1), np.zeros(1)))
+
+
+def _verde_least_squares(jacobian, data, weights, damping):
+    """verde's least-squares step, stated with the scikit-learn classes it
+    is built on: features scaled by their standard deviation (no centring),
+    an ordinary least-squares or ridge regression without intercept fitted
+    with the sample weights, then the coefficients divided by the scales."""
+    from sklearn.linear_model import LinearRegression, Ridge
+    from sklearn.preprocessing import StandardScaler
+
+    scaler = StandardScaler(copy=True, with_mean=False, with_std=True)
+    scaled = scaler.fit_transform(jacobian)
+    if damping is None:
+        regr = LinearRegression(fit_intercept=False)
+    else:
+        regr = Ridge(alpha=damping, fit_intercept=False)
+    regr.fit(scaled, data.ravel(), sample_weight=weights)
+    return regr.coef_ / scaler.scale_
+
+
+@pytest.mark.parametrize("damping", [None, 1e-3, 10.0])
+@pytest.mark.parametrize("weighted", [False, True])
+def test_least_squares_matches_verde_algorithm(damping, weighted):
+    """The fit's solver (torch, run here on CPU tensors) against the
+    scikit-learn statement of verde's least squares, on a 1/distance
+    Jacobian of sources below scattered data with noise in the data."""
+    pytest.importorskip("sklearn")
+    import torch
+
+    from harmonica_gb300.equivalent_sources import _least_squares
+
+    rng = np.random.default_rng(42)
+    n_data, n_src = 120, 40
+    data_xyz = np.stack([rng.uniform(0, 5e3, n_data), rng.uniform(0, 5e3, n_data),
+                         rng.uniform(0, 50, n_data)])
+    src_xyz = np.stack([rng.uniform(0, 5e3, n_src), rng.uniform(0, 5e3, n_src),
+                        np.full(n_src, -1e3)])
+    jac = 1 / np.linalg.norm(data_xyz[:, :, None] - src_xyz[:, None, :], axis=0)
+    data = jac @ rng.normal(0, 1e5, n_src) + rng.normal(0, 1.0, n_data)
+    weights = rng.uniform(0.5, 2.0, n_data) if weighted else None
+    expected = _verde_least_squares(jac, data, weights, damping)
+    got = _least_squares(torch.from_numpy(jac), torch.from_numpy(data),
+                         None if weights is None else torch.from_numpy(weights), damping)
+    # ridge: torch solves the normal equations, scikit-learn a Cholesky of
+    # the same matrix; cond(scaled Jacobian) ~1e4 here, so 1e-8 leaves room
+    # for the squared condition number (measured: 2e-10 at damping 1e-3)
+    npt.assert_allclose(got.numpy(), expected, rtol=0, atol=1e-8 * np.abs(expected).max())
+    npt.assert_allclose(jac @ got.numpy(), jac @ expected, rtol=0,
+                        atol=1e-11 * np.abs(data).max())
+
+
+def test_least_squares_constant_column():
+    """A column with zero spread keeps a scale of one (no division by zero),
+    as the standard scaler does."""
+    pytest.importorskip("sklearn")
+    import torch
+
+    from harmonica_gb300.equivalent_sources import _least_squares
+
+    rng = np.random.default_rng(3)
+    jac = rng.normal(size=(30, 5))
+    jac[:, 2] = 0.7
+    data = rng.normal(size=30)
+    expected = _verde_least_squares(jac, data, None, 0.5)
+    got = _least_squares(torch.from_numpy(jac), torch.from_numpy(data), None, 0.5)
+    npt.assert_allclose(got.numpy(), expected, rtol=1e-10, atol=1e-12)
