@@ -34,7 +34,7 @@ import ctypes
 import queue
 import threading
 import time
-from concurrent.futures import Future
+from concurrent.futures import Future, InvalidStateError
 
 import numpy as np
 
@@ -48,6 +48,16 @@ KTHREADS = 128  # points per work item (the kernels' tile)
 def chunk_for(n_prisms, max_chunk=2048):
     """Prism chunk of a request: a function of the request alone."""
     return max(128, min(max_chunk, ((n_prisms + 127) // 128) * 128))
+
+
+def _fail(req, exc):
+    """Resolve a request's future with ``exc`` unless it is already done
+    (finished, failed or cancelled by its caller)."""
+    if not req.future.done():
+        try:
+            req.future.set_exception(exc)
+        except InvalidStateError:  # cancelled between the check and the call
+            pass
 
 
 class _Layer:
@@ -134,6 +144,7 @@ class PrismServer:
         self._ids = 0
         self._lock = threading.Lock()
         self._stop = threading.Event()
+        self._broken = None  # the exception that stopped the scheduler, if any
         with torch.cuda.device(self.dev):
             self.compute = torch.cuda.Stream(self.dev)
             self.copy = torch.cuda.Stream(self.dev)
@@ -166,7 +177,12 @@ class PrismServer:
 
     def submit(self, coordinates, field, layer=None, prisms=None, density=None,
                check_singular=False):
-        """Queue one forward solve; returns a Future of the result array."""
+        """Queue one forward solve; returns a Future of the result array.
+
+        The future may be cancelled while the request waits for admission;
+        once admitted it runs to completion.  Raises ``RuntimeError`` after
+        :meth:`close` or after the scheduler stopped on an error."""
+        self._check_open()
         if field not in FIELD_CODES:
             raise ValueError(f"Gravitational field {field} not recognized")
         cast, coords, p_np, d_np = _prepare(
@@ -185,7 +201,15 @@ class PrismServer:
                        check_singular and field in TENSOR_FIELDS)
         req.shape = cast.shape
         self.inbox.put(req)
+        if self._broken is not None:  # the scheduler stopped while this was queued
+            _fail(req, RuntimeError("the prism server stopped after an error"))
         return req.future
+
+    def _check_open(self):
+        if self._broken is not None:
+            raise RuntimeError("the prism server stopped after an error") from self._broken
+        if self._stop.is_set():
+            raise RuntimeError("the prism server is closed")
 
     def close(self, drain=True, timeout=None):
         """Stop the scheduler (after finishing queued work if ``drain``)."""
@@ -238,46 +262,43 @@ class PrismServer:
             self._admit_locked()
 
     def _admit_locked(self):
-        torch = self.torch
         admitted = False
         while self.pending and self.free_slots:
             req = self.pending[0]
+            if req.future.cancelled():  # cancelled by its caller while it waited
+                self.pending.popleft()
+                continue
             layer = None
             if req.layer_key is not None:
                 layer = self.layers.get(req.layer_key)
                 if layer is None:
                     self.pending.popleft()
-                    req.future.set_exception(KeyError(f"layer {req.layer_key!r} not registered"))
+                    _fail(req, KeyError(f"layer {req.layer_key!r} not registered"))
                     continue
             need, chunk, n_chunks = self._request_bytes(req, layer)
             if need > self.budget:
                 self.pending.popleft()
-                req.future.set_exception(MemoryError(
+                _fail(req, MemoryError(
                     f"request needs {need} device bytes, above the server budget"))
                 continue
             if self.used + need > self.budget and not self._evict_for(need):
                 break  # wait for memory to free up (arrival order is kept)
             self.pending.popleft()
-            with torch.cuda.device(self.dev), torch.cuda.stream(self.copy):
-                e, n, u = (torch.from_numpy(c).pin_memory().to(self.dev, non_blocking=True)
-                           for c in req.coords)
-                if layer is None:
-                    pr = torch.from_numpy(np.ascontiguousarray(req.prisms)).to(self.dev)
-                    rho = torch.from_numpy(np.ascontiguousarray(req.density)).to(self.dev)
-                    soa = pack_prisms(pr, rho) if req.n_prisms else torch.zeros(
-                        (7, 1), dtype=torch.float64, device=self.dev)
-                    n_prisms = req.n_prisms
-                    req.tensors += [pr, rho]
-                else:
-                    soa = layer.soa
-                    n_prisms = layer.n_prisms
-                    layer.users += 1
-                    layer.last_used = time.perf_counter()
-                    self.layers.move_to_end(layer.key)
-                out = torch.empty(max(req.n_obs, 1), dtype=torch.float64, device=self.dev)
-                part = torch.empty(max(req.n_obs * n_chunks, 1), dtype=torch.float64,
-                                   device=self.dev)
-            req.tensors += [e, n, u, soa, out, part]
+            if not req.future.set_running_or_notify_cancel():
+                continue  # cancelled just now; from here on it runs to completion
+            try:
+                tensors, n_prisms, pinned_out = self._upload(req, layer, n_chunks)
+            except Exception as exc:  # noqa: BLE001 - an allocation or copy failed
+                # this request fails alone: nothing of it is on the device
+                # books yet, and the server keeps serving the others
+                _fail(req, exc)
+                continue
+            if layer is not None:
+                layer.users += 1
+                layer.last_used = time.perf_counter()
+                self.layers.move_to_end(layer.key)
+            req.tensors += tensors
+            e, n, u, soa, out, part = tensors[-6:]
             req.layer = layer
             req.bytes = need
             self.used += need
@@ -295,7 +316,7 @@ class PrismServer:
             req.n_chunks = -(-n_prisms // chunk) if n_prisms else 0
             req.n_items = -(-req.n_obs // KTHREADS) * req.n_chunks
             req.slot = self.free_slots.pop()
-            req.pinned_out = torch.empty(max(req.n_obs, 1), dtype=torch.float64, pin_memory=True)
+            req.pinned_out = pinned_out
             p = self.table[req.slot]
             p.obs_e, p.obs_n, p.obs_u = e.data_ptr(), n.data_ptr(), u.data_ptr()
             p.n_obs = req.n_obs
@@ -314,6 +335,33 @@ class PrismServer:
         if admitted:
             self._copy_event = self.torch.cuda.Event()
             self._copy_event.record(self.copy)
+
+    def _upload(self, req, layer, n_chunks):
+        """Device copies of a request's points (and prisms, unless it uses a
+        resident layer) and its output and partial-sum buffers, queued on the
+        copy stream, and the pinned host buffer of its result.  Returns the
+        device tensors (the output second to last), the number of prisms and
+        the pinned buffer."""
+        torch = self.torch
+        tensors = []
+        with torch.cuda.device(self.dev), torch.cuda.stream(self.copy):
+            e, n, u = (torch.from_numpy(c).pin_memory().to(self.dev, non_blocking=True)
+                       for c in req.coords)
+            if layer is None:
+                pr = torch.from_numpy(np.ascontiguousarray(req.prisms)).to(self.dev)
+                rho = torch.from_numpy(np.ascontiguousarray(req.density)).to(self.dev)
+                soa = pack_prisms(pr, rho) if req.n_prisms else torch.zeros(
+                    (7, 1), dtype=torch.float64, device=self.dev)
+                n_prisms = req.n_prisms
+                tensors += [pr, rho]
+            else:
+                soa = layer.soa
+                n_prisms = layer.n_prisms
+            out = torch.empty(max(req.n_obs, 1), dtype=torch.float64, device=self.dev)
+            part = torch.empty(max(req.n_obs * n_chunks, 1), dtype=torch.float64,
+                               device=self.dev)
+        pinned_out = torch.empty(max(req.n_obs, 1), dtype=torch.float64, pin_memory=True)
+        return tensors + [e, n, u, soa, out, part], n_prisms, pinned_out
 
     def _plan_round(self):
         """Items for the next round: shortest remaining work first, then grouped
@@ -424,7 +472,8 @@ class PrismServer:
     def _run(self):
         try:
             while True:
-                idle = not self.pending and not self.active and not self.in_flight
+                idle = (not self.pending and not self.active and not self.in_flight
+                        and self.inbox.empty())
                 if self._stop.is_set() and (idle or not getattr(self, "_drain", True)):
                     break
                 try:
@@ -443,7 +492,22 @@ class PrismServer:
                 self._retire(block=len(self.in_flight) >= self.rounds_in_flight)
         except Exception as exc:  # noqa: BLE001 - fail every waiting request
             self.errors.append(exc)
-            for r in list(self.active.values()) + list(self.pending):
-                if not r.future.done():
-                    r.future.set_exception(exc)
+            self._broken = exc  # submit() refuses new work from here on
+            self._fail_unfinished(exc)
             raise
+        # closed without draining: requests still queued or on the device
+        # will not finish (their device buffers stay referenced until the
+        # server object goes away, as rounds may still be running)
+        self._fail_unfinished(RuntimeError("the prism server was closed before this request "
+                                           "finished"))
+
+    def _fail_unfinished(self, exc):
+        """Fail every request that has not finished: admitted, pending and
+        still in the inbox."""
+        while True:
+            try:
+                self.pending.append(self.inbox.get_nowait())
+            except queue.Empty:
+                break
+        for r in list(self.active.values()) + list(self.pending):
+            _fail(r, exc)
