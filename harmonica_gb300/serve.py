@@ -227,6 +227,42 @@ class PrismServer:
                        mean_ms=float(lat.mean() * 1e3))
         return out
 
+    def metrics_text(self, prefix="hg_server"):
+        """The server's counters in the Prometheus text exposition format,
+        for a scrape endpoint: requests completed, admitted and waiting,
+        rounds, point-prism pairs done, device bytes held, scheduler errors
+        and the arrival-to-result latency quantiles (seconds)."""
+        st = self.stats()
+        with self._lock:
+            waiting = len(self.pending) + self.inbox.qsize()
+            active = len(self.active)
+            used = self.used
+        rows = [
+            ("requests_completed_total", "counter", "Requests finished with a result",
+             st["completed"]),
+            ("requests_active", "gauge", "Requests admitted to the device", active),
+            ("requests_waiting", "gauge", "Requests waiting for admission", waiting),
+            ("rounds_total", "counter", "Persistent launches issued", st["rounds"]),
+            ("pairs_total", "counter", "Point-prism pairs of finished requests",
+             st["pairs_done"]),
+            ("device_bytes", "gauge", "Device bytes held by requests and layers", used),
+            ("scheduler_errors_total", "counter", "Exceptions that stopped the scheduler",
+             st["errors"]),
+        ]
+        lines = []
+        for name, kind, text, value in rows:
+            lines += [f"# HELP {prefix}_{name} {text}", f"# TYPE {prefix}_{name} {kind}",
+                      f"{prefix}_{name} {float(value)!r}"]
+        name = f"{prefix}_latency_seconds"
+        lines += [f"# HELP {name} Arrival-to-result latency of finished requests",
+                  f"# TYPE {name} summary"]
+        for q, key in (("0.5", "p50_ms"), ("0.99", "p99_ms")):
+            if key in st:
+                lines.append(f'{name}{{quantile="{q}"}} {st[key] / 1e3!r}')
+        total = st.get("mean_ms", 0.0) * st["completed"] / 1e3
+        lines += [f"{name}_sum {total!r}", f"{name}_count {st['completed']}"]
+        return "\n".join(lines) + "\n"
+
     # ----------------------------------------------------------- internals
     def _pinned_round_buffers(self):
         torch = self.torch

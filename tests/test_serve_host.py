@@ -207,3 +207,25 @@ def test_close_with_drain_serves_requests_still_in_the_inbox():
     srv._stop.set()
     srv._run()  # empty request: admitted and completed without any round
     np.testing.assert_array_equal(fut.result(0), np.zeros(3))
+
+
+def test_metrics_text_parses_as_prometheus_exposition():
+    srv = _skeleton()
+    for k, latency in enumerate([0.1, 0.2, 0.3, 0.4]):
+        srv.completed.append(SimpleNamespace(t_submit=10.0 * k, t_done=10.0 * k + latency))
+    srv.rounds, srv.pairs_done, srv.used = 3, 1.5e9, 4096.0
+    _submit(srv)  # one request waiting for admission
+    text = srv.metrics_text()
+    parser = pytest.importorskip("prometheus_client.parser")
+    families = {f.name: f for f in parser.text_string_to_metric_families(text)}
+    value = {f.name: f.samples[0].value for f in families.values() if f.type != "summary"}
+    assert value["hg_server_requests_completed"] == 4
+    assert value["hg_server_requests_waiting"] == 1
+    assert value["hg_server_rounds"] == 3
+    assert value["hg_server_pairs"] == 1.5e9
+    assert value["hg_server_device_bytes"] == 4096.0
+    latency = {s.name + s.labels.get("quantile", ""): s.value
+               for s in families["hg_server_latency_seconds"].samples}
+    assert latency["hg_server_latency_seconds0.5"] == pytest.approx(0.25)
+    assert latency["hg_server_latency_seconds_count"] == 4
+    assert latency["hg_server_latency_seconds_sum"] == pytest.approx(1.0)
