@@ -45,3 +45,27 @@ def test_oracle_tensor_relation(oracle):
     bu = oracle.prism_magnetic(coords, prism, ([0.0], [0.0], [2.0]), "b_u")
     gzz = oracle.prism_gravity(coords, prism, [1.0], "g_zz")  # Eotvos for rho = 1
     npt.assert_allclose(bu, 1e-7 * 2.0 * gzz / 6.6743e-11, rtol=1e-12)
+
+
+def test_oracle_poisson_relation_all_components(oracle):
+    """Poisson's relation outside the prism: b_i = mu0/(4 pi G rho) sum_j V_ij M_j,
+    with V_ij the gravity tensor of the same prism in the (east, north, up)
+    frame (g_ez and g_nz are easting/northing-downward, so V_eu = -g_ez,
+    V_nu = -g_nz).  Checks every component for a general magnetization at
+    points above, beside and below the prism."""
+    prism = [-100, 120, -80, 60, -500, -200]
+    coords = ([10.0, 300.0, -250.0, 40.0], [-20.0, 50.0, 10.0, 400.0],
+              [100.0, 30.0, -350.0, -900.0])
+    m = np.array([1.5, -0.7, 2.0])
+    g = {f: np.asarray(oracle.prism_gravity(coords, prism, [1.0], f))
+         for f in ("g_ee", "g_nn", "g_zz", "g_en", "g_ez", "g_nz")}
+    tensor = np.array([[g["g_ee"], g["g_en"], -g["g_ez"]],
+                       [g["g_en"], g["g_nn"], -g["g_nz"]],
+                       [-g["g_ez"], -g["g_nz"], g["g_zz"]]])  # Eotvos, rho = 1
+    expected = 1e-7 / 6.6743e-11 * np.einsum("ijk,j->ik", tensor, m)
+    b = oracle.prism_magnetic(coords, prism, tuple([v] for v in m), "b")
+    scale = np.abs(expected).max()
+    for k, name in enumerate(("b_e", "b_n", "b_u")):
+        npt.assert_allclose(b[k], expected[k], rtol=1e-13, atol=1e-15 * scale, err_msg=name)
+        single = oracle.prism_magnetic(coords, prism, tuple([v] for v in m), name)
+        npt.assert_allclose(single, b[k], rtol=1e-14, atol=0)
