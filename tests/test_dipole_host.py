@@ -38,6 +38,30 @@ def test_oracle_matches_prism_far_field():
         npt.assert_allclose(got[k], ref, rtol=2e-3)
 
 
+
+def test_oracle_poisson_relation_with_point_mass_tensor():
+    """A dipole's field is mu0/(4 pi G) times the gravity tensor of a unit
+    point mass at the dipole contracted with the moment (the tensor from the
+    point-mass oracle; g_ez and g_nz are easting/northing-downward)."""
+    dipoles = (np.array([0.0, 120.0, -80.0]), np.array([0.0, -40.0, 60.0]),
+               np.array([-100.0, -300.0, -50.0]))
+    moments = (np.array([2e6, -1e6, 5e5]), np.array([-3e5, 4e6, 1e6]),
+               np.array([1e6, 2e6, -3e6]))
+    pts = (np.array([300.0, -200.0, 50.0, 10.0]), np.array([100.0, 400.0, -350.0, 20.0]),
+           np.array([250.0, 300.0, 500.0, -20.0]))
+    expected = np.zeros((3, 4))
+    for j in range(3):
+        src = tuple([c[j]] for c in dipoles)
+        g = {f: np.asarray(prism_oracle.point_gravity(pts, src, [1.0], f))
+             for f in ("g_ee", "g_nn", "g_zz", "g_en", "g_ez", "g_nz")}
+        tensor = np.array([[g["g_ee"], g["g_en"], -g["g_ez"]],
+                           [g["g_en"], g["g_nn"], -g["g_nz"]],
+                           [-g["g_ez"], -g["g_nz"], g["g_zz"]]])  # Eotvos per kg
+        m = np.array([c[j] for c in moments])
+        expected += 1e-7 / 6.6743e-11 * np.einsum("ijk,j->ik", tensor, m)
+    got = dipole_oracle.dipole_magnetic(pts, dipoles, moments)
+    npt.assert_allclose(np.array(got), expected, rtol=1e-12, atol=1e-14 * np.abs(expected).max())
+
 def test_invalid_field():
     """test/test_dipole.py:29-38."""
     msg = re.escape("Invalid field 'Not a valid field'. Please choose one of")
