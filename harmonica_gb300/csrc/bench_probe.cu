@@ -4,7 +4,15 @@
 // (8 chains x iters FMAs x 2 flops).
 #include <cuda_runtime.h>
 
+#include <string>
+
+#include "../../include/harmonica_gb300.h"
 #include "../../include/harmonica_gb300_bench.h"
+
+namespace hg {
+int set_error(int code, const std::string& msg);
+int cuda_check(cudaError_t e, const char* what);
+}  // namespace hg
 
 namespace {
 
@@ -22,8 +30,10 @@ __global__ void fp64_fma_chains(double* out, int iters, double a, double b) {
 
 extern "C" int hg_fp64_peak_probe(double* out, int64_t n_threads_total, int iters, void* stream) {
   const int threads = 256;
-  if (n_threads_total <= 0 || n_threads_total % threads != 0 || iters <= 0 || !out) return -1;
+  if (!out) return hg::set_error(HG_ERR_INVALID, "null pointer");
+  if (n_threads_total <= 0 || n_threads_total % threads != 0 || iters <= 0)
+    return hg::set_error(HG_ERR_INVALID, "bad arguments (threads: a positive multiple of 256)");
   fp64_fma_chains<<<(unsigned)(n_threads_total / threads), threads, 0, (cudaStream_t)stream>>>(
       out, iters, 0.999999, 1e-6);
-  return cudaGetLastError() == cudaSuccess ? 0 : -2;
+  return hg::cuda_check(cudaGetLastError(), "fp64 peak probe launch");
 }

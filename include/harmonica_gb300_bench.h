@@ -16,7 +16,8 @@ extern "C" {
  * Launch n_threads_total threads (a multiple of 256) that each run
  * 16 * iters FP64 flops (independent fused multiply-adds) and write one
  * double to out[n_threads_total] (device memory).  Asynchronous on `stream`.
- * Returns 0, or a negative value on bad arguments / launch failure.
+ * Returns 0 (HG_OK), or HG_ERR_INVALID (-1) on bad arguments / HG_ERR_CUDA (-2)
+ * on a launch failure, with the message in hg_last_error().
  */
 int hg_fp64_peak_probe(double *out, int64_t n_threads_total, int iters, void *stream);
 

@@ -108,3 +108,53 @@ def test_tesseroid_and_eqs_validation_without_gpu():
     assert lib.hg_eqs_predict(None, None, None, 2, None, None, None, None, 3, 0, None, None, 0,
                               None) < 0
     assert b"null pointer" in lib.hg_last_error()
+
+
+_PROBE = r"""
+import ctypes, json, sys
+sys.path.insert(0, sys.argv[1])
+from harmonica_gb300 import _native
+lib = _native.lib()
+report = {}
+for name, (res, args) in _native.PROTOTYPES.items():
+    if not args or name == "hg_batch_destroy":
+        continue
+    for mode in ("negative sizes", "null pointers"):
+        vals = []
+        for a in args:
+            if a in (ctypes.c_int64, ctypes.c_int32, ctypes.c_int):
+                vals.append(-1 if mode == "negative sizes" else 3)
+            elif a is ctypes.c_uint32:
+                vals.append(1 << 3)
+            elif a is ctypes.c_size_t:
+                vals.append(0)
+            elif a is ctypes.c_double:
+                vals.append(0.0)
+            else:
+                vals.append(None)
+        rc = getattr(lib, name)(*vals)
+        report[name + ": " + mode] = [rc, lib.hg_last_error().decode()]
+print(json.dumps(report))
+"""
+
+
+def test_every_entry_point_rejects_bad_arguments_before_cuda():
+    """Every function of the C ABI, called with negative sizes or with null
+    pointers, returns HG_ERR_INVALID with a message and touches neither
+    memory nor the GPU (run in a child process, so a crash fails the test
+    instead of the test run)."""
+    import json
+    import subprocess
+    import sys
+
+    from harmonica_gb300 import _native
+
+    _native.build()
+    run = subprocess.run([sys.executable, "-c", _PROBE, ROOT], capture_output=True, text=True,
+                         timeout=300)
+    assert run.returncode == 0, run.stderr[-2000:]
+    report = json.loads(run.stdout.strip().splitlines()[-1])
+    declared = set(declared_functions()) - {"hg_version", "hg_last_error", "hg_batch_destroy"}
+    assert {k.split(":")[0] for k in report} == declared
+    bad = {k: v for k, v in report.items() if v[0] != -1 or not v[1]}
+    assert not bad, bad
