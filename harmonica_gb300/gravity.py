@@ -25,6 +25,7 @@ import warnings
 import numpy as np
 
 from . import _native
+from ._trace import stage
 from .fields import FIELD_CODES, FIELDS, TENSOR_FIELDS, field_mask
 
 
@@ -168,9 +169,10 @@ def _run_host(coords, prisms, density, mask, check_singular, device, progressbar
     dev = _device(device)
     n_obs = coords[0].size
     with torch.cuda.device(dev):
-        pr = torch.from_numpy(np.ascontiguousarray(prisms)).to(dev)
-        rho = torch.from_numpy(np.ascontiguousarray(density)).to(dev)
-        soa = pack_prisms(pr, rho)
+        with stage("upload prisms"):
+            pr = torch.from_numpy(np.ascontiguousarray(prisms)).to(dev)
+            rho = torch.from_numpy(np.ascontiguousarray(density)).to(dev)
+            soa = pack_prisms(pr, rho)
         n_rows = bin(mask).count("1")
         result = np.empty((n_rows, n_obs), dtype=np.float64)
         flagged = False
@@ -179,10 +181,14 @@ def _run_host(coords, prisms, density, mask, check_singular, device, progressbar
         progress = _Progress(n_obs, progressbar)
         for c in range(n_chunks):
             lo, hi = int(bounds[c]), int(bounds[c + 1])
-            e, n, u = (torch.from_numpy(x[lo:hi]).to(dev) for x in coords)
-            out, flag = forward_on_device(e, n, u, soa, prisms.shape[0], mask, check_singular)
-            result[:, lo:hi] = out.cpu().numpy()
-            flagged |= bool(flag.item())
+            with stage("upload points"):
+                e, n, u = (torch.from_numpy(x[lo:hi]).to(dev) for x in coords)
+            with stage("forward"):
+                out, flag = forward_on_device(e, n, u, soa, prisms.shape[0], mask,
+                                              check_singular)
+            with stage("download"):
+                result[:, lo:hi] = out.cpu().numpy()
+                flagged |= bool(flag.item())
             progress.update(hi - lo)
     return result, flagged
 
@@ -237,7 +243,8 @@ def prism_gravity(
     """
     if field not in FIELD_CODES:
         raise ValueError(f"Gravitational field {field} not recognized")
-    cast, coords, prisms, density = _prepare(coordinates, prisms, density, disable_checks)
+    with stage("prism_gravity checks"):
+        cast, coords, prisms, density = _prepare(coordinates, prisms, density, disable_checks)
     check_singular = (not disable_checks) and field in TENSOR_FIELDS
     result, flagged = _run_host(
         coords, prisms, density, field_mask([field]), check_singular, device, progressbar

@@ -20,6 +20,7 @@ import warnings
 import numpy as np
 
 from . import _native
+from ._trace import stage
 from .fields import FIELD_CODES, field_mask
 
 try:  # optional, as in the reference environment
@@ -315,14 +316,17 @@ def layer_forward(coords, easting, northing, bottom, top, density, mask, thresho
     n_obs = coords[0].size
     n_rows = bin(mask).count("1")
     with torch.cuda.device(dev):
-        e, n, u = (torch.from_numpy(np.ascontiguousarray(c)).to(dev) for c in coords)
-        ce = torch.from_numpy(np.ascontiguousarray(easting, dtype=np.float64)).to(dev)
-        cn = torch.from_numpy(np.ascontiguousarray(northing, dtype=np.float64)).to(dev)
-        bt = torch.from_numpy(np.ascontiguousarray(bottom, dtype=np.float64)).to(dev)
-        tp = torch.from_numpy(np.ascontiguousarray(top, dtype=np.float64)).to(dev)
-        rho = torch.from_numpy(np.ascontiguousarray(density, dtype=np.float64)).to(dev)
-        out = layer_forward_device(e, n, u, ce, cn, bt, tp, rho, mask, threshold)
-        return out.cpu().numpy()
+        with stage("upload layer and points"):
+            e, n, u = (torch.from_numpy(np.ascontiguousarray(c)).to(dev) for c in coords)
+            ce = torch.from_numpy(np.ascontiguousarray(easting, dtype=np.float64)).to(dev)
+            cn = torch.from_numpy(np.ascontiguousarray(northing, dtype=np.float64)).to(dev)
+            bt = torch.from_numpy(np.ascontiguousarray(bottom, dtype=np.float64)).to(dev)
+            tp = torch.from_numpy(np.ascontiguousarray(top, dtype=np.float64)).to(dev)
+            rho = torch.from_numpy(np.ascontiguousarray(density, dtype=np.float64)).to(dev)
+        with stage("layer forward"):
+            out = layer_forward_device(e, n, u, ce, cn, bt, tp, rho, mask, threshold)
+        with stage("download"):
+            return out.cpu().numpy()
 
 
 def layer_forward_device(e, n, u, ce, cn, bottom, top, density, mask, threshold):

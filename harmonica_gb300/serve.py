@@ -39,6 +39,7 @@ from concurrent.futures import Future, InvalidStateError
 import numpy as np
 
 from . import _native
+from ._trace import stage
 from .fields import FIELD_CODES, TENSOR_FIELDS
 from .gravity import _prepare, pack_prisms
 
@@ -519,13 +520,16 @@ class PrismServer:
                         self.pending.append(self.inbox.get_nowait())
                 except queue.Empty:
                     pass
-                self._admit()
+                with stage("serve admit"):
+                    self._admit()
                 if len(self.in_flight) < self.rounds_in_flight:
                     items, counts, finishing = self._plan_round()
                     if items is not None:
-                        self._launch_round(items, counts, finishing)
+                        with stage("serve round"):
+                            self._launch_round(items, counts, finishing)
                         continue
-                self._retire(block=len(self.in_flight) >= self.rounds_in_flight)
+                with stage("serve retire"):
+                    self._retire(block=len(self.in_flight) >= self.rounds_in_flight)
         except Exception as exc:  # noqa: BLE001 - fail every waiting request
             self.errors.append(exc)
             self._broken = exc  # submit() refuses new work from here on
