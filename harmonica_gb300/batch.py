@@ -259,7 +259,7 @@ def autotune(problems, chunks=(2048, 8192, 32768), cta_multipliers=(1, 2),
     if cache:
         table[key] = result
         os.makedirs(os.path.dirname(cache), exist_ok=True)
-        tmp = cache + ".tmp"
+        tmp = f"{cache}.{os.getpid()}.tmp"  # one writer per file; the rename is atomic
         with open(tmp, "w") as f:
             json.dump(table, f, indent=1)
         os.replace(tmp, cache)
