@@ -162,7 +162,12 @@ class PrismServer:
 
     # ------------------------------------------------------------------ api
     def register_layer(self, key, prisms, density):
-        """Keep a prism model resident (evictable when idle); returns its bytes."""
+        """Keep a prism model resident (evictable when idle); returns its bytes.
+
+        Registering an existing key replaces that layer when no admitted
+        request uses it (``RuntimeError`` otherwise)."""
+        with self._lock:
+            self._check_replaceable(key)
         torch = self.torch
         _, _, p_np, d_np = _prepare(([0.0], [0.0], [0.0]), prisms, density, False)
         with torch.cuda.device(self.dev), torch.cuda.stream(self.copy):
@@ -172,9 +177,34 @@ class PrismServer:
             self.copy.synchronize()
         layer = _Layer(key, soa, p_np.shape[0])
         with self._lock:
-            self.layers[key] = layer
-            self.used += layer.bytes
+            self._add_layer(layer)
         return layer.bytes
+
+    def unregister_layer(self, key):
+        """Drop a resident layer that no admitted request uses; returns the
+        device bytes it held (``KeyError`` for an unknown key,
+        ``RuntimeError`` while it is in use)."""
+        with self._lock:
+            layer = self.layers[key]
+            self._check_replaceable(key)
+            del self.layers[key]
+            self.used -= layer.bytes
+        return layer.bytes
+
+    def _check_replaceable(self, key):
+        old = self.layers.get(key)
+        if old is not None and old.users:
+            raise RuntimeError(f"layer {key!r} is in use by admitted requests")
+
+    def _add_layer(self, layer):
+        """Book a layer, replacing an idle one of the same key (its bytes
+        are released)."""
+        self._check_replaceable(layer.key)
+        old = self.layers.pop(layer.key, None)
+        if old is not None:
+            self.used -= old.bytes
+        self.layers[layer.key] = layer
+        self.used += layer.bytes
 
     def submit(self, coordinates, field, layer=None, prisms=None, density=None,
                check_singular=False):

@@ -229,3 +229,35 @@ def test_metrics_text_parses_as_prometheus_exposition():
     assert latency["hg_server_latency_seconds0.5"] == pytest.approx(0.25)
     assert latency["hg_server_latency_seconds_count"] == 4
     assert latency["hg_server_latency_seconds_sum"] == pytest.approx(1.0)
+
+
+def _layer(key, n_prisms):
+    from harmonica_gb300.serve import _Layer
+
+    return _Layer(key, torch.zeros((7, n_prisms), dtype=torch.float64), n_prisms)
+
+
+def test_reregistering_a_layer_releases_the_old_bytes():
+    srv = _skeleton()
+    srv._add_layer(_layer("topo", 100))
+    assert srv.used == 7 * 100 * 8
+    srv._add_layer(_layer("topo", 40))  # replaced: the old 100 prisms are released
+    assert srv.used == 7 * 40 * 8 and srv.layers["topo"].n_prisms == 40
+    assert srv.unregister_layer("topo") == 7 * 40 * 8
+    assert srv.used == 0.0 and not srv.layers
+    with pytest.raises(KeyError):
+        srv.unregister_layer("topo")
+
+
+def test_a_layer_in_use_is_neither_replaced_nor_dropped():
+    srv = _skeleton()
+    srv._add_layer(_layer("topo", 10))
+    fut = srv.submit(_problem()[0], "g_z", layer="topo")
+    srv.pending.append(srv.inbox.get_nowait())
+    srv._admit()
+    assert fut.running() and srv.layers["topo"].users == 1
+    with pytest.raises(RuntimeError, match="in use"):
+        srv._add_layer(_layer("topo", 20))
+    with pytest.raises(RuntimeError, match="in use"):
+        srv.unregister_layer("topo")
+    assert srv.layers["topo"].n_prisms == 10
