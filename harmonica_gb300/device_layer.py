@@ -52,6 +52,12 @@ class DevicePrismLayer:
         self.top = None
         self.bottom = None
         _check_regular_grid(easting.cpu().numpy(), northing.cpu().numpy())
+        for name, value in properties.items():
+            if tuple(value.shape) != self.shape:
+                raise ValueError(
+                    f"Invalid property '{name}' with shape '{tuple(value.shape)}'. "
+                    "Its shape should be (northing, easting) = " + f"'{self.shape}'."
+                )
         self._spacing = (
             float(northing[1] - northing[0]) if northing.numel() > 1 else 0.0,
             float(easting[1] - easting[0]) if easting.numel() > 1 else 0.0,

@@ -63,6 +63,11 @@ def dipole_magnetic(coordinates, dipoles, magnetic_moments, field, parallel=True
     # the kernels read three moment components per dipole whatever the checks
     if len(magnetic_moments) != 3 or any(m.size != dipoles[0].size for m in magnetic_moments):
         raise ValueError("magnetic_moments must hold 3 components of one value per dipole")
+    if not dipoles[0].size == dipoles[1].size == dipoles[2].size:
+        raise ValueError(
+            "The coordinates of the dipoles must have the same number of elements "
+            f"({dipoles[0].size}, {dipoles[1].size}, {dipoles[2].size})"
+        )
     comp = _COMPONENT[field]
     rows = 3 if comp == 3 else 1
     n_obs, n_dip = coords[0].size, dipoles[0].size

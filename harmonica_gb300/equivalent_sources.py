@@ -41,6 +41,16 @@ def _tensors(arrays, dev):
     return [torch.from_numpy(np.array(np.ravel(a), dtype=np.float64)).to(dev) for a in arrays]
 
 
+def _same_sizes(arrays, what):
+    """The three coordinates of the data or of the sources have one value per
+    point each (the kernels read all three at every index)."""
+    sizes = [np.size(a) for a in arrays[:3]]
+    if len(sizes) != 3 or len(set(sizes)) != 1:
+        raise ValueError(f"The coordinates of the {what} must be three arrays of the same "
+                         f"number of elements (got sizes {sizes})")
+    return sizes[0]
+
+
 def greens_jacobian(coordinates, points, spherical=False, device=None, as_tensor=False):
     """(n_data, n_points) matrix of 1 / distance between data points and
     sources (``jacobian`` of the reference) computed on the GPU."""
@@ -48,6 +58,8 @@ def greens_jacobian(coordinates, points, spherical=False, device=None, as_tensor
 
     from .gravity import _ptr  # noqa: PLC0415
 
+    _same_sizes(coordinates, "data points")
+    _same_sizes(points, "sources")
     dev = _device(device)
     with torch.cuda.device(dev):
         c = _tensors(coordinates[:3], dev)
@@ -67,6 +79,10 @@ def greens_predict(coordinates, points, coefs, spherical=False, device=None):
 
     from .gravity import _ptr  # noqa: PLC0415
 
+    n_points = _same_sizes(points, "sources")
+    if np.size(coefs) != n_points:
+        raise ValueError(f"Number of coefficients ({np.size(coefs)}) mismatch the number of "
+                         f"sources ({n_points})")
     dev = _device(device)
     shape = np.broadcast(*coordinates[:3]).shape
     coords = [np.broadcast_to(np.asarray(c, dtype=np.float64), shape) for c in coordinates[:3]]

@@ -90,6 +90,13 @@ def forward_on_device(easting, northing, upward, prisms_soa, n_prisms, mask, che
     point was met for a requested tensor field).
     """
     torch = _torch()
+    _check_device_arrays(easting=easting, northing=northing, upward=upward)
+    if not easting.numel() == northing.numel() == upward.numel():
+        raise ValueError("The coordinates of the observation points must have the same "
+                         "number of elements.")
+    if n_prisms and (prisms_soa is None or prisms_soa.dim() != 2 or prisms_soa.shape[0] != 7
+                     or prisms_soa.shape[1] < n_prisms):
+        raise ValueError(f"prisms_soa must be a (7, >= {n_prisms}) tensor from pack_prisms")
     lib = _native.lib()
     n_obs = easting.numel()
     n_rows = bin(mask).count("1")
@@ -114,9 +121,25 @@ def forward_on_device(easting, northing, upward, prisms_soa, n_prisms, mask, che
     return out, flag
 
 
+def _check_device_arrays(**tensors):
+    """Float64 and contiguous: the kernels read the raw buffers as packed
+    doubles."""
+    torch = _torch()
+    for name, t in tensors.items():
+        if t.dtype != torch.float64 or not t.is_contiguous():
+            raise ValueError(f"'{name}' must be a contiguous float64 tensor "
+                             f"(got {t.dtype}, contiguous={t.is_contiguous()})")
+
+
 def pack_prisms(prisms, density):
     """Pack (M, 6) prisms and (M,) densities (CUDA float64) into a (7, M) SoA tensor."""
     torch = _torch()
+    _check_device_arrays(prisms=prisms, density=density)
+    if prisms.dim() != 2 or prisms.shape[1] != 6 or density.numel() != prisms.shape[0]:
+        raise ValueError(
+            f"pack_prisms needs (M, 6) prisms and M densities, got {tuple(prisms.shape)} "
+            f"and {density.numel()}"
+        )
     lib = _native.lib()
     m = prisms.shape[0]
     soa = torch.empty((7, max(m, 1)), dtype=torch.float64, device=prisms.device)
@@ -136,14 +159,28 @@ def _prepare(coordinates, prisms, density, disable_checks):
     )
     prisms = np.atleast_2d(np.asarray(prisms, dtype=np.float64))
     density = np.atleast_1d(np.asarray(density, dtype=np.float64)).ravel()
+    # the array sizes are checked even with disable_checks: the kernels read
+    # six boundaries and one density per prism, and a short array would be
+    # read past its end on the device
+    check_sizes(prisms, density)
     if not disable_checks:
-        if density.size != prisms.shape[0]:
-            raise ValueError(
-                f"Number of elements in density ({density.size}) "
-                + f"mismatch the number of prisms ({prisms.shape[0]})"
-            )
         check_prisms(prisms)
     return cast, coords, prisms, density
+
+
+def check_sizes(prisms, density, name="density"):
+    """Six boundaries per prism and one ``name`` value per prism
+    (``ValueError`` otherwise, with the reference's message for the count)."""
+    if prisms.ndim != 2 or prisms.shape[1] != 6:
+        raise ValueError(
+            f"Invalid prisms array with shape {prisms.shape}: each prism needs its six "
+            "boundaries [west, east, south, north, bottom, top]."
+        )
+    if density.size != prisms.shape[0]:
+        raise ValueError(
+            f"Number of elements in {name} ({density.size}) "
+            + f"mismatch the number of prisms ({prisms.shape[0]})"
+        )
 
 
 class _Progress:

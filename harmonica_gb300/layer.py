@@ -142,6 +142,14 @@ def prism_layer(coordinates, surface, reference, properties=None):
     data = None
     if properties:
         data = {name: np.asarray(value) for name, value in properties.items()}
+        for name, value in data.items():
+            # xarray refuses these too (its dimensions would conflict)
+            if value.shape != (northing.size, easting.size):
+                raise ValueError(
+                    f"Invalid property '{name}' with shape '{value.shape}'. "
+                    "Its shape should be (northing, easting) = "
+                    + f"'{(northing.size, easting.size)}'."
+                )
     if xr is not None:
         data_vars = {k: (DIMS, v) for k, v in (data or {}).items()}
         prisms = xr.Dataset(data_vars, coords={"easting": easting, "northing": northing})
@@ -335,6 +343,18 @@ def layer_forward_device(e, n, u, ce, cn, bottom, top, density, mask, threshold)
 
     from .gravity import _ptr  # noqa: PLC0415
 
+    # the kernel reads one value of each grid per prism and three coordinates
+    # per point: a short array would be read past its end on the device
+    n_prisms = ce.numel() * cn.numel()
+    for name, grid in (("bottom", bottom), ("top", top), ("density", density)):
+        if grid.numel() != n_prisms:
+            raise ValueError(
+                f"Invalid '{name}' with {grid.numel()} values: the layer has "
+                f"{cn.numel()} x {ce.numel()} prisms (northing x easting)."
+            )
+    if not e.numel() == n.numel() == u.numel():
+        raise ValueError("The coordinates of the observation points must have the same "
+                         "number of elements.")
     lib = _native.lib()
     n_obs = e.numel()
     n_rows = bin(mask).count("1")

@@ -11,7 +11,7 @@ of the prism gravity formulation).
 import numpy as np
 
 from . import _native
-from .gravity import check_prisms
+from .gravity import check_prisms, check_sizes
 
 VALID_FIELDS = ("b", "b_e", "b_n", "b_u")
 _COMPONENT = {"b_e": 0, "b_n": 1, "b_u": 2, "b": 3}
@@ -38,17 +38,22 @@ def prism_magnetic(coordinates, prisms, magnetization, field, parallel=True, dty
                    for c in coordinates[:3])
     prisms = np.atleast_2d(np.asarray(prisms, dtype=np.float64))
     mag = tuple(np.atleast_1d(np.asarray(m, dtype=np.float64)).ravel() for m in magnetization)
-    if not disable_checks:
-        if (size := len(mag)) != 3:
+    # the sizes are checked even with disable_checks: the kernels read six
+    # boundaries and three magnetization components per prism, and a short
+    # array would be read past its end on the device
+    if (size := len(mag)) != 3:
+        raise ValueError(
+            f"Invalid magnetization vectors with '{size}' elements. "
+            + "Magnetization vectors should have only 3 elements."
+        )
+    for component in mag:
+        if component.size != prisms.shape[0]:
             raise ValueError(
-                f"Invalid magnetization vectors with '{size}' elements. "
-                + "Magnetization vectors should have only 3 elements."
-            )
-        if mag[0].size != prisms.shape[0]:
-            raise ValueError(
-                f"Number of magnetization vectors ({mag[0].size}) "
+                f"Number of magnetization vectors ({component.size}) "
                 + f"mismatch the number of prisms ({prisms.shape[0]})"
             )
+    check_sizes(prisms, mag[0], name="magnetization")
+    if not disable_checks:
         check_prisms(prisms)
     comp = _COMPONENT[field]
     rows = 3 if comp == 3 else 1

@@ -57,6 +57,12 @@ def point_gravity(coordinates, points, masses, field, coordinate_system="cartesi
     pts = tuple(np.ascontiguousarray(np.atleast_1d(np.asarray(p, dtype=np.float64)).ravel())
                 for p in points[:3])
     masses = np.ascontiguousarray(np.atleast_1d(np.asarray(masses, dtype=np.float64)).ravel())
+    # the kernels read three coordinates and one mass per point
+    if not pts[0].size == pts[1].size == pts[2].size:
+        raise ValueError(
+            "The coordinates of the point masses must have the same number of elements "
+            f"({pts[0].size}, {pts[1].size}, {pts[2].size})"
+        )
     if masses.size != pts[0].size:
         raise ValueError(
             f"Number of elements in masses ({masses.size}) "
