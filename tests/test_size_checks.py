@@ -121,3 +121,24 @@ def test_host_layer_property_shapes():
     assert layer.prism_layer.shape == (2, 3)
     with pytest.raises(ValueError, match="Invalid property 'density'"):
         hg.prism_layer((easting, northing), surface, 0.0, properties={"density": np.ones((3, 2))})
+
+
+def test_tesseroid_device_entry_checks_sizes_and_layout():
+    from harmonica_gb300.tesseroid import tesseroid_gravity_device
+
+    pts = _f64(0.0, 1.0)
+    tess = torch.zeros((3, 6), dtype=torch.float64)
+    with pytest.raises(ValueError, match="same number of elements"):
+        tesseroid_gravity_device(pts, _f64(0.0), pts, tess, torch.zeros(3, dtype=torch.float64),
+                                 "g_z")
+    with pytest.raises(ValueError, match=r"density must have shape \(3,\) or \(3, 2\)"):
+        tesseroid_gravity_device(pts, pts, pts, tess, torch.zeros(2, dtype=torch.float64), "g_z")
+    with pytest.raises(ValueError, match=r"\(M, 6\)"):
+        tesseroid_gravity_device(pts, pts, pts, torch.zeros((3, 5), dtype=torch.float64),
+                                 torch.zeros(3, dtype=torch.float64), "g_z")
+    with pytest.raises(ValueError, match="contiguous float64"):
+        tesseroid_gravity_device(pts.float(), pts, pts, tess, torch.zeros(3, dtype=torch.float64),
+                                 "g_z")
+    with pytest.raises(ValueError, match="status"):
+        tesseroid_gravity_device(pts, pts, pts, tess, torch.zeros(3, dtype=torch.float64), "g_z",
+                                 status=torch.zeros(1, dtype=torch.int64))
