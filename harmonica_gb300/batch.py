@@ -102,6 +102,9 @@ class PrismBatch:
         coords = pb["coordinates"]
         if isinstance(coords[0], torch.Tensor):
             e, n, u = (c.to(dev, torch.float64).contiguous().ravel() for c in coords[:3])
+            if not e.numel() == n.numel() == u.numel():
+                raise ValueError("The coordinates of a problem must have the same number of "
+                                 "elements.")
             shape = tuple(coords[0].shape)
         else:
             cast, host_coords, _, _ = _prepare(coords, np.zeros((0, 6)), np.zeros(0), True)
