@@ -499,7 +499,7 @@ def run_points(args, rank, world, local):
     out = torch.empty(B, dtype=torch.float64, device=dev)
     ws = _native.ctypes.c_size_t(0)
     _native.check(lib.hg_point_forward_workspace(B, pe.size, _native.ctypes.byref(ws)))
-    work = torch.empty(max(1, ws.value // 8), dtype=torch.float64, device=dev)
+    work = torch.empty(max(1, (ws.value + 7) // 8), dtype=torch.float64, device=dev)
 
     def step(s):
         lo = (s * B) % (c[0].numel() - B)
@@ -556,7 +556,7 @@ def run_magnetic(args, rank, world, local):
     out = torch.empty((3, B), dtype=torch.float64, device=dev)
     ws = _native.ctypes.c_size_t(0)
     _native.check(lib.hg_prism_magnetic_workspace(B, m, 3, _native.ctypes.byref(ws)))
-    work = torch.empty(max(1, ws.value // 8), dtype=torch.float64, device=dev)
+    work = torch.empty(max(1, (ws.value + 7) // 8), dtype=torch.float64, device=dev)
 
     def step(s):
         lo = (s * B) % (c[0].numel() - B)
