@@ -37,12 +37,21 @@ def gather_shards(local, n, world, group=None):
 def forward_sharded(coordinates, compute, rank, world, group=None):
     """
     Run ``compute(shard_coordinates) -> np.ndarray`` on this rank's shard and
-    return the gathered full result on every rank.
+    return the gathered full result on every rank, with the broadcast shape
+    of the coordinates.  The coordinates are broadcast against each other
+    first (a scalar height with arrays of eastings and northings, as the
+    forward models accept).  With an NCCL group the shards are gathered on
+    this rank's current CUDA device.
     """
     import torch
+    import torch.distributed as dist
 
-    n = np.size(coordinates[0])
+    coords = np.broadcast_arrays(*(np.asarray(c, dtype=np.float64) for c in coordinates[:3]))
+    shape = coords[0].shape
+    n = coords[0].size
     lo, hi = shard_bounds(n, rank, world)
-    part = compute(tuple(np.asarray(c).ravel()[lo:hi] for c in coordinates[:3]))
-    local = torch.from_numpy(np.ascontiguousarray(part, dtype=np.float64))
-    return gather_shards(local, n, world, group).numpy()
+    part = compute(tuple(np.ascontiguousarray(c.ravel()[lo:hi]) for c in coords))
+    local = torch.from_numpy(np.ascontiguousarray(np.ravel(part), dtype=np.float64))
+    if dist.get_backend(group) == "nccl":
+        local = local.to(torch.device("cuda", torch.cuda.current_device()))
+    return gather_shards(local, n, world, group).cpu().numpy().reshape(shape)

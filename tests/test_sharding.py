@@ -44,7 +44,7 @@ def _worker(rank, world, port, out_path):
                               rng.uniform(-1e3, 0, 50), rng.uniform(10, 1e3, 50),
                               rng.uniform(-900, -500, 50), rng.uniform(-400, -10, 50)])
     rho = rng.uniform(-300, 300, 50)
-    coords = tuple(rng.uniform(-2e3, 2e3, 37) for _ in range(2)) + (np.full(37, 100.0),)
+    coords = tuple(rng.uniform(-2e3, 2e3, 37) for _ in range(2)) + (100.0,)  # broadcast
     full = forward_sharded(coords, lambda c: prism_oracle.prism_gravity(c, prisms, rho, "g_z",
                                                                        n_threads=1),
                            rank, world)
