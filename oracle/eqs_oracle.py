@@ -6,7 +6,9 @@ numpy restatement of harmonica ``src/harmonica/_equivalent_sources``:
 ``jacobian`` and ``predict`` (utils.py:54-96) with ``greens_func_cartesian``
 (cartesian.py:635-644: 1 / distance_cartesian) and ``greens_func_spherical``
 (spherical.py:413-424: 1 / distance_spherical, utils.py:122-201 of
-_forward).
+_forward).  Pinned to the reference: tests/golden/reference_eqs.npz holds
+the outputs of the reference's own loops (make_eqs_golden.py), which the
+Jacobians here reproduce bit for bit.
 """
 
 import numpy as np

@@ -126,3 +126,23 @@ def test_least_squares_constant_column():
     expected = _verde_least_squares(jac, data, None, 0.5)
     got = _least_squares(torch.from_numpy(jac), torch.from_numpy(data), None, 0.5)
     npt.assert_allclose(got.numpy(), expected, rtol=1e-10, atol=1e-12)
+
+
+def test_oracle_matches_reference_golden():
+    """The oracle against harmonica's own jacobian/predict loops and Green's
+    functions run from the reference sources (tests/golden/make_eqs_golden.py):
+    the Jacobians bit for bit, the predictions to the rounding of the sum
+    order (the reference adds coefficient x Green's function source by
+    source; the oracle uses a matrix product)."""
+    import os
+
+    from oracle import eqs_oracle
+
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "reference_eqs.npz"))
+    for name, spherical in (("cart", False), ("sph", True)):
+        data, src = g[f"{name}_data"], g[f"{name}_src"]
+        npt.assert_array_equal(eqs_oracle.jacobian(data, src, spherical=spherical),
+                               g[f"{name}_jacobian"])
+        ref = g[f"{name}_predict"]
+        npt.assert_allclose(eqs_oracle.predict(data, src, g["coefs"], spherical=spherical), ref,
+                            rtol=0, atol=1e-14 * np.abs(ref).max())
