@@ -42,3 +42,18 @@ def test_errors():
     with pytest.raises(ValueError, match=msg):
         hg.point_gravity([0, 0, 250], [[-10, 0], [0, 0], [-100, -10]], [1000, 2000, 3000],
                          "potential")
+
+
+def test_oracle_spherical_matches_reference_golden(oracle):
+    """Spherical potential and g_z against harmonica's own point_gravity run
+    from the reference sources (tests/golden/make_point_golden.py; its
+    spherical kernels are harmonica code), masses right below, near and far
+    from the points: measured agreement 2.5e-16."""
+    import os
+
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden",
+                             "reference_point_spherical.npz"))
+    for field in ("potential", "g_z"):
+        got = oracle.point_gravity(tuple(g["coordinates"]), tuple(g["points"]), g["masses"],
+                                   field, coordinate_system="spherical")
+        npt.assert_allclose(got, g[field], rtol=1e-14, atol=0)
