@@ -47,8 +47,10 @@ KTHREADS = 128  # points per work item (the kernels' tile)
 
 
 def chunk_for(n_prisms, max_chunk=2048):
-    """Prism chunk of a request: a function of the request alone."""
-    return max(128, min(max_chunk, ((n_prisms + 127) // 128) * 128))
+    """Prism chunk of a request: a function of the request alone, in whole
+    128-prism tiles (the cap is rounded down to a whole tile)."""
+    cap = max(128, (int(max_chunk) // 128) * 128)
+    return max(128, min(cap, ((n_prisms + 127) // 128) * 128))
 
 
 def _fail(req, exc):

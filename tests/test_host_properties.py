@@ -1,0 +1,89 @@
+"""
+Property-based tests (hypothesis) of host helpers: shard partitions, chunk
+sizes of the serving loop, longitude continuity of tesseroids, the prism
+boundary check and the magnetic vector conversions.  CPU only; skipped where
+hypothesis is not installed.
+"""
+
+import numpy as np
+import numpy.testing as npt
+import pytest
+
+hypothesis = pytest.importorskip("hypothesis")
+st = pytest.importorskip("hypothesis.strategies")
+given, settings = hypothesis.given, hypothesis.settings
+
+from harmonica_gb300.gravity import check_prisms  # noqa: E402
+from harmonica_gb300.magnetic_utils import (  # noqa: E402
+    magnetic_angles_to_vec,
+    magnetic_vec_to_angles,
+)
+from harmonica_gb300.serve import chunk_for  # noqa: E402
+from harmonica_gb300.sharding import shard_bounds  # noqa: E402
+from harmonica_gb300.tesseroid import longitude_continuity  # noqa: E402
+
+FAST = settings(max_examples=200, deadline=None)
+
+
+@FAST
+@given(st.integers(0, 10**7), st.integers(1, 64))
+def test_shards_partition_the_points(n, world):
+    spans = [shard_bounds(n, r, world) for r in range(world)]
+    assert spans[0][0] == 0 and spans[-1][1] == n
+    assert all(a[1] == b[0] for a, b in zip(spans, spans[1:]))
+    sizes = [hi - lo for lo, hi in spans]
+    assert min(sizes) >= 0 and max(sizes) - min(sizes) <= 1
+
+
+@FAST
+@given(st.integers(0, 10**8), st.integers(128, 1 << 16))
+def test_chunks_are_whole_tiles(n_prisms, max_chunk):
+    chunk = chunk_for(n_prisms, max_chunk)
+    assert chunk % 128 == 0 and 128 <= chunk <= max(128, max_chunk)
+    if n_prisms <= (max_chunk // 128) * 128:
+        assert chunk >= n_prisms  # one chunk holds the whole request
+
+
+_lon = st.floats(-180, 360, allow_nan=False)
+
+
+@FAST
+@given(st.lists(st.tuples(_lon, _lon), min_size=1, max_size=20))
+def test_longitude_continuity(pairs):
+    tess = np.array([[w, e, -1.0, 1.0, 1.0, 2.0] for w, e in pairs])
+    out = longitude_continuity(tess)
+    moved = tess[:, 0] > tess[:, 1]
+    # rows with west <= east are untouched, the others moved into [-180, 180)
+    npt.assert_array_equal(out[~moved], tess[~moved])
+    for col in (0, 1):
+        new = out[moved, col]
+        assert np.all((new >= -180) & (new < 180))
+        # the same meridian: a whole number of turns apart
+        turns = (tess[moved, col] - new) / 360.0
+        npt.assert_allclose(turns, np.round(turns), atol=1e-9)
+    npt.assert_array_equal(out[:, 2:], tess[:, 2:])
+
+
+_coord = st.floats(-1e4, 1e4, allow_nan=False)
+
+
+@FAST
+@given(st.lists(st.tuples(*[_coord] * 6), min_size=1, max_size=10))
+def test_check_prisms_raises_exactly_on_inverted_boundaries(rows):
+    prisms = np.array(rows)
+    bad = ((prisms[:, 0] > prisms[:, 1]) | (prisms[:, 2] > prisms[:, 3])
+           | (prisms[:, 4] > prisms[:, 5]))
+    if bad.any():
+        with pytest.raises(ValueError, match="Invalid prism or prisms"):
+            check_prisms(prisms)
+    else:
+        check_prisms(prisms)
+
+
+@FAST
+@given(st.floats(1e-3, 1e5), st.floats(-89.9, 89.9), st.floats(-179.9, 179.9))
+def test_magnetic_angles_round_trip(intensity, inclination, declination):
+    vec = magnetic_angles_to_vec(intensity, inclination, declination)
+    npt.assert_allclose(magnetic_vec_to_angles(*vec), (intensity, inclination, declination),
+                        rtol=1e-9, atol=1e-9)
+    npt.assert_allclose(np.linalg.norm(vec), intensity, rtol=1e-12)
