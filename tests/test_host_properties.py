@@ -87,3 +87,72 @@ def test_magnetic_angles_round_trip(intensity, inclination, declination):
     npt.assert_allclose(magnetic_vec_to_angles(*vec), (intensity, inclination, declination),
                         rtol=1e-9, atol=1e-9)
     npt.assert_allclose(np.linalg.norm(vec), intensity, rtol=1e-12)
+
+
+def _tesseroid_errors(t):
+    """Whether the reference's checks reject these tesseroids (its order of
+    conditions, longitudes made continuous before the west/east checks)."""
+    w, e, s, n, b, top = (t[:, i].copy() for i in range(6))
+    if np.any((s < -90) | (s > 90) | (n < -90) | (n > 90)) or np.any(s > n):
+        return True
+    if np.any((b < 0) | (top < 0)) or np.any(b > top):
+        return True
+    if np.any((w < -180) | (w > 360) | (e < -180) | (e > 360)):
+        return True
+    flip = w > e
+    w[flip] = ((w[flip] + 180) % 360) - 180
+    e[flip] = ((e[flip] + 180) % 360) - 180
+    return bool(np.any(w > e) or np.any(e - w > 360))
+
+
+_lat = st.floats(-95, 95, allow_nan=False)
+_rad = st.floats(-1.0, 1e4, allow_nan=False)
+_lon_wide = st.floats(-185, 365, allow_nan=False)
+
+
+def _row(values):
+    """Latitudes and radii put in order unless the flags leave them as drawn,
+    so that valid and invalid tesseroids are both common."""
+    w, e, s, n, b, t, keep_lat, keep_rad = values
+    if not keep_lat:
+        s, n = sorted((s, n))
+    if not keep_rad:
+        b, t = sorted((b, t))
+    return [w, e, s, n, b, t]
+
+
+@FAST
+@given(st.lists(st.tuples(_lon_wide, _lon_wide, _lat, _lat, _rad, _rad,
+                          st.booleans(), st.booleans()).map(_row),
+                min_size=1, max_size=4))
+def test_check_tesseroids_rejects_exactly_the_invalid(rows):
+    from harmonica_gb300.tesseroid import check_tesseroids
+
+    t = np.array(rows)
+    if _tesseroid_errors(t):
+        with pytest.raises(ValueError, match="Invalid tesseroid or tesseroids"):
+            check_tesseroids(t)
+    else:
+        out = check_tesseroids(t)
+        assert np.all(out[:, 0] <= out[:, 1])
+
+
+@settings(max_examples=25, deadline=None)
+@given(st.floats(-3.0, 3.0), st.floats(0.1, 5.0), st.floats(10.0, 5e3))
+def test_density_based_discretization_tiles_the_radial_range(amplitude, rate, thickness):
+    """The radial pieces of a tesseroid chain from its bottom to its top, in
+    the reference's order of discovery, and keep its horizontal bounds."""
+    from harmonica_gb300.tesseroid import density_based_discretization
+
+    bottom, top = 6.3e6, 6.3e6 + thickness
+
+    def density(radius):
+        return 2670.0 + 300.0 * amplitude * np.exp(-rate * (radius - bottom) / thickness)
+
+    pieces = density_based_discretization(np.array([[-1.0, 1.0, -2.0, 2.0, bottom, top]]),
+                                          density)
+    npt.assert_array_equal(pieces[:, :4], np.tile([-1.0, 1.0, -2.0, 2.0], (len(pieces), 1)))
+    radial = pieces[np.argsort(pieces[:, 4]), 4:]
+    assert radial[0, 0] == bottom and radial[-1, 1] == top
+    npt.assert_array_equal(radial[1:, 0], radial[:-1, 1])
+    assert np.all(radial[:, 0] < radial[:, 1])
