@@ -156,3 +156,32 @@ def test_density_based_discretization_tiles_the_radial_range(amplitude, rate, th
     assert radial[0, 0] == bottom and radial[-1, 1] == top
     npt.assert_array_equal(radial[1:, 0], radial[:-1, 1])
     assert np.all(radial[:, 0] < radial[:, 1])
+
+
+@settings(max_examples=50, deadline=None)
+@given(st.integers(2, 6), st.integers(2, 6), st.floats(1.0, 500.0), st.floats(1.0, 500.0),
+       st.integers(0, 2**31 - 1))
+def test_layer_prisms_index_and_order(n_north, n_east, s_north, s_east, seed):
+    """prism_layer: top >= bottom with {top, bottom} = {surface, reference}
+    on every cell, and ``get_prism((i, j))`` is row ``i * n_east + j`` of
+    ``_to_prisms()`` (the reference's (northing, easting) order).  Two or
+    more prisms per axis: like the reference, a one-prism axis has no
+    spacing and fails the regular-grid check."""
+    from harmonica_gb300 import prism_layer
+
+    rng = np.random.default_rng(seed)
+    easting = 1000.0 + s_east * np.arange(n_east)
+    northing = -500.0 + s_north * np.arange(n_north)
+    surface = rng.uniform(-1e3, 1e3, (n_north, n_east))
+    reference = rng.uniform(-1e3, 1e3, (n_north, n_east))
+    layer = prism_layer((easting, northing), surface, reference,
+                        properties={"density": rng.uniform(2000, 3000, (n_north, n_east))})
+    top, bottom = np.asarray(layer.top), np.asarray(layer.bottom)
+    assert np.all(top >= bottom)
+    npt.assert_array_equal(top, np.maximum(surface, reference))
+    npt.assert_array_equal(bottom, np.minimum(surface, reference))
+    prisms = layer.prism_layer._to_prisms()
+    assert prisms.shape == (n_north * n_east, 6)
+    for i in range(n_north):
+        for j in range(n_east):
+            npt.assert_array_equal(layer.prism_layer.get_prism((i, j)), prisms[i * n_east + j])
