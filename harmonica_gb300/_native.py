@@ -8,6 +8,7 @@ missing, :func:`lib` raises, so a GPU run can never silently compute on the
 CPU.
 """
 
+import contextlib
 import ctypes
 import os
 import shutil
@@ -66,14 +67,38 @@ def is_stale():
     return any(os.path.getmtime(d) > t for d in _deps())
 
 
+@contextlib.contextmanager
+def _build_lock():
+    """Exclusive lock across processes (ranks of one job, test workers) on
+    the build folder, so that only one of them compiles and links at a time."""
+    import fcntl  # noqa: PLC0415
+
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    with open(os.path.join(BUILD_DIR, ".build.lock"), "w") as handle:
+        fcntl.flock(handle, fcntl.LOCK_EX)
+        try:
+            yield
+        finally:
+            fcntl.flock(handle, fcntl.LOCK_UN)
+
+
 def build(force=False, verbose=False):
     """Compile every CUDA translation unit for sm_103a into one shared library.
 
     Objects are compiled in parallel, then linked with nvcc (static cudart).
+    Concurrent calls from several processes build once: the others wait for
+    the lock and find the library up to date (unless ``force``).
     """
     if not force and not is_stale():
         return LIB_PATH
-    os.makedirs(BUILD_DIR, exist_ok=True)
+    with _build_lock():
+        if not force and not is_stale():  # built by another process meanwhile
+            return LIB_PATH
+        _compile_and_link(verbose)
+    return LIB_PATH
+
+
+def _compile_and_link(verbose):
     nvcc = nvcc_path()
     common = [
         nvcc, *ARCH_FLAGS, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
@@ -96,13 +121,12 @@ def build(force=False, verbose=False):
             )
         if verbose and out:
             print(out.decode(errors="replace"))
-    tmp = LIB_PATH + ".tmp"
+    tmp = f"{LIB_PATH}.{os.getpid()}.tmp"
     link = [nvcc, *ARCH_FLAGS, "-shared", "-o", tmp, *objs]
     res = subprocess.run(link, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
     if res.returncode != 0:
         raise RuntimeError("nvcc link failed:\n" + res.stdout.decode(errors="replace"))
-    os.replace(tmp, LIB_PATH)
-    return LIB_PATH
+    os.replace(tmp, LIB_PATH)  # atomic: a loader sees the old or the new library
 
 
 _c_double_p = ctypes.c_void_p  # device pointers travel as integers

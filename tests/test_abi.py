@@ -158,3 +158,34 @@ def test_every_entry_point_rejects_bad_arguments_before_cuda():
     assert {k.split(":")[0] for k in report} == declared
     bad = {k: v for k, v in report.items() if v[0] != -1 or not v[1]}
     assert not bad, bad
+
+
+_LOCK_CHILD = r"""
+import sys, time
+sys.path.insert(0, sys.argv[1])
+from harmonica_gb300 import _native
+
+def fake_compile(verbose):
+    start = time.time()
+    time.sleep(0.5)
+    with open(sys.argv[2], "a") as log:
+        log.write(f"{start} {time.time()}\n")
+
+_native._compile_and_link = fake_compile
+_native.build(force=True)
+"""
+
+
+def test_concurrent_builds_are_serialised(tmp_path):
+    """Two processes building at once take turns on the build lock (the
+    compile step is replaced by a half-second stub in the children)."""
+    import subprocess
+    import sys
+
+    log = tmp_path / "intervals.txt"
+    procs = [subprocess.Popen([sys.executable, "-c", _LOCK_CHILD, ROOT, str(log)])
+             for _ in range(2)]
+    assert all(p.wait(timeout=120) == 0 for p in procs)
+    (a0, a1), (b0, b1) = sorted(tuple(map(float, line.split()))
+                                for line in log.read_text().splitlines())
+    assert a1 <= b0  # the second build started after the first one ended
