@@ -48,8 +48,18 @@ _lib = None
 
 
 def build_oracle():
-    """Compile ``prism_oracle.c`` with the Makefile next to this file."""
-    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    """Compile the C oracle with the Makefile next to this file, one process
+    at a time (a file lock in the build folder; make skips an up-to-date
+    library, and the library is renamed into place whole)."""
+    import fcntl  # noqa: PLC0415
+
+    os.makedirs(os.path.dirname(LIB_PATH), exist_ok=True)
+    with open(os.path.join(os.path.dirname(LIB_PATH), ".build.lock"), "w") as handle:
+        fcntl.flock(handle, fcntl.LOCK_EX)
+        try:
+            subprocess.run(["make", "-s", "-C", HERE], check=True)
+        finally:
+            fcntl.flock(handle, fcntl.LOCK_UN)
 
 
 def _load():
