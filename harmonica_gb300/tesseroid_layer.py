@@ -144,6 +144,14 @@ def tesseroid_layer(coordinates, surface, reference, properties=None):
     data = None
     if properties:
         data = {name: np.asarray(value) for name, value in properties.items()}
+        for name, value in data.items():
+            # xarray refuses these too (its dimensions would conflict)
+            if value.shape != (latitude.size, longitude.size):
+                raise ValueError(
+                    f"Invalid property '{name}' with shape '{value.shape}'. "
+                    "Its shape should be (latitude, longitude) = "
+                    + f"'{(latitude.size, longitude.size)}'."
+                )
     if xr is not None:
         data_vars = {k: (DIMS, v) for k, v in (data or {}).items()}
         layer = xr.Dataset(data_vars, coords={"longitude": longitude, "latitude": latitude})

@@ -142,3 +142,14 @@ def test_tesseroid_device_entry_checks_sizes_and_layout():
     with pytest.raises(ValueError, match="status"):
         tesseroid_gravity_device(pts, pts, pts, tess, torch.zeros(3, dtype=torch.float64), "g_z",
                                  status=torch.zeros(1, dtype=torch.int64))
+
+
+def test_tesseroid_layer_property_shapes():
+    longitude, latitude = np.linspace(-10, 10, 5), np.linspace(-5, 5, 3)
+    surface = np.full((3, 5), 6.371e6)
+    layer = hg.tesseroid_layer((longitude, latitude), surface, 6.36e6,
+                               properties={"density": np.ones((3, 5))})
+    assert layer.tesseroid_layer.shape == (3, 5)
+    with pytest.raises(ValueError, match="Invalid property 'density'"):
+        hg.tesseroid_layer((longitude, latitude), surface, 6.36e6,
+                           properties={"density": np.ones((5, 3))})
