@@ -183,6 +183,24 @@ Plan make_plan(int64_t n_obs, int64_t n_prisms, uint32_t mask) {
   return p;
 }
 
+// The plan with at most as many prism chunks as `max_bytes` of partial sums
+// hold: longer chunks (a whole number of tiles) when the plan's own chunking
+// needs more, one chunk (no partial sums at all) when fewer than two fit.
+Plan cap_plan(Plan p, int64_t n_obs, int64_t n_prisms, size_t max_bytes) {
+  if (p.workspace_bytes <= max_bytes) return p;
+  const size_t per_chunk = (size_t)p.n_rows * (size_t)n_obs * sizeof(double);
+  const int64_t max_chunks = (int64_t)(max_bytes / per_chunk);
+  int64_t n_prism_tiles = (n_prisms + kTile - 1) / kTile;
+  if (n_prism_tiles < 1) n_prism_tiles = 1;
+  const int64_t tiles_per_chunk =
+      max_chunks < 2 ? n_prism_tiles : (n_prism_tiles + max_chunks - 1) / max_chunks;
+  p.chunk = tiles_per_chunk * kTile;
+  p.n_chunks = (n_prisms + p.chunk - 1) / p.chunk;
+  if (p.n_chunks < 1) p.n_chunks = 1;
+  p.workspace_bytes = p.n_chunks > 1 ? (size_t)p.n_chunks * per_chunk : 0;
+  return p;
+}
+
 template <class Source>
 int launch_forward(const Plan& plan, const double* oe, const double* on, const double* ou,
                    int64_t n_obs, const Source& src, int64_t n_prisms, uint32_t mask, double* out,
@@ -192,21 +210,27 @@ int launch_forward(const Plan& plan, const double* oe, const double* on, const d
   const bool direct = plan.n_chunks == 1;
   double* dst = out;
   int64_t chunk_stride = 0;
-  bool own_ws = false;
+  // A workspace this call allocated itself is released on every return path.
+  struct OwnedWorkspace {
+    void* ptr = nullptr;
+    cudaStream_t stream = nullptr;
+    ~OwnedWorkspace() {
+      if (ptr) cudaFreeAsync(ptr, stream);
+    }
+  } owned;
   if (!direct) {
     if (workspace == nullptr) {
       cudaError_t e = cudaMallocAsync(&workspace, plan.workspace_bytes, stream);
       if (e != cudaSuccess) return cuda_check(e, "cudaMallocAsync(workspace)");
-      own_ws = true;
+      owned.ptr = workspace;
+      owned.stream = stream;
     }
     dst = static_cast<double*>(workspace);
     chunk_stride = (int64_t)plan.n_rows * n_obs;
   }
-  if (n_prisms == 0) {
-    cudaError_t e = cudaMemsetAsync(out, 0, sizeof(double) * plan.n_rows * n_obs, stream);
-    if (own_ws) cudaFreeAsync(workspace, stream);
-    return cuda_check(e, "cudaMemsetAsync(out)");
-  }
+  if (n_prisms == 0)
+    return cuda_check(cudaMemsetAsync(out, 0, sizeof(double) * plan.n_rows * n_obs, stream),
+                      "cudaMemsetAsync(out)");
   if (flag == nullptr) check_singular = false;
   dim3 grid((unsigned)plan.n_tiles, (unsigned)plan.n_chunks);
   const int scale = direct ? 1 : 0;
@@ -241,7 +265,6 @@ int launch_forward(const Plan& plan, const double* oe, const double* on, const d
     reduce_chunks_kernel<<<(unsigned)blocks, dim3(32, kReduceGroups), 0, stream>>>(
         dst, plan.n_chunks, chunk_stride, n_obs, plan.n_rows, rf, out);
     rc = cuda_check(cudaGetLastError(), "reduce_chunks_kernel launch");
-    if (own_ws) cudaFreeAsync(workspace, stream);
     if (rc != HG_OK) return rc;
   }
   return HG_OK;
@@ -354,7 +377,11 @@ int hg_layer_forward(const double* obs_e, const double* obs_n, const double* obs
 // neither hand it a workspace nor let it call cudaMallocAsync.
 // hg_prism_forward_noalloc runs the same kernels with that scratch taken from
 // a fixed array compiled into the library (kNoAllocScratchBytes = 8 MiB; every
-// GPU that loads the library holds it until the process exits).
+// GPU that loads the library holds it until the process exits).  Problems
+// whose usual chunking would need more partial sums than the array holds run
+// with fewer, longer chunks (cap_plan), down to one chunk, which needs no
+// scratch; so no problem is rejected for its size, and the only cost is less
+// parallelism for many fields at once over tens of thousands of points.
 
 namespace {
 
@@ -373,7 +400,9 @@ std::mutex g_noalloc_mutex;
 double* g_noalloc_ptr[kNoAllocMaxDevices] = {};
 
 // Device address of g_noalloc_scratch on the current device, looked up with
-// cudaGetSymbolAddress the first time each device is used.
+// cudaGetSymbolAddress the first time each device is used and kept for the
+// life of the process (a device reset while the library is in use would
+// leave it stale: callers must not reset a device they use this entry on).
 int noalloc_scratch(double** ptr) {
   int dev = 0;
   int rc = cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
@@ -404,14 +433,15 @@ extern "C" int hg_prism_forward_noalloc(const double* obs_e, const double* obs_n
   if (n_obs > 0 && (!obs_e || !obs_n || !obs_u || !out))
     return set_error(HG_ERR_INVALID, "null pointer");
   if (n_prisms > 0 && !prisms_soa) return set_error(HG_ERR_INVALID, "null prisms pointer");
-  const Plan plan = make_plan(n_obs, n_prisms, field_mask);
+  const Plan plan =
+      cap_plan(make_plan(n_obs, n_prisms, field_mask), n_obs, n_prisms, kNoAllocScratchBytes);
+  // cap_plan keeps every plan within the array; this check guards that invariant
   if (plan.workspace_bytes > kNoAllocScratchBytes)
     return set_error(HG_ERR_INVALID,
                      "hg_prism_forward_noalloc: this problem needs " +
                          std::to_string(plan.workspace_bytes) +
                          " bytes of scratch, more than the fixed " +
-                         std::to_string(kNoAllocScratchBytes) +
-                         " bytes; request fewer fields or use hg_prism_forward with a workspace");
+                         std::to_string(kNoAllocScratchBytes) + " bytes");
   double* scratch = nullptr;
   if (plan.workspace_bytes > 0) {
     const int rc = noalloc_scratch(&scratch);

@@ -105,12 +105,17 @@ int hg_prism_forward(const double *obs_e, const double *obs_n, const double *obs
  * workspace) and calls no cudaMalloc/cudaFree: its scratch for partial sums
  * is a fixed 8 MiB array in the library's device image, held by every GPU
  * that loads the library until the process exits.
- *   - Problems whose partial sums need more than 8 MiB are rejected with
- *     HG_ERR_INVALID and a message giving the size (calls for up to three
- *     fields always fit; many fields at once with few points may not).
+ *   - When the usual split of the prisms into chunks would need more than
+ *     8 MiB of partial sums (n_chunks x fields x n_obs doubles), the prisms
+ *     are split into fewer, longer chunks, down to a single chunk, which
+ *     needs no scratch: no problem is rejected for its size.  Results then
+ *     differ from hg_prism_forward's only by the order in which the chunk
+ *     sums are added; many fields at once over tens of thousands of points
+ *     run with less parallelism.
  *   - The first call on each device looks up the array's device address
- *     (cudaGetSymbolAddress) with that device current; make that first call
- *     before any stream capture.
+ *     (cudaGetSymbolAddress) with that device current and keeps it for the
+ *     life of the process; make that first call before any stream capture,
+ *     and do not reset the device (cudaDeviceReset) while using this entry.
  *   - All calls on a device share the one array and it keeps the last call's
  *     contents (nothing in it needs to start at zero).  Calls that overlap on
  *     the GPU (e.g. on two streams at once) race on it: serialise them.

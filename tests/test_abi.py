@@ -110,6 +110,29 @@ def test_tesseroid_and_eqs_validation_without_gpu():
     assert b"null pointer" in lib.hg_last_error()
 
 
+def test_noalloc_validation_without_gpu():
+    """hg_prism_forward_noalloc checks its arguments before any CUDA call:
+    negative sizes, a bad field mask, a prism stride below the prism count
+    and null pointers with work to do are rejected with a message."""
+    from harmonica_gb300 import _native
+
+    lib = _native.lib()
+    f = lib.hg_prism_forward_noalloc
+    assert f(None, None, None, -1, None, 10, 10, 1 << 3, None, None, None) < 0
+    assert b"bad sizes" in lib.hg_last_error()
+    assert f(None, None, None, 4, None, 10, 10, 0, None, None, None) < 0
+    assert b"field mask" in lib.hg_last_error()
+    assert f(None, None, None, 4, None, 10, 10, 1 << 10, None, None, None) < 0
+    assert f(None, None, None, 4, None, 5, 10, 1 << 3, None, None, None) < 0
+    assert b"bad sizes" in lib.hg_last_error()
+    assert f(None, None, None, 4, None, 10, 10, 1 << 3, None, None, None) < 0
+    assert b"null pointer" in lib.hg_last_error()
+    assert lib.hg_prism_forward_noalloc(
+        ctypes.c_void_p(8), ctypes.c_void_p(8), ctypes.c_void_p(8), 4, None, 10, 10, 1 << 3,
+        ctypes.c_void_p(8), None, None) < 0
+    assert b"null prisms pointer" in lib.hg_last_error()
+
+
 _PROBE = r"""
 import ctypes, json, sys
 sys.path.insert(0, sys.argv[1])

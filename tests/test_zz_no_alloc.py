@@ -4,12 +4,16 @@ memory (host frameworks that own the device pool, loops that must not
 allocate mid-step, plugins with a fixed GPU budget).  It uses a fixed scratch
 array in the library instead of a caller workspace or cudaMallocAsync.
 
-Checked through the C ABI against hg_prism_forward (given a workspace) on
-two calls in a row, each with inputs that make the kernels use the scratch
+Checked through the C ABI against two references on the same inputs:
+hg_prism_forward given a workspace (the same kernels with caller scratch) and
+the CPU oracle (an independent restatement of the reference's loop).  Two
+calls run in a row, each with inputs that make the kernels use the scratch
 (few points, many prisms: the prisms are split into chunks whose partial sums
 live in the scratch); the second call also shows that the first call's
-scratch contents do not leak into it.  Tolerance: the FP64 parity tolerance
-of the GPU tests (1e-8 relative + 1e-9 of the largest value).
+scratch contents do not leak into it.  Problems whose usual chunking needs
+more partial sums than the scratch holds run with longer chunks and must
+still match.  Tolerance: the FP64 parity tolerance of the GPU tests (1e-8
+relative + 1e-9 of the largest value).
 
 This file is collected last on purpose: if it fails, a run that stops at the
 first failure has already run every other test.
@@ -22,6 +26,8 @@ import numpy.testing as npt
 import pytest
 
 pytestmark = pytest.mark.gpu
+
+FIELD_NAMES = ("potential", "g_e", "g_n", "g_z", "g_ee", "g_nn", "g_zz", "g_en", "g_ez", "g_nz")
 
 
 def _problem(seed, n_obs, n_prisms):
@@ -53,6 +59,8 @@ def _device_inputs(lib, coords, prisms, density):
 
 
 def _run_both(lib, coords, prisms, density, mask):
+    """(hg_prism_forward with a workspace, hg_prism_forward_noalloc, bytes of
+    the workspace the first one was given)."""
     import torch
 
     e, n, u, soa = _device_inputs(lib, coords, prisms, density)
@@ -73,38 +81,62 @@ def _run_both(lib, coords, prisms, density, mask):
                                       soa.data_ptr(), m, m, mask, new.data_ptr(), None, stream)
     assert rc == 0, lib.hg_last_error()
     torch.cuda.synchronize()
-    return ref.cpu().numpy(), new.cpu().numpy()
+    return ref.cpu().numpy(), new.cpu().numpy(), ws_bytes.value
 
 
 def _close(new, ref):
     npt.assert_allclose(new, ref, rtol=1e-8, atol=1e-9 * np.abs(ref).max())
 
 
-def test_noalloc_matches_workspace_entry_point_twice(gpu_lib):
+def _check_oracle(oracle, new, coords, prisms, density, mask, stations=None):
+    """Rows of `new` (one per field of `mask`) against the CPU oracle, on all
+    points or on the given subset of them."""
+    idx = np.arange(coords[0].size) if stations is None else np.asarray(stations)
+    sub = tuple(np.ascontiguousarray(c[idx]) for c in coords)
+    row = 0
+    for code, name in enumerate(FIELD_NAMES):
+        if (mask >> code) & 1:
+            ref = oracle.prism_gravity(sub, prisms, density, field=name)
+            _close(new[row][idx], ref)
+            row += 1
+
+
+def test_noalloc_matches_workspace_entry_point_and_oracle_twice(gpu_lib, oracle):
     lib = gpu_lib
     # first call: g_z, 300 points x 6000 prisms (the prisms are split in chunks)
     coords, prisms, density = _problem(11, 300, 6000)
-    ref, new = _run_both(lib, coords, prisms, density, 1 << 3)
+    ref, new, _ = _run_both(lib, coords, prisms, density, 1 << 3)
     _close(new, ref)
+    _check_oracle(oracle, new, coords, prisms, density, 1 << 3)
     # second call right after, other inputs and two fields: stale scratch from
     # the first call must not show up
     coords, prisms, density = _problem(12, 177, 4100)
-    ref, new = _run_both(lib, coords, prisms, density, (1 << 0) | (1 << 6))
+    mask = (1 << 0) | (1 << 6)
+    ref, new, _ = _run_both(lib, coords, prisms, density, mask)
     _close(new, ref)
+    _check_oracle(oracle, new, coords, prisms, density, mask)
 
 
-def test_noalloc_rejects_problems_beyond_its_scratch(gpu_lib):
-    import torch
-
+def test_noalloc_runs_problems_beyond_the_usual_chunking(gpu_lib, oracle):
+    """Problems whose usual chunking needs more partial sums than the fixed
+    scratch holds (8 MiB) run with longer chunks instead of being rejected."""
     lib = gpu_lib
-    # all ten fields for two tiles of points against many prisms needs
-    # more partial sums than the fixed scratch holds
-    coords, prisms, density = _problem(13, 250, 200_000)
-    e, n, u, soa = _device_inputs(lib, coords, prisms, density)
-    out = torch.empty((10, e.numel()), dtype=torch.float64, device=e.device)
-    rc = lib.hg_prism_forward_noalloc(e.data_ptr(), n.data_ptr(), u.data_ptr(), e.numel(),
-                                      soa.data_ptr(), soa.shape[1], soa.shape[1], 0x3FF,
-                                      out.data_ptr(), None,
-                                      torch.cuda.current_stream().cuda_stream)
-    assert rc < 0
-    assert b"bytes of scratch" in lib.hg_last_error()
+    # g_z, 128 points x 2e6 prisms: the usual chunking wants ~16 MB
+    coords, prisms, density = _problem(13, 128, 2_000_000)
+    ref, new, ws = _run_both(lib, coords, prisms, density, 1 << 3)
+    assert ws > 8 << 20
+    _close(new, ref)
+    _check_oracle(oracle, new, coords, prisms, density, 1 << 3, stations=np.arange(0, 128, 16))
+    # all ten fields, 250 points x 200 000 prisms: the usual chunking wants
+    # far more than 8 MiB
+    coords, prisms, density = _problem(14, 250, 200_000)
+    ref, new, ws = _run_both(lib, coords, prisms, density, 0x3FF)
+    assert ws > 8 << 20
+    _close(new, ref)
+    _check_oracle(oracle, new, coords, prisms, density, 0x3FF, stations=[0, 97, 249])
+    # ten fields over 60 000 points: fewer than two chunks fit, one chunk runs
+    coords, prisms, density = _problem(15, 60_000, 3000)
+    ref, new, ws = _run_both(lib, coords, prisms, density, 0x3FF)
+    assert ws > 8 << 20
+    _close(new, ref)
+    _check_oracle(oracle, new, coords, prisms, density, 0x3FF, stations=[1, 30_000, 59_999])
