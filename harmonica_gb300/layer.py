@@ -4,15 +4,18 @@ Layer of prisms on a regular horizontal grid and its ``prism_layer`` accessor.
 Mirrors harmonica ``src/harmonica/_forward/prisms/layer.py``:
 ``prism_layer`` (:23-138), ``_check_regular_grid`` (:141-155) and
 ``DatasetAccessorPrismLayer`` (:157-519, without ``to_pyvista``, which is
-visualization).  The forward sum of ``gravity`` (:314-433) runs on the GPU
-through the C ABI ``hg_layer_forward``, which builds the prism boundaries
-from the grid on the fly and applies the same skips (:596-607).
+visualization).  The members the prism and tesseroid layers share live in
+:mod:`harmonica_gb300._grid_layer`.  The forward sum of ``gravity``
+(:314-433) runs on the GPU through the C ABI ``hg_layer_forward``, which
+builds the prism boundaries from the grid on the fly and applies the same
+skips (:596-607).
 
 When :mod:`xarray` is importable, ``prism_layer`` returns an
-``xarray.Dataset`` and the accessor is registered as ``.prism_layer``, like
-the reference.  Without xarray it returns a :class:`PrismLayer`, a small
-numpy container with the same attribute surface (``easting``, ``northing``,
-``top``, ``bottom``, data variables, ``coords``, ``attrs``, ``.prism_layer``).
+``xarray.Dataset`` and the accessor is registered on it as ``.prism_layer``
+when this module is imported, like the reference.  Without xarray it returns
+a :class:`PrismLayer`, a numpy container with the same attribute surface
+(``easting``, ``northing``, ``top``, ``bottom``, data variables, ``coords``,
+``attrs``, ``.prism_layer``).
 """
 
 import warnings
@@ -20,47 +23,28 @@ import warnings
 import numpy as np
 
 from . import _native
+from ._grid_layer import (
+    GridDataset,
+    GridLayerAccessor,
+    check_even_spacing,
+    check_property_shapes,
+    grid_axes,
+    new_layer_dataset,
+    register_layer_accessor,
+)
 from ._trace import stage
 from .fields import FIELD_CODES, field_mask
-
-try:  # optional, as in the reference environment
-    import xarray as xr
-except ImportError:  # pragma: no cover - depends on the environment
-    xr = None
 
 DIMS = ("northing", "easting")
 
 
 def _check_regular_grid(easting, northing):
-    """Same check and messages as layer.py:141-155."""
-    if not np.allclose(easting[1] - easting[0], easting[1:] - easting[:-1]):
-        msg = "Passed easting coordinates are not evenly spaced."
-        raise ValueError(msg)
-    if not np.allclose(northing[1] - northing[0], northing[1:] - northing[:-1]):
-        msg = "Passed northing coordinates are not evenly spaced."
-        raise ValueError(msg)
+    """ValueError unless both axes are evenly spaced (layer.py:141-155)."""
+    check_even_spacing(easting, "easting")
+    check_even_spacing(northing, "northing")
 
 
-class _Var(np.ndarray):
-    """ndarray with a ``.values`` view, standing in for an xarray.DataArray."""
-
-    @property
-    def values(self):
-        return self.view(np.ndarray)
-
-
-def _var(a):
-    return np.array(a, dtype=np.float64 if np.asarray(a).dtype.kind in "iu" else None).view(_Var)
-
-
-class _Coords(dict):
-    def __setitem__(self, key, value):
-        if isinstance(value, tuple) and len(value) == 2:
-            value = value[1]
-        super().__setitem__(key, _var(value))
-
-
-class PrismLayer:
+class PrismLayer(GridDataset):
     """
     Numpy stand-in for the xarray Dataset that ``prism_layer`` builds.
 
@@ -68,52 +52,8 @@ class PrismLayer:
     ``bottom`` (n_n, n_e), data variables (n_n, n_e), ``attrs``.
     """
 
-    def __init__(self, easting, northing, data=None, attrs=None):
-        object.__setattr__(self, "coords", _Coords())
-        object.__setattr__(self, "data_vars", {})
-        object.__setattr__(self, "attrs", dict(attrs or {}))
-        self.coords["easting"] = np.asarray(easting, dtype=np.float64)
-        self.coords["northing"] = np.asarray(northing, dtype=np.float64)
-        for name, value in (data or {}).items():
-            self.data_vars[name] = _var(np.asarray(value))
-
-    def __getattr__(self, name):
-        coords = object.__getattribute__(self, "coords")
-        if name in coords:
-            return coords[name]
-        data_vars = object.__getattribute__(self, "data_vars")
-        if name in data_vars:
-            return data_vars[name]
-        if name == "prism_layer":
-            return DatasetAccessorPrismLayer(self)
-        raise AttributeError(name)
-
-    def __getitem__(self, name):
-        if name in self.data_vars:
-            return self.data_vars[name]
-        return self.coords[name]
-
-    def __contains__(self, name):
-        return name in self.data_vars or name in self.coords
-
-    @property
-    def dims(self):
-        return {"northing": self.northing.size, "easting": self.easting.size}
-
-    def __repr__(self):
-        return (
-            f"<PrismLayer northing: {self.northing.size}, easting: {self.easting.size}; "
-            f"coords: {list(self.coords)}; data_vars: {list(self.data_vars)}>"
-        )
-
-
-def _grid_axes(coordinates):
-    easting, northing = (np.asarray(c, dtype=np.float64) for c in coordinates[:2])
-    if easting.ndim == 2:
-        easting = easting[0, :]
-    if northing.ndim == 2:
-        northing = northing[:, 0]
-    return easting, northing
+    def __init__(self, easting, northing, data=None):
+        super().__init__(DIMS, {"easting": easting, "northing": northing}, data)
 
 
 def prism_layer(coordinates, surface, reference, properties=None):
@@ -138,109 +78,29 @@ def prism_layer(coordinates, surface, reference, properties=None):
         Layer with ``easting``, ``northing``, ``top``, ``bottom`` coordinates
         and the properties as data variables.
     """
-    easting, northing = _grid_axes(coordinates)
-    data = None
-    if properties:
-        data = {name: np.asarray(value) for name, value in properties.items()}
-        for name, value in data.items():
-            # xarray refuses these too (its dimensions would conflict)
-            if value.shape != (northing.size, easting.size):
-                raise ValueError(
-                    f"Invalid property '{name}' with shape '{value.shape}'. "
-                    "Its shape should be (northing, easting) = "
-                    + f"'{(northing.size, easting.size)}'."
-                )
-    if xr is not None:
-        data_vars = {k: (DIMS, v) for k, v in (data or {}).items()}
-        prisms = xr.Dataset(data_vars, coords={"easting": easting, "northing": northing})
-    else:
-        prisms = PrismLayer(easting, northing, data)
-    _check_regular_grid(prisms.easting.values, prisms.northing.values)
-    prisms.attrs = {"coords_units": "meters", "properties_units": "SI"}
-    DatasetAccessorPrismLayer(prisms).update_top_bottom(surface, reference)
-    return prisms
+    easting, northing = grid_axes(coordinates)
+    data = check_property_shapes(properties, *DIMS, (northing.size, easting.size))
+    layer = new_layer_dataset(DIMS, {"easting": easting, "northing": northing}, data,
+                              lambda dims, axes, d: PrismLayer(axes["easting"],
+                                                               axes["northing"], d))
+    _check_regular_grid(easting, northing)
+    layer.attrs = {"coords_units": "meters", "properties_units": "SI"}
+    DatasetAccessorPrismLayer(layer).update_top_bottom(surface, reference)
+    return layer
 
 
-class DatasetAccessorPrismLayer:
+@register_layer_accessor("prism_layer")
+class DatasetAccessorPrismLayer(GridLayerAccessor):
     """
     Accessor for a layer of prisms (layer.py:157-519).
 
     Use it through the ``prism_layer`` attribute of the layer returned by
-    :func:`prism_layer`.
+    :func:`prism_layer`: ``spacing`` is ``(s_north, s_east)``, ``shape``
+    ``(n_north, n_east)``, ``boundaries`` ``(west, east, south, north)``.
     """
 
-    def __init__(self, xarray_obj):
-        self._obj = xarray_obj
-
-    @property
-    def dims(self):
-        """The dims tuple of the layer: ``("northing", "easting")``."""
-        return DIMS
-
-    @property
-    def spacing(self):
-        """Spacing between prism centres: ``(s_north, s_east)``."""
-        easting, northing = self._obj.easting.values, self._obj.northing.values
-        _check_regular_grid(easting, northing)
-        s_north, s_east = northing[1] - northing[0], easting[1] - easting[0]
-        return s_north, s_east
-
-    @property
-    def boundaries(self):
-        """Boundaries of the layer: ``(west, east, south, north)``."""
-        s_north, s_east = self.spacing
-        west = self._obj.easting.values.min() - s_east / 2
-        east = self._obj.easting.values.max() + s_east / 2
-        south = self._obj.northing.values.min() - s_north / 2
-        north = self._obj.northing.values.max() + s_north / 2
-        return west, east, south, north
-
-    @property
-    def size(self):
-        """Total number of prisms in the layer."""
-        return self._obj.northing.size * self._obj.easting.size
-
-    @property
-    def shape(self):
-        """Number of prisms per direction: ``(n_north, n_east)``."""
-        return (self._obj.northing.size, self._obj.easting.size)
-
-    def _get_prism_horizontal_boundaries(self, easting, northing):
-        spacing = self.spacing
-        west = easting - spacing[1] / 2
-        east = easting + spacing[1] / 2
-        south = northing - spacing[0] / 2
-        north = northing + spacing[0] / 2
-        return west, east, south, north
-
-    def update_top_bottom(self, surface, reference):
-        """
-        Set ``top``/``bottom`` from ``surface`` and ``reference``
-        (layer.py:264-312): the top is the higher of the two on every cell.
-        """
-        surface, reference = np.asarray(surface), np.asarray(reference)
-        if surface.shape != self.shape:
-            raise ValueError(
-                f"Invalid surface array with shape '{surface.shape}'. "
-                + "Its shape should be compatible with the coordinates "
-                + "of the layer of prisms."
-            )
-        if reference.ndim != 0:
-            if reference.shape != self.shape:
-                raise ValueError(
-                    f"Invalid reference array with shape '{reference.shape}'. "
-                    + "Its shape should be compatible with the coordinates "
-                    + "of the layer of prisms."
-                )
-        else:
-            reference = reference * np.ones(self.shape)
-        top = surface.copy()
-        bottom = reference.copy()
-        reverse = surface < reference
-        top[reverse] = reference[reverse]
-        bottom[reverse] = surface[reverse]
-        self._obj.coords["top"] = (self.dims, top)
-        self._obj.coords["bottom"] = (self.dims, bottom)
+    _dims = DIMS
+    _bodies = "prisms"
 
     def gravity(
         self,
@@ -293,24 +153,11 @@ class DatasetAccessorPrismLayer:
 
     def _to_prisms(self):
         """Boundaries of every prism, one row each, in (northing, easting) order."""
-        easting, northing = np.meshgrid(self._obj.easting.values, self._obj.northing.values)
-        west, east, south, north = self._get_prism_horizontal_boundaries(
-            easting.ravel(), northing.ravel()
-        )
-        bottom = np.asarray(self._obj.bottom.values).ravel()
-        top = np.asarray(self._obj.top.values).ravel()
-        return np.vstack((west, east, south, north, bottom, top)).T
+        return self._cells()
 
     def get_prism(self, indices):
         """Boundaries of the prism at ``(index_northing, index_easting)``."""
-        center_easting = self._obj.easting.values[indices[1]]
-        center_northing = self._obj.northing.values[indices[0]]
-        west, east, south, north = self._get_prism_horizontal_boundaries(
-            center_easting, center_northing
-        )
-        bottom = self._obj.bottom.values[indices]
-        top = self._obj.top.values[indices]
-        return west, east, south, north, bottom, top
+        return self._cell(indices)
 
 
 def layer_forward(coords, easting, northing, bottom, top, density, mask, threshold, device=None):

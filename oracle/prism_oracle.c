@@ -234,6 +234,94 @@ void oracle_layer_gravity(int field, int64_t n_obs, const double *easting, const
     (void)n_threads;
 }
 
+/*
+ * All ten raw kernels of one prism at one point at once, each equal bit for
+ * bit to oracle_prism_kernel(field, ...): the three logs ln(a + r) and the
+ * three arctangents of a vertex are the same expressions for every field
+ * (vertex_term), so they are evaluated once per vertex and combined per
+ * field in the same operation order; the vertex sums run in the same order.
+ */
+static void prism_kernel_all(double e, double n, double u, const double *p, double rho,
+                             double out[10])
+{
+    double xs[2] = {p[0] - e, p[1] - e};
+    double ys[2] = {p[2] - n, p[3] - n};
+    double zs[2] = {p[4] - u, p[5] - u};
+    double sum[10] = {0.0};
+    for (int i = 0; i < 2; i++)
+        for (int j = 0; j < 2; j++)
+            for (int k = 0; k < 2; k++) {
+                double sign = ((i + j + k) % 2 == 1) ? 1.0 : -1.0;
+                double x = xs[i], y = ys[j], z = zs[k];
+                double r = sqrt(x * x + y * y + z * z);
+                double lz = log_plus_r(z, x, y, r); /* ln(z + r) */
+                double lx = log_plus_r(x, y, z, r); /* ln(x + r) */
+                double ly = log_plus_r(y, z, x, r); /* ln(y + r) */
+                double ax = x == 0.0 ? 0.0 : atan(y * z / (x * r));
+                double ay = y == 0.0 ? 0.0 : atan(z * x / (y * r));
+                double az = z == 0.0 ? 0.0 : atan(x * y / (z * r));
+#define CL(coef, l) ((coef) == 0.0 ? 0.0 : (coef) * (l))
+#define CA(coef, a) ((coef) == 0.0 ? 0.0 : (coef) * (a))
+                double t[10];
+                t[0] = CL(x * y, lz) + CL(y * z, lx) + CL(z * x, ly) - CA(0.5 * x * x, ax) -
+                       CA(0.5 * y * y, ay) - CA(0.5 * z * z, az);
+                t[1] = CL(y, lz) + CL(z, ly) - CA(x, ax);
+                t[2] = CL(z, lx) + CL(x, lz) - CA(y, ay);
+                t[3] = CL(x, ly) + CL(y, lx) - CA(z, az);
+#undef CL
+#undef CA
+                t[4] = -face_atan(x, y, z, r, i);
+                t[5] = -face_atan(y, z, x, r, j);
+                t[6] = -face_atan(z, x, y, r, k);
+                t[7] = lz;
+                t[8] = ly;
+                t[9] = lx;
+                for (int f = 0; f < 10; f++) sum[f] += sign * t[f];
+            }
+    for (int f = 0; f < 10; f++) {
+        double pref = ORACLE_G * rho;
+        if (f >= 1 && f <= 3) pref = -pref;
+        out[f] = (f >= 4 && oracle_is_singular(f, e, n, u, p)) ? NAN : pref * sum[f];
+    }
+}
+
+/*
+ * All ten fields of the prism-layer forward (oracle_layer_gravity for every
+ * field in one pass, same loop order and skips); out is (10, n_obs).
+ */
+void oracle_layer_gravity_all(int64_t n_obs, const double *easting, const double *northing,
+                              const double *upward, int64_t n_east, int64_t n_north,
+                              const double *centre_e, const double *centre_n,
+                              const double *bottom, const double *top, const double *density,
+                              double threshold, double *out, int n_threads)
+{
+    double half_e = (centre_e[1] - centre_e[0]) / 2.0;
+    double half_n = (centre_n[1] - centre_n[0]) / 2.0;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 4) num_threads(n_threads > 0 ? n_threads : 1)
+#endif
+    for (int64_t i = 0; i < n_obs; i++) {
+        double acc[10];
+        for (int f = 0; f < 10; f++) acc[f] = out[f * n_obs + i];
+        for (int64_t j = 0; j < n_east; j++) {
+            double w = centre_e[j] - half_e, e = centre_e[j] + half_e;
+            for (int64_t k = 0; k < n_north; k++) {
+                double rho = density[k * n_east + j];
+                if (rho == 0.0 || isnan(rho)) continue;
+                double b = bottom[k * n_east + j], t = top[k * n_east + j];
+                if (t - b < threshold) continue;
+                if (isnan(t) || isnan(b)) continue;
+                double p[6] = {w, e, centre_n[k] - half_n, centre_n[k] + half_n, b, t};
+                double v[10];
+                prism_kernel_all(easting[i], northing[i], upward[i], p, rho, v);
+                for (int f = 0; f < 10; f++) acc[f] += v[f];
+            }
+        }
+        for (int f = 0; f < 10; f++) out[f * n_obs + i] = acc[f];
+    }
+    (void)n_threads;
+}
+
 /* Serial any-pair singular check with early exit, as gravity.py:272-449. */
 int oracle_any_singular(int field, int64_t n_obs, const double *easting, const double *northing,
                         const double *upward, int64_t n_prisms, const double *prisms)

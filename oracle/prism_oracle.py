@@ -87,6 +87,10 @@ def _load():
         ctypes.c_int, i64, dp, dp, dp, i64, i64, dp, dp, dp, dp, dp, ctypes.c_double, dp,
         ctypes.c_int,
     ]
+    lib.oracle_layer_gravity_all.restype = None
+    lib.oracle_layer_gravity_all.argtypes = [
+        i64, dp, dp, dp, i64, i64, dp, dp, dp, dp, dp, ctypes.c_double, dp, ctypes.c_int,
+    ]
     lib.oracle_any_singular.restype = ctypes.c_int
     lib.oracle_any_singular.argtypes = [ctypes.c_int, i64, dp, dp, dp, i64, dp]
     lib.oracle_point_gravity.restype = None
@@ -288,6 +292,34 @@ def layer_gravity(
     )
     scale_result(out, field)
     return out.reshape(cast.shape)
+
+
+def layer_gravity_fields(coordinates, easting, northing, bottom, top, density,
+                         thickness_threshold=None, n_threads=None):
+    """All ten fields of ``layer_gravity`` in one pass over the pairs (each
+    field equal bit for bit to ``layer_gravity`` of that field); returns a
+    dict field -> array in harmonica units."""
+    cast = np.broadcast(*coordinates[:3])
+    coordinates = tuple(
+        _f64(np.broadcast_to(np.asarray(c, dtype=np.float64), cast.shape)).ravel()
+        for c in coordinates[:3]
+    )
+    easting, northing = _f64(easting), _f64(northing)
+    bottom, top, density = _f64(bottom), _f64(top), _f64(density)
+    threshold = 0.0 if thickness_threshold is None else float(thickness_threshold)
+    e, n, u = coordinates
+    out = np.zeros((len(FIELDS), e.size), dtype=np.float64)
+    _load().oracle_layer_gravity_all(
+        e.size, _ptr(e), _ptr(n), _ptr(u), easting.size, northing.size, _ptr(easting),
+        _ptr(northing), _ptr(bottom), _ptr(top), _ptr(density), threshold, _ptr(out),
+        n_threads or default_threads(),
+    )
+    result = {}
+    for f, code in FIELD_CODES.items():
+        row = out[code].copy()
+        scale_result(row, f)
+        result[f] = row.reshape(cast.shape)
+    return result
 
 
 POINT_FIELDS = {
