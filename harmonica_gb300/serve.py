@@ -14,9 +14,17 @@ arrive at any time through :meth:`PrismServer.submit` and get a
   least-recently-used when memory is needed;
 * launches **rounds**: each round is one persistent launch (``hg_round_run``)
   over work items (request, 128-point tile, prism chunk) taken from every
-  admitted request, shortest remaining work first, up to a per-round budget
-  of point-prism pairs, so requests that arrive while others are on the GPU
-  join the next round instead of waiting for the earlier ones to finish;
+  admitted request, earliest virtual deadline first (arrival time plus the
+  request's pairs at the nominal rate: small requests overtake large ones,
+  and a large request's turn comes once its deadline is the earliest, so
+  none starves), up to a per-round budget of point-prism pairs, so requests
+  that arrive while others are on the GPU join the next round instead of
+  waiting for the earlier ones to finish;
+* optionally **sheds load** (``max_backlog_s``): a request is refused at
+  submission (its future fails with :class:`ServerOverloaded`) when the
+  pairs not yet finished, its own included, would take longer than that at
+  the measured rate, so the latency of the accepted requests stays bounded
+  under overload;
 * finishes requests with ``hg_round_reduce`` (each point's chunks added in
   fixed order), copies results to pinned host memory and resolves the
   futures, recording arrival-to-result latency.
@@ -44,6 +52,11 @@ from .fields import FIELD_CODES, TENSOR_FIELDS
 from .gravity import _prepare, pack_prisms
 
 KTHREADS = 128  # points per work item (the kernels' tile)
+
+
+class ServerOverloaded(RuntimeError):
+    """A request refused at submission because the server's backlog would
+    exceed its ``max_backlog_s``."""
 
 
 def chunk_for(n_prisms, max_chunk=2048):
@@ -93,6 +106,8 @@ class _Request:
         self.bytes = 0
         self.n_obs = coords[0].size
         self.n_prisms = prisms.shape[0] if prisms is not None else None
+        self.pairs = 0.0      # point-prism pairs of the request
+        self.deadline = 0.0   # virtual deadline: arrival + pairs / nominal rate
         self.next_item = 0
         self.n_items = 0
         self.chunk = 0
@@ -116,10 +131,19 @@ class PrismServer:
         Size of the device problem table (admitted requests at once).
     chunk : int
         Largest prism chunk of a work item.
+    nominal_rate : float
+        Pairs per second used for the virtual deadlines of the scheduling
+        order and as the first estimate of the GPU's rate for load shedding
+        (then replaced by the measured rate of finished rounds).
+    max_backlog_s : float or None
+        Refuse new requests (:class:`ServerOverloaded`) while the unfinished
+        pairs, the new request's included, exceed this many seconds of work;
+        ``None`` accepts everything.
     """
 
     def __init__(self, device=None, memory_budget=120e9, round_pairs=4e8, max_active=1024,
-                 chunk=2048, n_ctas=0, rounds_in_flight=2):
+                 chunk=2048, n_ctas=0, rounds_in_flight=2, nominal_rate=1e10,
+                 max_backlog_s=None):
         import torch
 
         from .gravity import _device
@@ -134,6 +158,12 @@ class PrismServer:
         self.max_chunk = int(chunk)
         self.n_ctas = int(n_ctas)
         self.rounds_in_flight = int(rounds_in_flight)
+        self.nominal_rate = float(nominal_rate)
+        self.max_backlog_s = None if max_backlog_s is None else float(max_backlog_s)
+        self.rate = float(nominal_rate)  # measured pairs/s of finished rounds
+        self.backlog_pairs = 0.0         # pairs of accepted requests not yet finished
+        self.rejected = 0
+        self._busy_since = None
         self.layers = collections.OrderedDict()
         self.inbox = queue.Queue()
         self.pending = collections.deque()
@@ -145,7 +175,7 @@ class PrismServer:
         self.rounds = 0
         self.pairs_done = 0.0
         self._ids = 0
-        self._lock = threading.Lock()
+        self._lock = threading.RLock()  # re-entered by future callbacks run under it
         self._stop = threading.Event()
         self._broken = None  # the exception that stopped the scheduler, if any
         with torch.cuda.device(self.dev):
@@ -226,17 +256,41 @@ class PrismServer:
         )
         if layer is None and prisms is None:
             raise ValueError("submit needs a registered layer key or prisms and density")
-        with self._lock:
-            rid = self._ids
-            self._ids += 1
-        req = _Request(rid, coords, field, layer, p_np if layer is None else None,
+        req = _Request(-1, coords, field, layer, p_np if layer is None else None,
                        d_np if layer is None else None,
                        check_singular and field in TENSOR_FIELDS)
         req.shape = cast.shape
+        with self._lock:
+            known = self.layers.get(layer) if layer is not None else None
+            n_prisms = known.n_prisms if known is not None else (req.n_prisms or 0)
+            req.pairs = float(req.n_obs) * float(n_prisms)
+            req.deadline = req.t_submit + req.pairs / self.nominal_rate
+            if (self.max_backlog_s is not None and self.backlog_pairs > 0
+                    and (self.backlog_pairs + req.pairs) / self.rate > self.max_backlog_s):
+                self.rejected += 1
+                req.future.set_exception(ServerOverloaded(
+                    f"request of {req.pairs:.3g} pairs refused: the backlog of "
+                    f"{self.backlog_pairs:.3g} pairs is {self.backlog_pairs / self.rate:.2f} s "
+                    f"of work (limit {self.max_backlog_s} s)"))
+                return req.future
+            req.id = self._ids
+            self._ids += 1
+            self.backlog_pairs += req.pairs
+        req.future.add_done_callback(self._forget_backlog(req))
         self.inbox.put(req)
         if self._broken is not None:  # the scheduler stopped while this was queued
             _fail(req, RuntimeError("the prism server stopped after an error"))
         return req.future
+
+    def _forget_backlog(self, req):
+        """Callback for a request's future: its pairs leave the backlog when
+        it finishes, fails or is cancelled."""
+
+        def done(_future):
+            with self._lock:
+                self.backlog_pairs = max(0.0, self.backlog_pairs - req.pairs)
+
+        return done
 
     def _check_open(self):
         if self._broken is not None:
@@ -253,7 +307,8 @@ class PrismServer:
     def stats(self):
         lat = np.array([r.t_done - r.t_submit for r in self.completed])
         out = {"completed": len(self.completed), "rounds": self.rounds,
-               "pairs_done": self.pairs_done, "errors": len(self.errors)}
+               "pairs_done": self.pairs_done, "errors": len(self.errors),
+               "rejected": self.rejected, "rate_pairs_per_s": self.rate}
         if lat.size:
             out.update(p50_ms=float(np.percentile(lat, 50) * 1e3),
                        p99_ms=float(np.percentile(lat, 99) * 1e3),
@@ -433,15 +488,17 @@ class PrismServer:
         return tensors + [e, n, u, soa, out, part], n_prisms, pinned_out
 
     def _plan_round(self):
-        """Items for the next round: shortest remaining work first, then grouped
-        by field (each field runs its own specialised persistent launch).
-        Returns (items, per-field item counts, finishing requests)."""
+        """Items for the next round: earliest virtual deadline first (ties in
+        arrival order), then grouped by field (each field runs its own
+        specialised persistent launch).  Returns (items, per-field item
+        counts, finishing requests)."""
         reqs = [r for r in self.active.values() if r.next_item < r.n_items]
         if not reqs:
-            return None, None, []
-        reqs.sort(key=lambda r: (r.n_items - r.next_item) * r.chunk)
+            return None, None, [], 0.0
+        reqs.sort(key=lambda r: (r.deadline, r.id))
         budget = self.round_pairs
         parts, finishing = [], []
+        pairs = 0.0
         for r in reqs:
             if budget <= 0:
                 break
@@ -453,6 +510,10 @@ class PrismServer:
             items[:, 1] = k // r.n_chunks  # tile
             items[:, 2] = k % r.n_chunks   # chunk
             items[:, 3] = 0
+            n_prisms = r.layer.n_prisms if r.layer else r.n_prisms
+            pts = np.minimum(KTHREADS, r.n_obs - items[:, 1].astype(np.int64) * KTHREADS)
+            prs = np.minimum(r.chunk, n_prisms - items[:, 2].astype(np.int64) * r.chunk)
+            pairs += float(np.dot(pts, prs))
             parts.append((FIELD_CODES[r.field], items))
             r.next_item += take
             budget -= take * per_item
@@ -462,9 +523,9 @@ class PrismServer:
         for code, items in parts:
             counts[code] += items.shape[0]
         order = sorted(range(len(parts)), key=lambda i: parts[i][0])  # stable
-        return np.concatenate([parts[i][1] for i in order]), counts, finishing
+        return np.concatenate([parts[i][1] for i in order]), counts, finishing, pairs
 
-    def _launch_round(self, items, counts, finishing):
+    def _launch_round(self, items, counts, finishing, pairs):
         torch = self.torch
         buf = self._ring[self._ring_next]
         self._ring_next = (self._ring_next + 1) % len(self._ring)
@@ -500,18 +561,19 @@ class PrismServer:
             ev = torch.cuda.Event()
             ev.record(self.compute)
         buf["event"] = ev
-        self.in_flight.append((ev, finishing, items, 0.0))
+        self.in_flight.append((ev, finishing, pairs, time.perf_counter()))
         self.rounds += 1
 
     def _retire(self, block=False):
         while self.in_flight:
-            ev, finishing, items, _ = self.in_flight[0]
+            ev, finishing, pairs, launched = self.in_flight[0]
             if not block and not ev.query():
                 return
             ev.synchronize()
             self.in_flight.popleft()
             block = False
             now = time.perf_counter()
+            self._measure_rate(pairs, launched, now)
             flags = None
             if any(r.check_singular for r in finishing):
                 with self.torch.cuda.stream(self.compute):
@@ -527,6 +589,16 @@ class PrismServer:
                     self._release(r)
                 self.completed.append(r)
                 r.future.set_result(result)
+
+    def _measure_rate(self, pairs, launched, now):
+        """Update the measured rate (pairs/s) from a finished round: its
+        pairs over the time since the later of its launch and the previous
+        round's end (rounds in flight overlap), smoothed over rounds."""
+        start = launched if self._busy_since is None else max(launched, self._busy_since)
+        self._busy_since = now if self.in_flight else None
+        if pairs > 0 and now > start:
+            sample = pairs / (now - start)
+            self.rate = sample if self.rounds <= 2 else 0.8 * self.rate + 0.2 * sample
 
     def _release(self, r):
         self.active.pop(r.id, None)
@@ -555,10 +627,10 @@ class PrismServer:
                 with stage("serve admit"):
                     self._admit()
                 if len(self.in_flight) < self.rounds_in_flight:
-                    items, counts, finishing = self._plan_round()
+                    items, counts, finishing, pairs = self._plan_round()
                     if items is not None:
                         with stage("serve round"):
-                            self._launch_round(items, counts, finishing)
+                            self._launch_round(items, counts, finishing, pairs)
                         continue
                 with stage("serve retire"):
                     self._retire(block=len(self.in_flight) >= self.rounds_in_flight)

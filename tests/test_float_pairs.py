@@ -17,8 +17,6 @@ import sys
 import numpy as np
 import pytest
 
-mpmath = pytest.importorskip("mpmath")
-
 sys.path.insert(0, os.path.join(os.path.dirname(__file__), "native"))
 
 
@@ -42,6 +40,7 @@ def pairs():
 
 
 def exact(kind, p, q):
+    mpmath = pytest.importorskip("mpmath")  # CPU test: the GPU image has no mpmath
     mpmath.mp.dps = 40
     res = []
     for i in range(p[0].size):

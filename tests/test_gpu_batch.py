@@ -106,3 +106,20 @@ def test_autotune_returns_a_candidate(gpu_lib, tmp_path):
     again = hg.autotune(probs, chunks=(256, 1024), cta_multipliers=(1,), repeats=1,
                         cache=str(tmp_path / "tune.json"))
     assert again == choice
+
+
+def test_batched_workload_full_size_against_oracle(gpu_lib, oracle):
+    """The batched workload at full size (256 problems of 1e3-2e5 prisms and
+    1e3-5e4 stations, g_z and g_zz): every 31st problem (both fields) against
+    the oracle on 48 of its stations (strided) and all of its prisms."""
+    probs = synthetic.batched_problems(256, seed=4)
+    res = hg.prism_gravity_batch(probs, disable_checks=True)
+    for k in range(0, 256, 31):
+        p = probs[k]
+        n = p["coordinates"][0].size
+        idx = np.linspace(0, n - 1, min(48, n)).astype(int)
+        sub = tuple(np.ascontiguousarray(c[idx]) for c in p["coordinates"])
+        ref = oracle.prism_gravity(sub, p["prisms"], p["density"], p["field"],
+                                   disable_checks=True)
+        npt.assert_allclose(res[k][idx], ref, rtol=1e-8, atol=1e-9 * np.abs(ref).max(),
+                            err_msg=f"problem {k} ({p['field']})")

@@ -136,18 +136,24 @@ def test_topography_1e4_full_size_against_oracle(gpu_lib, oracle):
 
 
 def test_topography_1e6_subset_against_oracle(gpu_lib, oracle):
-    """The 1000 x 1000-prism layer (all 1e6 prisms) on a subset of 16 stations."""
+    """The 1000 x 1000-prism layer (all 1e6 prisms) on 256 of its stations,
+    all ten fields, through the accessor (single-field kernels) and the fused
+    all-field layer launch, against the oracle's layer loop."""
+    from harmonica_gb300.layer import layer_forward
+
     L = synthetic.layer_topography_1e6()
     rng = np.random.default_rng(0)
-    idx = rng.choice(L["coordinates"][0].size, 16, replace=False)
+    idx = rng.choice(L["coordinates"][0].size, 256, replace=False)
     coords = tuple(c[idx] for c in L["coordinates"])
     layer = hg.prism_layer((L["easting"], L["northing"]), L["top"], L["bottom"],
                            properties={"density": L["density"]})
-    for field in ("g_z", "g_zz"):
-        res = layer.prism_layer.gravity(coords, field=field)
-        ref = oracle.layer_gravity(coords, L["easting"], L["northing"], L["bottom"], L["top"],
-                                   L["density"], field)
-        assert_parity(res, ref, msg=field)
+    ref = oracle.layer_gravity_fields(coords, L["easting"], L["northing"], L["bottom"],
+                                      L["top"], L["density"])
+    fused = layer_forward(coords, L["easting"], L["northing"], L["bottom"], L["top"],
+                          L["density"], 0x3FF, 0.0)
+    for code, field in enumerate(hg.FIELDS):
+        assert_parity(layer.prism_layer.gravity(coords, field=field), ref[field], msg=field)
+        assert_parity(fused[code], ref[field], msg=f"{field} fused")
 
 
 def test_layer_no_singular_warning(gpu_lib, dummy_layer):

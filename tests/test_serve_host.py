@@ -48,9 +48,15 @@ def _skeleton(budget=1e9, max_active=4):
     srv.rounds = 0
     srv.pairs_done = 0.0
     srv._ids = 0
-    srv._lock = threading.Lock()
+    srv._lock = threading.RLock()
     srv._stop = threading.Event()
     srv._broken = None
+    srv.nominal_rate = 1e10
+    srv.max_backlog_s = None
+    srv.rate = 1e10
+    srv.backlog_pairs = 0.0
+    srv.rejected = 0
+    srv._busy_since = None
     srv.table = (_native.HgProblemPlan * max_active)()
     srv.flags = torch.zeros(max_active, dtype=torch.int32)
     srv.uploads = []
@@ -261,3 +267,50 @@ def test_a_layer_in_use_is_neither_replaced_nor_dropped():
     with pytest.raises(RuntimeError, match="in use"):
         srv.unregister_layer("topo")
     assert srv.layers["topo"].n_prisms == 10
+
+
+def test_earliest_virtual_deadline_first_lets_no_request_starve():
+    """Rounds take items earliest virtual deadline first (arrival + pairs at
+    the nominal rate): a small request that arrives after a large one goes
+    first while its deadline is earlier, and the large one's turn comes as
+    soon as its deadline is the earliest, however many small requests follow."""
+    srv = _skeleton(max_active=8)
+    srv.nominal_rate = 1e3  # pairs/s: deadlines far apart for these small cases
+    srv.round_pairs = 1  # one work item per round
+    big = _submit(srv, n_obs=300, n_prisms=3)    # 900 pairs: deadline t0 + 0.9 s
+    small = _submit(srv, n_obs=10, n_prisms=3)   # 30 pairs: deadline t1 + 0.03 s
+    srv._admit()
+    reqs = {r.n_obs: r for r in srv.active.values()}
+    assert reqs[10].deadline < reqs[300].deadline
+    items, _, finishing, _ = srv._plan_round()
+    assert items[0, 0] == reqs[10].slot and finishing == [reqs[10]]
+    # a later small request whose deadline falls after the big one's waits
+    reqs[300].deadline = reqs[10].deadline - 1.0  # the big request has aged past it
+    late = _submit(srv, n_obs=10, n_prisms=3)
+    srv._admit()
+    items, _, _, _ = srv._plan_round()
+    assert items[0, 0] == reqs[300].slot
+    assert big.running() and small.running() and late.running()
+
+
+def test_load_shedding_refuses_requests_beyond_the_backlog_and_counts_them():
+    from harmonica_gb300.serve import ServerOverloaded
+
+    srv = _skeleton()
+    srv.max_backlog_s = 1.0
+    srv.rate = 1000.0  # pairs/s
+    first = _submit(srv, n_obs=200, n_prisms=3)  # 600 pairs: 0.6 s of work
+    assert srv.backlog_pairs == 600
+    coords, prisms, density = _problem(n_obs=200, n_prisms=3)
+    refused = srv.submit(coords, "g_z", prisms=prisms, density=density)  # 1.2 s > 1 s
+    with pytest.raises(ServerOverloaded, match="backlog"):
+        refused.result(0)
+    assert srv.rejected == 1 and srv.inbox.empty() and srv.backlog_pairs == 600
+    fits = _submit(srv, n_obs=100, n_prisms=3)  # 0.9 s with the first: accepted
+    assert srv.backlog_pairs == 900
+    # a finished or failed request leaves the backlog
+    first.set_running_or_notify_cancel()
+    first.set_result(np.zeros(200))
+    assert srv.backlog_pairs == 300
+    assert fits.cancel() and srv.backlog_pairs == 0
+    assert srv.stats()["rejected"] == 1

@@ -1,0 +1,110 @@
+"""
+The checkers against exact values (tests/golden/mp_truth.npz: 50-digit
+evaluations of the closed form), on the CPU:
+
+* the oracle (the per-vertex restatement of the reference's loop in FP64) is
+  within the parity bar of the exact values on near prisms, on face planes,
+  edge lines and vertices and on the 1e6-prism layer sample: this pins the
+  oracle itself, independently of the reference's printed 5-decimal numbers;
+* the edge/face formulation of the CUDA kernels, compiled for the host
+  (tests/native/host_pair.cu), meets the bars the GPU tests state
+  (tests/test_gpu_truth.py), so a GPU failure there points at the device
+  build, not the formulation.
+"""
+
+import ctypes
+import os
+import sys
+import warnings
+
+import numpy as np
+import numpy.testing as npt
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "native"))
+
+FIELDS = ("potential", "g_e", "g_n", "g_z", "g_ee", "g_nn", "g_zz", "g_en", "g_ez", "g_nz")
+RTOL, ATOL_FRAC = 1e-8, 1e-9
+
+
+@pytest.fixture(scope="module")
+def truth():
+    return np.load(os.path.join(HERE, "golden", "mp_truth.npz"))
+
+
+@pytest.fixture(scope="module")
+def host():
+    import build_host
+
+    lib = ctypes.CDLL(build_host.build())
+    dp = ctypes.POINTER(ctypes.c_double)
+    lib.host_prism_gravity.argtypes = [
+        ctypes.c_int, ctypes.c_int64, dp, dp, dp, ctypes.c_int64, dp, dp, dp, ctypes.c_int
+    ]
+    lib.host_prism_gravity.restype = None
+
+    def run(points, prisms, density, field, mode):
+        e, n, u = (np.ascontiguousarray(points[:, c]) for c in range(3))
+        p = np.ascontiguousarray(np.atleast_2d(prisms), dtype=np.float64)
+        rho = np.ascontiguousarray(np.atleast_1d(density), dtype=np.float64).ravel()
+        out = np.zeros(e.size)
+        P = lambda a: a.ctypes.data_as(dp)  # noqa: E731
+        lib.host_prism_gravity(FIELDS.index(field), e.size, P(e), P(n), P(u), p.shape[0], P(p),
+                               P(rho), P(out), mode)
+        return out
+
+    return run
+
+
+def _bar(actual, exact, msg):
+    npt.assert_array_equal(np.isnan(actual), np.isnan(exact), err_msg=msg)
+    ok = np.isfinite(exact)
+    npt.assert_allclose(actual[ok], exact[ok], rtol=RTOL,
+                        atol=ATOL_FRAC * np.abs(exact[ok]).max(), err_msg=msg)
+
+
+def _singles(truth, evaluate):
+    sp, sd = truth["single_prisms"], truth["single_density"]
+    pts, which = truth["single_points"], truth["single_which"]
+    return np.array([evaluate(pts[i:i + 1], sp[which[i]], [sd[which[i]]])[0]
+                     for i in range(pts.shape[0])])
+
+
+@pytest.mark.parametrize("field", FIELDS)
+def test_oracle_against_exact_values(oracle, truth, field):
+    def evaluate(points, prisms, density):
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            return oracle.prism_gravity(tuple(points[:, c] for c in range(3)), prisms, density,
+                                        field)
+
+    near = truth["single_class"] <= 5.0
+    got = _singles(truth, evaluate)
+    exact = truth[f"single_{field}"]
+    assert np.max(np.abs(got[near] / exact[near] - 1)) <= RTOL
+    _bar(evaluate(truth["faces_points"], truth["faces_prism"], [float(truth["faces_density"])]),
+         truth[f"faces_{field}"], field)
+    _bar(evaluate(truth["layer_points"], truth["layer_prisms"], truth["layer_density"].ravel()),
+         truth[f"layer_{field}"], field)
+
+
+@pytest.mark.parametrize("mode", [0, 2], ids=["single-field", "fused"])
+@pytest.mark.parametrize("field", FIELDS)
+def test_kernel_formulation_against_exact_values(oracle, host, truth, field, mode):
+    got = _singles(truth, lambda pts, p, d: host(pts, p, d, field, mode))
+    exact = truth[f"single_{field}"]
+    klass = truth["single_class"]
+    near = klass <= 5.0
+    assert np.max(np.abs(got[near] / exact[near] - 1)) <= RTOL
+    ref = _singles(truth, lambda pts, p, d: oracle.prism_gravity(
+        tuple(pts[:, c] for c in range(3)), p, d, field))
+    for km in (50.0, 300.0):
+        sel = klass == km
+        ours = np.max(np.abs(got[sel] / exact[sel] - 1))
+        theirs = np.max(np.abs(ref[sel] / exact[sel] - 1))
+        assert ours <= max(theirs, RTOL) and ours <= 1e-4, (km, ours, theirs)
+    _bar(host(truth["faces_points"], truth["faces_prism"], [float(truth["faces_density"])],
+              field, mode), truth[f"faces_{field}"], field)
+    _bar(host(truth["layer_points"], truth["layer_prisms"], truth["layer_density"], field, mode),
+         truth[f"layer_{field}"], field)
