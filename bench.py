@@ -1,39 +1,50 @@
 """
-Benchmark: FP64 g_z prism-station pair evaluations per second on one GB300.
+Benchmark of the prism gravity forward model on one GB300: FP64 g_z
+prism-station pairs/s of the plain drop-in, with the served and batched
+forms of the same path beside it.
 
-Workload (N=1): the 1e6-prism topography layer (1000 x 1000 prisms on a
-200 m grid, 200 km square, Gaussian-sum tops, bottoms at -10 000 m, densities
-U(1800, 3100)) with its 500 x 500-station survey at 2000 m + N(0, 50 m)
-(harmonica_gb300.synthetic.layer_topography_1e6, seeded; synthetic data).
-The full survey is 2.5e11 pairs; a STEP is one batch of the survey
-(``--stations-per-step`` consecutive stations, default 5000) against all 1e6
-prisms, the batches walking through the survey step after step.  Per-pair
-cost is uniform, so pairs/s over batches equals pairs/s over the full survey.
+Workload of the headline (N=1): the 1e6-prism topography layer (1000 x 1000
+prisms on a 200 m grid, 200 km square, Gaussian-sum tops, bottoms at
+-10 000 m, densities U(1800, 3100)) with its 500 x 500-station survey at
+2000 m + N(0, 50 m) (harmonica_gb300.synthetic.layer_topography_1e6, seeded;
+synthetic data).  The full survey is 2.5e11 pairs; a STEP is one batch of
+the survey (``--stations-per-step`` consecutive stations, default 5000)
+against all 1e6 prisms, the batches walking through the survey step after
+step.  Per-pair cost is uniform, so pairs/s over batches equals pairs/s over
+the full survey.
 
-* ``value``: pairs/s with the layer and survey resident in HBM, timed with
-  CUDA events around each step's launches on the launching stream.
-* ``e2e``: pairs/s through the public drop-in call
+Keys of the JSON line:
+
+* ``value``: pairs/s of the layer forward with the layer and survey resident
+  in HBM, CUDA events around each step's launches on the launching stream,
+  L2 flushed between steps.
+* ``e2e``: the same through the public drop-in call
   ``layer.prism_layer.gravity(coords, "g_z")`` with host (numpy) buffers:
   host->device copies of the layer and the batch, the kernels and the
-  device->host copy of the result are inside the timed region.
-* ``roofline``: FP64-pipe bound.  ``achieved`` is the algorithmic FP64 flop
-  rate of the layer kernel, 720 flop per pair (8 vertices x (~16 basic +
-  sqrt + 2 log + 1 atan2) at basic=1, sqrt=4, log=20, atan2=30), over the
-  average kernel time; ``peak`` is the FP64 fused multiply-add rate measured
-  live by the hg_fp64_peak_probe launch (no FP64 figure exists in the
-  measured peak file).  The kernel evaluates the pair on float pairs
-  and executes ~9 FP64 instructions per pair instead of the convention's
-  720 flop, so ``frac`` far exceeds 1: it rates the algorithm, not the
-  hardware.  ``fp64_pipe_frac`` is the FP64 pipe's hardware use (ncu FP64
-  instructions per pair, recorded in profiles/forward_kernel_gz_layer1e6.md,
-  x pairs/s over the measured FP64 instruction peak); ``hw`` is the binding
-  resource, warp-instruction issue (ncu instructions per pair x pairs/s over
-  4 per clock per SM at the sampled clock).  ``traffic`` is the DRAM bytes of
-  one step's launch from the same profile (the 24 MB layer read once; it
-  stays in L2).
-* ``cpu_baseline``: the CPU oracle (a C/OpenMP restatement of the reference's
-  per-vertex loop) on all host cores, on a bounded sample of stations of the
-  same workload.
+  device->host copy of the result inside the timed region.
+* ``roofline``: the binding hardware resource of the layer kernel.  The pair
+  is evaluated on FP32 float pairs, so the kernel is bound by instruction
+  issue (one warp instruction per clock per SM sub-partition): ``achieved``
+  = warp instructions per pair x the kernel's pairs/s, ``peak`` = 4 x SMs x
+  the SM clock sampled during the timed steps.  The instruction, FP64 and
+  DRAM counts per pair come from one ncu capture of the same kernel and are
+  used only while the kernel sources hash to the value recorded with them
+  (otherwise ``stale`` and no fraction).  ``algorithmic`` holds the survey's
+  flop convention for the closed form (720 flop per g_z pair: 8 vertices x
+  (~16 basic + sqrt + 2 log + 1 atan2) at basic=1, sqrt=4, log=20,
+  atan2=30) against the FP64 FMA rate measured live.
+* ``all_fields`` / ``potential``: the fused all-field kernel and the
+  potential kernel on the same layer (sampled stations).
+* ``batched``: the batched workload (256 uneven g_z/g_zz problems) in one
+  persistent graph-captured launch per field, against the plain drop-in
+  ``prism_gravity`` called once per problem from host buffers.
+* ``served``: a Poisson stream of forward solves through the
+  continuous-batching server with load shedding, p50/p99 latency over the
+  accepted requests, the refused share, and the plain drop-in on the same
+  requests one by one from host buffers.
+* ``cpu_baseline``: the CPU oracle (a C/OpenMP restatement of the
+  reference's per-vertex loop) on all host cores, on a bounded sample of
+  stations of the same workload.
 
 ``--impl reference`` times the reference's CPU path instead (the oracle port:
 the reference's numba + choclo stack is not installable offline) and prints
@@ -41,6 +52,8 @@ its own JSON line.
 """
 
 import argparse
+import ctypes
+import hashlib
 import json
 import os
 import subprocess
@@ -53,17 +66,30 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 
-ALGO_FLOP_PER_PAIR_GZ = 720.0
-# ncu counts for forward_kernel<g_z, LayerSource> (profiles/forward_kernel_gz_layer1e6.md):
-# FP64 thread-instructions per pair (sm__sass_thread_inst_executed_op_fp64_pred_on / pairs),
-# warp instructions issued per pair (smsp__inst_executed / pairs) and DRAM read+write bytes of
-# one default step's launch (5000 stations x 1e6 prisms).
-FP64_INST_PER_PAIR_GZ = 9.37
-WARP_INST_PER_PAIR_GZ = 65.9
-TRAFFIC_BYTES_GZ_STEP = 25041664 + 18485760
-ISSUE_PER_SM_PER_CLOCK = 4  # one warp instruction per clock per SM sub-partition, 4 per SM
-METRIC = "FP64 g_z prism-station pairs/s"
+METRIC = ("FP64 g_z prism·station pairs/s, served vs plain on 1 GB300 @≤1e-8 rel; "
+          "p50/p99 ms")
+ARITH = ("FP64 inputs, outputs and accumulation; each pair's closed form evaluated on float "
+         "pairs (two FP32 numbers, ~2^-44 relative) with FP64 fallbacks for degenerate "
+         "geometry; per-pair error against 50-digit values in tests/test_gpu_truth.py")
 WORKLOAD = "layer_topography_1e6: 1000x1000 prisms (200 m grid), 500x500 stations, g_z"
+ALGO_FLOP_PER_PAIR_GZ = 720.0
+ISSUE_PER_SM_PER_CLOCK = 4  # one warp instruction per clock per SM sub-partition
+
+# Kernel sources whose hash keys the ncu counts below.
+KERNEL_SOURCES = ("prism_math.cuh", "lean_math.cuh", "lean_packed.cuh", "lean_tables.inc",
+                  "forward_core.cuh", "prism_forward.cu")
+# ncu counts of the layer g_z kernel (forward_kernel<3, LayerSource>) per pair:
+# smsp__inst_executed.sum (warp instructions), sm__sass_thread_inst_executed_op_fp64_pred_on.sum
+# (FP64 thread instructions) and dram__bytes_read.sum + dram__bytes_write.sum per station of
+# a step (the step's kernels read the layer once and write and read the chunk partial sums),
+# from the capture summarised under profiles/, for the kernel sources of `sources_sha`.
+KERNEL_COUNTS = {
+    "sources_sha": None,
+    "warp_inst_per_pair": None,
+    "fp64_inst_per_pair": None,
+    "dram_bytes_per_step_station": None,
+    "capture": None,
+}
 
 
 def parse_args():
@@ -77,17 +103,20 @@ def parse_args():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-all-fields", action="store_true")
+    p.add_argument("--no-batched", action="store_true")
+    p.add_argument("--no-served", action="store_true")
     p.add_argument("--all-fields-stations", type=int, default=1000)
-    p.add_argument("--workload", default="layer", choices=["layer", "batched", "inversion", "serving", "points", "magnetic",
+    p.add_argument("--workload", default="layer",
+                   choices=["layer", "batched", "inversion", "serving", "points", "magnetic",
                             "tesseroids"],
-                   help="layer: the 1e6-prism layer (default); batched: 256 uneven "
-                        "g_z/g_zz problems, one persistent graph-captured launch vs one "
-                        "launch per problem")
+                   help="layer: the 1e6-prism layer with the batched and served blocks "
+                        "(default); the others run one secondary workload alone")
     p.add_argument("--batch-problems", type=int, default=256)
     p.add_argument("--autotune", action="store_true")
-    p.add_argument("--arrival-seconds", type=float, default=5.0)
-    p.add_argument("--drain-seconds", type=float, default=30.0)
+    p.add_argument("--arrival-seconds", type=float, default=4.0)
     p.add_argument("--rate", type=float, default=200.0)
+    p.add_argument("--max-backlog-s", type=float, default=2.0)
+    p.add_argument("--plain-sample-seconds", type=float, default=8.0)
     return p.parse_args()
 
 
@@ -96,6 +125,15 @@ def dist_env():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return rank, world, local
+
+
+def kernel_sources_sha():
+    csrc = os.path.join(HERE, "harmonica_gb300", "csrc")
+    h = hashlib.sha256()
+    for name in KERNEL_SOURCES:
+        with open(os.path.join(csrc, name), "rb") as f:
+            h.update(name.encode() + b"\0" + f.read())
+    return h.hexdigest()[:16]
 
 
 class ClockSampler:
@@ -158,8 +196,22 @@ class ClockSampler:
         }
 
 
-def fp64_peak(torch, lib):
+def bench_lib():
+    """The benchmark-support library (include/harmonica_gb300_bench.h)."""
+    from harmonica_gb300 import _native
+
+    _native.build()
+    _native.lib()  # the bench library resolves the product library's symbols
+    lib = ctypes.CDLL(_native.BENCH_LIB_PATH)
+    lib.hg_fp64_peak_probe.restype = ctypes.c_int
+    lib.hg_fp64_peak_probe.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int,
+                                       ctypes.c_void_p]
+    return lib
+
+
+def fp64_peak(torch):
     """Measured FP64 FMA peak (TFLOP/s) of this GPU via hg_fp64_peak_probe."""
+    lib = bench_lib()
     n_threads = 152 * 8 * 256
     iters = 4000
     out = torch.empty(n_threads, dtype=torch.float64, device="cuda")
@@ -207,12 +259,11 @@ def run_reference(args, rank, world):
     n = max(1, args.cpu_sample_stations)
     for _ in range(max(0, min(args.warmup, 1))):
         cpu_baseline(layer, coords, max(1, n // 8), threads)
-    rates, times = [], []
+    times = []
     for _ in range(args.steps):
-        rate, dt, pairs = cpu_baseline(layer, coords, n, threads)
-        rates.append(rate)
+        _, dt, _ = cpu_baseline(layer, coords, n, threads)
         times.append(dt)
-    value = float(np.sum([n * layer["top"].size for _ in times]) / np.sum(times))
+    value = float(n * layer["top"].size * len(times) / np.sum(times))
     line = {
         "impl": "reference",
         "metric": METRIC,
@@ -226,6 +277,7 @@ def run_reference(args, rank, world):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64",
+        "arith": "FP64 throughout (per-vertex closed form, the reference's algorithm)",
         "data": "synthetic",
         "config": {
             "workload": WORKLOAD,
@@ -246,21 +298,22 @@ def run_reference(args, rank, world):
     print(json.dumps(line))
 
 
-def run_batched(args, rank, world, local):
-    """Batched workload: one persistent graph-captured launch vs one launch per problem."""
-    import torch
+# --------------------------------------------------------------------------
+# batched block
 
-    from harmonica_gb300 import _native, synthetic
+def batched_block(args, torch, local, timed_replays=2):
+    """The batched workload in one persistent graph-captured launch per field
+    against (a) the plain drop-in prism_gravity once per problem from host
+    buffers, (b) one hg_prism_forward launch per problem on resident inputs."""
+    import harmonica_gb300 as hg
+    from harmonica_gb300 import synthetic
     from harmonica_gb300.batch import PrismBatch, autotune
     from harmonica_gb300.fields import FIELD_CODES
     from harmonica_gb300.gravity import forward_on_device
 
-    _native.build()
-    torch.cuda.set_device(local)
     problems = synthetic.batched_problems(args.batch_problems, seed=4)
-    if world > 1:
-        problems = problems[rank::world]
-    chunk, ctas, tuned = 0, 0, None
+    tuned = None
+    chunk = ctas = 0
     if args.autotune:
         tuned = autotune(problems, repeats=1)
         chunk, ctas = tuned["chunk_prisms"], tuned["n_ctas"]
@@ -268,25 +321,22 @@ def run_batched(args, rank, world, local):
     info = batch.info()
     pairs = info["pairs"]
     batch.capture()
-    for _ in range(max(1, args.warmup)):
-        batch.replay()
+    batch.replay()
     torch.cuda.synchronize()
-    sampler = ClockSampler(local)
-    sampler.start()
     t0 = torch.cuda.Event(enable_timing=True)
     t1 = torch.cuda.Event(enable_timing=True)
     t0.record()
-    for _ in range(args.steps):
+    for _ in range(timed_replays):
         batch.replay()
     t1.record()
     torch.cuda.synchronize()
-    clocks = sampler.stop()
-    batched_s = t0.elapsed_time(t1) * 1e-3 / args.steps
-    batched_results = [o.clone() for o in batch.outputs]
+    batched_s = t0.elapsed_time(t1) * 1e-3 / timed_replays
+    batched = [o.clone() for o in batch.outputs]
 
-    # plain: the single-launch drop-in once per problem, same resident inputs
+    # (b) one launch per problem on the batch's resident inputs
     keep = batch._keep
-    def plain_pass():
+
+    def device_pass():
         outs = []
         for k, p in enumerate(problems):
             e, n, u, soa = keep[4 * k: 4 * k + 4]
@@ -294,49 +344,168 @@ def run_batched(args, rank, world, local):
             out, _ = forward_on_device(e, n, u, soa, m, 1 << FIELD_CODES[p["field"]], False)
             outs.append(out)
         return outs
-    plain_pass()
+
+    device_pass()
     torch.cuda.synchronize()
-    p0 = torch.cuda.Event(enable_timing=True)
-    p1 = torch.cuda.Event(enable_timing=True)
-    p0.record()
-    outs = plain_pass()
-    p1.record()
+    d0 = time.perf_counter()
+    outs = device_pass()
     torch.cuda.synchronize()
-    plain_s = p0.elapsed_time(p1) * 1e-3
+    device_s = time.perf_counter() - d0
     worst = 0.0
-    for a, b in zip(batched_results, outs):
+    for a, b in zip(batched, outs):
         ref = b[0]
         if ref.numel():
-            d = (a - ref).abs().max().item() / max(ref.abs().max().item(), 1e-300)
-            worst = max(worst, d)
-    if rank != 0:
-        return
-    line = {
-        "metric": "FP64 g_z/g_zz prism-station pairs/s, batched persistent launch",
-        "value": pairs * world / batched_s,
-        "unit": "pairs/s",
-        "n_gpus": world,
-        "steps": args.steps,
-        "warmup": args.warmup,
-        "ms_per_step": batched_s * 1e3,
-        "higher_is_better": True,
-        "scaling": "weak",
-        "vs_baseline": None,
-        "dtype": "f64",
-        "data": "synthetic",
-        "config": {"workload": f"batched: {len(problems)} problems, prisms log-U[1e3,2e5], "
-                               f"stations log-U[1e3,5e4], fields g_z/g_zz alternating",
-                   "pairs_per_step": pairs, "work_items": info["items"],
-                   "persistent_ctas": info["ctas"], "tuned": tuned},
-        "plain": {"value": pairs / plain_s, "unit": "pairs/s",
-                  "note": "one hg_prism_forward launch per problem on the same resident inputs"},
-        "batched_over_plain": plain_s / batched_s,
-        "max_rel_diff_batched_vs_plain": worst,
-        "gpu_launches": 2 * args.steps,
-        "clocks": clocks,
-    }
-    print(json.dumps(line))
+            worst = max(worst, (a - ref).abs().max().item() / max(ref.abs().max().item(), 1e-300))
     batch.close()
+
+    # (a) the drop-in from host buffers, problem after problem
+    hg.prism_gravity(problems[0]["coordinates"], problems[0]["prisms"], problems[0]["density"],
+                     field=problems[0]["field"])
+    torch.cuda.synchronize()
+    h0 = time.perf_counter()
+    for p in problems:
+        hg.prism_gravity(p["coordinates"], p["prisms"], p["density"], field=p["field"])
+    plain_s = time.perf_counter() - h0
+    return {
+        "workload": f"{len(problems)} independent problems, prisms log-U[1e3,2e5], stations "
+                    "log-U[1e3,5e4], fields g_z/g_zz alternating",
+        "pairs_per_pass": pairs,
+        "value": pairs / batched_s, "unit": "pairs/s",
+        "ms_per_pass": batched_s * 1e3,
+        "plain": {"value": pairs / plain_s, "unit": "pairs/s", "ms_per_pass": plain_s * 1e3,
+                  "path": "harmonica_gb300.prism_gravity once per problem, numpy inputs"},
+        "batched_over_plain": plain_s / batched_s,
+        "per_problem_launches": {"value": pairs / device_s, "unit": "pairs/s",
+                                 "path": "one hg_prism_forward launch per problem on the "
+                                         "resident inputs"},
+        "batched_over_per_problem_launches": device_s / batched_s,
+        "max_rel_diff_batched_vs_per_problem": worst,
+        "work_items": info["items"], "persistent_ctas": info["ctas"], "tuned": tuned,
+        "timed_replays": timed_replays,
+    }
+
+
+# --------------------------------------------------------------------------
+# served block
+
+def served_block(args, torch, local):
+    """A Poisson stream of forward solves through PrismServer (load shedding
+    on), and the plain drop-in on the same requests one by one."""
+    import harmonica_gb300 as hg
+    from harmonica_gb300 import synthetic
+    from harmonica_gb300.serve import PrismServer, ServerOverloaded
+
+    models = synthetic.serving_models()
+    stream = synthetic.serving_stream(rate=args.rate, seconds=args.arrival_seconds)
+    srv = PrismServer(memory_budget=120e9, max_active=4096, max_backlog_s=args.max_backlog_s)
+    for k in range(8):
+        srv.register_layer(f"layer{k}", models[k][0], models[k][1])
+    coords_of = [synthetic.serving_request_coordinates(r, models[r["model"]][2]) for r in stream]
+    # warm the kernels of the three fields outside the measured stream
+    warm = [srv.submit(coords_of[0], f, layer="layer0") for f in ("g_z", "potential", "g_zz")]
+    for f in warm:
+        f.result()
+    srv.rate = srv.nominal_rate  # start the stream from the nominal rate estimate
+    offered = sum(r["n_stations"] * models[r["model"]][0].shape[0] for r in stream)
+    futures = []
+    t0 = time.perf_counter()
+    for r, coords in zip(stream, coords_of):
+        delay = r["t"] - (time.perf_counter() - t0)
+        if delay > 0:
+            time.sleep(delay)
+        if r["resident"]:
+            f = srv.submit(coords, r["field"], layer=f"layer{r['model']}")
+        else:
+            f = srv.submit(coords, r["field"], prisms=models[r["model"]][0],
+                           density=models[r["model"]][1])
+        futures.append((f, r, time.perf_counter()))
+    accepted = [(f, r, ts) for f, r, ts in futures
+                if not (f.done() and isinstance(f.exception(), ServerOverloaded))]
+    done_pairs = 0.0
+    for f, r, ts in accepted:
+        f.result()  # accepted requests all finish (the backlog is bounded)
+        done_pairs += r["n_stations"] * models[r["model"]][0].shape[0]
+    st = srv.stats()
+    mine = {id(f) for f, _, _ in accepted}
+    finished = [req for req in srv.completed if id(req.future) in mine]
+    latencies = np.array([req.t_done - req.t_submit for req in finished])
+    elapsed = max(req.t_done for req in finished) - t0
+    srv.close(drain=True, timeout=60)
+    fields = {}
+    for f, r, ts in accepted:
+        fields[r["field"]] = fields.get(r["field"], 0) + 1
+
+    # the plain drop-in on the stream's requests one by one (a bounded sample)
+    plain_pairs, plain_s, n_plain = 0.0, 0.0, 0
+    for r, coords in zip(stream, coords_of):
+        prisms, density, _ = models[r["model"]]
+        torch.cuda.synchronize()
+        a = time.perf_counter()
+        hg.prism_gravity(coords, prisms, density, field=r["field"])
+        plain_s += time.perf_counter() - a
+        plain_pairs += r["n_stations"] * prisms.shape[0]
+        n_plain += 1
+        if plain_s >= args.plain_sample_seconds:
+            break
+    served_rate = done_pairs / elapsed
+    plain_rate = plain_pairs / plain_s
+    return {
+        "workload": f"Poisson {args.rate}/s for {args.arrival_seconds} s, prisms log-U[1e3,1e6], "
+                    "stations log-U[1e3,2.5e5], fields g_z/potential/g_zz, 30% on 8 resident "
+                    "layers, 120 GB budget",
+        "requests": len(stream),
+        "offered_pairs_per_s": offered / args.arrival_seconds,
+        "accepted": len(accepted), "refused": st["rejected"],
+        "refused_share": st["rejected"] / max(len(stream), 1),
+        "max_backlog_s": args.max_backlog_s,
+        "completed": len(latencies),
+        "value": served_rate, "unit": "pairs/s",
+        "p50_ms": float(np.percentile(latencies, 50) * 1e3) if latencies.size else None,
+        "p99_ms": float(np.percentile(latencies, 99) * 1e3) if latencies.size else None,
+        "latency_over": "every accepted request (all finished); refused requests are answered "
+                        "at once with ServerOverloaded",
+        "measured_seconds": elapsed, "rounds": st["rounds"],
+        "accepted_fields": fields,
+        "plain": {"value": plain_rate, "unit": "pairs/s", "requests": n_plain,
+                  "path": "harmonica_gb300.prism_gravity once per request, numpy inputs, "
+                          "the stream's first requests in order"},
+        "served_over_plain": served_rate / plain_rate,
+    }
+
+
+# --------------------------------------------------------------------------
+# secondary workloads (run alone with --workload)
+
+def run_batched(args, rank, world, local):
+    import torch
+
+    from harmonica_gb300 import _native
+
+    _native.build()
+    torch.cuda.set_device(local)
+    blk = batched_block(args, torch, local, timed_replays=max(1, args.steps))
+    if rank == 0:
+        print(json.dumps({"metric": "FP64 g_z/g_zz prism-station pairs/s, batched persistent "
+                                    "launch", "value": blk["value"], "unit": "pairs/s",
+                          "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                          "higher_is_better": True, "dtype": "f64", "arith": ARITH,
+                          "data": "synthetic", "batched": blk,
+                          "gpu_launches": 3 * args.steps}))
+
+
+def run_serving(args, rank, world, local):
+    import torch
+
+    from harmonica_gb300 import _native
+
+    _native.build()
+    torch.cuda.set_device(local)
+    blk = served_block(args, torch, local)
+    if rank == 0:
+        print(json.dumps({"metric": "served FP64 pairs/s and latency, Poisson stream of "
+                                    "forward solves", "value": blk["value"], "unit": "pairs/s",
+                          "n_gpus": world, "steps": 1, "warmup": 0, "higher_is_better": True,
+                          "dtype": "f64", "arith": ARITH, "data": "synthetic", "served": blk}))
 
 
 def run_inversion(args, rank, world, local):
@@ -386,91 +555,12 @@ def run_inversion(args, rank, world, local):
         "metric": "basement inversion step (FP64 g_z forward + adjoint d/drho, d/dbottom)",
         "value": pairs / step_s, "unit": "forward pairs/s", "ms_per_step": step_s * 1e3,
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
-        "dtype": "f64", "data": "synthetic",
+        "dtype": "f64", "arith": ARITH, "data": "synthetic",
         "config": {"workload": "200x200 layer (500 m), tops 0, smooth bottoms N(-3000,800), "
                                "contrast -400, 100x100 stations at 500 m",
                    "pairs_per_forward": pairs, "loss": float(loss),
                    "grad_bottom_norm": float(gb.norm()), "grad_density_norm": float(gr.norm())},
         "gpu_launches": 4 * args.steps,
-    }))
-
-
-def run_serving(args, rank, world, local):
-    """Poisson stream of forward solves through the continuous-batching server."""
-    import torch
-
-    from harmonica_gb300 import _native
-    from harmonica_gb300.serve import PrismServer
-
-    _native.build()
-    torch.cuda.set_device(local)
-    rng = np.random.default_rng(7)
-
-    def model(m, seed):
-        r = np.random.default_rng(seed)
-        side = np.sqrt(m) * 200.0
-        west = r.uniform(0, side, m)
-        south = r.uniform(0, side, m)
-        top = r.uniform(-3000, 1000, m)
-        prisms = np.column_stack([west, west + 200.0, south, south + 200.0,
-                                  top - r.uniform(100, 5000, m), top])
-        return prisms, r.uniform(1800, 3100, m), side
-
-    # a pool of prism models (log-uniform 1e3..1e6 prisms); 30% of the
-    # requests use one of the first 8 as a resident layer
-    sizes = np.exp(rng.uniform(np.log(1e3), np.log(1e6), 24)).astype(int)
-    models = [model(int(m), 100 + k) for k, m in enumerate(sizes)]
-    srv = PrismServer(memory_budget=120e9, max_active=4096)
-    for k in range(8):
-        srv.register_layer(f"layer{k}", models[k][0], models[k][1])
-    fields = ("g_z", "potential", "g_zz")
-    # arrivals
-    t, arrivals = 0.0, []
-    while t < args.arrival_seconds:
-        t += rng.exponential(1.0 / args.rate)
-        n_st = int(np.exp(rng.uniform(np.log(1e3), np.log(2.5e5))))
-        resident = rng.uniform() < 0.3
-        k = int(rng.integers(0, 8)) if resident else int(rng.integers(8, len(models)))
-        arrivals.append((t, n_st, resident, k, fields[int(rng.integers(0, 3))],
-                         int(rng.integers(1 << 30))))
-    offered = sum(n * models[k][0].shape[0] for _, n, _, k, _, _ in arrivals)
-    futures = []
-    t0 = time.perf_counter()
-    for (ta, n_st, resident, k, field, seed) in arrivals:
-        delay = ta - (time.perf_counter() - t0)
-        if delay > 0:
-            time.sleep(delay)
-        side = models[k][2]
-        r = np.random.default_rng(seed)
-        coords = (r.uniform(0, side, n_st), r.uniform(0, side, n_st), r.uniform(100, 3000, n_st))
-        if resident:
-            f = srv.submit(coords, field, layer=f"layer{k}")
-        else:
-            f = srv.submit(coords, field, prisms=models[k][0], density=models[k][1])
-        futures.append((f, n_st * models[k][0].shape[0]))
-    deadline = t0 + args.arrival_seconds + args.drain_seconds
-    while time.perf_counter() < deadline and not all(f.done() for f, _ in futures):
-        time.sleep(0.05)
-    elapsed = time.perf_counter() - t0
-    st = srv.stats()
-    done_pairs = sum(p for f, p in futures if f.done() and f.exception() is None)
-    srv.close(drain=False, timeout=60)
-    if rank != 0:
-        return
-    print(json.dumps({
-        "metric": "served FP64 pairs/s and latency, Poisson stream of forward solves",
-        "value": done_pairs / elapsed, "unit": "pairs/s",
-        "n_gpus": world, "steps": 1, "warmup": 0, "higher_is_better": True, "dtype": "f64",
-        "data": "synthetic",
-        "config": {"workload": f"Poisson {args.rate}/s for {args.arrival_seconds} s, prisms "
-                               "log-U[1e3,1e6], stations log-U[1e3,2.5e5], fields "
-                               "g_z/potential/g_zz, 30% on 8 resident layers, 120 GB budget",
-                   "requests": len(arrivals), "offered_pairs": offered,
-                   "offered_pairs_per_s": offered / args.arrival_seconds,
-                   "measured_seconds": elapsed},
-        "served": {"completed": st["completed"], "pending": len(arrivals) - st["completed"],
-                   "p50_ms": st.get("p50_ms"), "p99_ms": st.get("p99_ms"),
-                   "mean_ms": st.get("mean_ms"), "rounds": st["rounds"]},
     }))
 
 
@@ -579,7 +669,7 @@ def run_magnetic(args, rank, world, local):
         print(json.dumps({"metric": "FP64 prism magnetic pairs/s (b_e, b_n, b_u per pair)",
                           "value": B * m / sec, "unit": "pairs/s", "ms_per_step": sec * 1e3,
                           "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-                          "dtype": "f64", "data": "synthetic",
+                          "dtype": "f64", "arith": ARITH, "data": "synthetic",
                           "config": {"workload": "1e6-prism layer, magnetization U(-1,1) A/m, "
                                                  "1000 stations per step"},
                           "gpu_launches": 2 * args.steps}))
@@ -587,8 +677,8 @@ def run_magnetic(args, rank, world, local):
 
 # Per-pair instruction counts of the tesseroid forward kernel on the Andes layer, from
 # ncu on one bench launch (smsp__inst_executed.sum and
-# sm__sass_thread_inst_executed_op_fp64_pred_on.sum over its 3825 x 93121 pairs;
-# profiles/tesseroid_forward_andes.md), and the DRAM bytes of that launch.
+# sm__sass_thread_inst_executed_op_fp64_pred_on.sum over its 3825 x 93121 pairs), and the
+# DRAM bytes of that launch; summarised under profiles/.
 WARP_INST_PER_TESS_PAIR = 20.4
 FP64_INST_PER_TESS_PAIR = 2.56
 TRAFFIC_BYTES_TESS_STEP = 46889728 + 35952384
@@ -603,7 +693,6 @@ def run_tesseroids(args, rank, world, local):
     from harmonica_gb300 import _native, synthetic, tesseroid
 
     _native.build()
-    lib = _native.lib()
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     L = synthetic.tesseroid_layer_andes()
@@ -625,7 +714,7 @@ def run_tesseroids(args, rank, world, local):
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
-    peak = fp64_peak(torch, lib)
+    peak = fp64_peak(torch)
     sampler = ClockSampler(local)
     sampler.start()
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
@@ -685,11 +774,9 @@ def run_tesseroids(args, rank, world, local):
     if rank != 0:
         return
     kernel_rate = n_obs * m / (dev_time / args.steps)
-    # the binding resource is instruction issue (the far path runs on packed FP32
-    # float pairs): warp instructions per pair x pairs/s against 4 per clock per SM
     n_sms = torch.cuda.get_device_properties(dev).multi_processor_count
     sm_hz = (clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 0.0) * 1e6
-    issue_peak = 4 * n_sms * sm_hz
+    issue_peak = ISSUE_PER_SM_PER_CLOCK * n_sms * sm_hz
     issue_rate = WARP_INST_PER_TESS_PAIR * kernel_rate
     roof = {"bound": "instruction issue", "achieved": issue_rate / 1e9,
             "peak": issue_peak / 1e9 if issue_peak else None, "unit": "G warp-instructions/s",
@@ -715,29 +802,63 @@ def run_tesseroids(args, rank, world, local):
     }))
 
 
+# --------------------------------------------------------------------------
+# the headline
+
+def layer_roofline(torch, dev, kernel_pairs_per_s, clocks, stations_per_step):
+    """Roofline of the layer g_z kernel on its binding resource (instruction
+    issue), with the algorithmic FP64 figure beside it."""
+    peak = fp64_peak(torch)
+    sha = kernel_sources_sha()
+    counts = KERNEL_COUNTS
+    fresh = counts["sources_sha"] == sha and counts["warp_inst_per_pair"] is not None
+    n_sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    sm_hz = (clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 0.0) * 1e6
+    issue_peak = ISSUE_PER_SM_PER_CLOCK * n_sms * sm_hz
+    algo = ALGO_FLOP_PER_PAIR_GZ * kernel_pairs_per_s / 1e12
+    roof = {
+        "bound": "instruction issue",
+        "unit": "G warp-instructions/s",
+        "peak": issue_peak / 1e9 if issue_peak else None,
+        "peak_source": "4 warp instructions per clock per SM x SMs x the SM clock sampled "
+                       "during the timed steps",
+        "kernel_sources_sha": sha,
+        "counts_from": counts["capture"] if fresh else None,
+        "stale": not fresh,
+        "achieved": None, "frac": None, "traffic": None,
+        "algorithmic": {
+            "flop_per_pair": ALGO_FLOP_PER_PAIR_GZ,
+            "achieved": algo, "unit": "TFLOP/s",
+            "fp64_peak": peak, "fp64_peak_source": "measured live: hg_fp64_peak_probe "
+                                                   "(FP64 FMA chains)",
+            "ratio_to_fp64_peak": algo / peak,
+            "note": "the convention's flops per pair over the FP64 peak: the kernel evaluates "
+                    "the pair on float pairs and runs far fewer FP64 instructions, so this "
+                    "ratio rates the algorithm, not the hardware",
+        },
+    }
+    if fresh:
+        issue_rate = counts["warp_inst_per_pair"] * kernel_pairs_per_s
+        roof.update(achieved=issue_rate / 1e9,
+                    frac=issue_rate / issue_peak if issue_peak else None,
+                    warp_inst_per_pair=counts["warp_inst_per_pair"],
+                    traffic=counts["dram_bytes_per_step_station"] * stations_per_step,
+                    fp64={"inst_per_pair": counts["fp64_inst_per_pair"],
+                          "pipe_frac": counts["fp64_inst_per_pair"] * kernel_pairs_per_s
+                          / (peak * 1e12 / 2.0)})
+    return roof
+
+
 def main():
     args = parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":
         run_reference(args, rank, world)
         return
-    if args.workload == "batched":
-        run_batched(args, rank, world, local)
-        return
-    if args.workload == "inversion":
-        run_inversion(args, rank, world, local)
-        return
-    if args.workload == "serving":
-        run_serving(args, rank, world, local)
-        return
-    if args.workload == "points":
-        run_points(args, rank, world, local)
-        return
-    if args.workload == "magnetic":
-        run_magnetic(args, rank, world, local)
-        return
-    if args.workload == "tesseroids":
-        run_tesseroids(args, rank, world, local)
+    secondary = {"batched": run_batched, "inversion": run_inversion, "serving": run_serving,
+                 "points": run_points, "magnetic": run_magnetic, "tesseroids": run_tesseroids}
+    if args.workload in secondary:
+        secondary[args.workload](args, rank, world, local)
         return
 
     import torch
@@ -786,15 +907,14 @@ def main():
 
     flush = torch.empty(256 * 1024 * 1024 // 8, dtype=torch.float64, device=dev)
 
-    def step_device(step):
+    def step_device(step, field_mask=mask):
         lo, hi = batch(step)
-        return layer_forward_device(de[lo:hi], dn[lo:hi], du[lo:hi], ce, cn, bt, tp, rho, mask,
-                                    0.0)
+        return layer_forward_device(de[lo:hi], dn[lo:hi], du[lo:hi], ce, cn, bt, tp, rho,
+                                    field_mask, 0.0)
 
     for s in range(args.warmup):
         step_device(s)
     torch.cuda.synchronize()
-    peak = fp64_peak(torch, lib)
 
     sampler = ClockSampler(local)
     sampler.start()
@@ -853,28 +973,31 @@ def main():
             e2e_pairs *= world
         h2d = 8 * (3 * B + layer["easting"].size + layer["northing"].size + 3 * n_prisms)
         e2e = {"value": e2e_pairs / e2e_time, "unit": "pairs/s", "h2d_bytes_per_step": h2d,
-               "d2h_bytes_per_step": 8 * B}
+               "d2h_bytes_per_step": 8 * B,
+               "path": "prism_layer(...).prism_layer.gravity(coords, 'g_z'), numpy inputs"}
 
-    # all ten fields fused on the same layer (one launch computes every field)
-    all_fields = None
-    if not args.no_all_fields:
+    def sampled_rate(field_mask, label):
+        """One launch of `field_mask` on sampled stations of the layer."""
         nb = min(args.all_fields_stations, n_total)
         lo = rank * nb % n_total
-        layer_forward_device(de[lo:lo + nb], dn[lo:lo + nb], du[lo:lo + nb], ce, cn, bt, tp, rho,
-                             0x3FF, 0.0)
+        sl = slice(lo, lo + nb)
+        layer_forward_device(de[sl], dn[sl], du[sl], ce, cn, bt, tp, rho, field_mask, 0.0)
         torch.cuda.synchronize()
         a0 = torch.cuda.Event(enable_timing=True)
         a1 = torch.cuda.Event(enable_timing=True)
         a0.record()
-        layer_forward_device(de[lo:lo + nb], dn[lo:lo + nb], du[lo:lo + nb], ce, cn, bt, tp, rho,
-                             0x3FF, 0.0)
+        layer_forward_device(de[sl], dn[sl], du[sl], ce, cn, bt, tp, rho, field_mask, 0.0)
         a1.record()
         torch.cuda.synchronize()
         sec = a0.elapsed_time(a1) * 1e-3
-        all_fields = {"value": nb * n_prisms / sec, "unit": "pairs/s (all 10 fields per pair)",
-                      "field_values_per_s": 10 * nb * n_prisms / sec,
-                      "sample": f"{nb} stations x all 1e6 prisms, one fused launch",
-                      "ms": sec * 1e3}
+        return {"value": nb * n_prisms / sec, "unit": f"pairs/s ({label})",
+                "sample": f"{nb} stations x all 1e6 prisms, one launch", "ms": sec * 1e3}
+
+    all_fields = potential = None
+    if not args.no_all_fields:
+        all_fields = sampled_rate(0x3FF, "all 10 fields per pair, one fused launch")
+        all_fields["field_values_per_s"] = 10 * all_fields["value"]
+        potential = sampled_rate(1 << 0, "potential")
 
     base = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -884,22 +1007,18 @@ def main():
                 "sample": f"{args.cpu_sample_stations} strided stations x all 1e6 prisms "
                           f"({sample_pairs:.3g} pairs, {dt:.1f} s)"}
 
+    batched = served = None
+    if rank == 0 and not args.no_batched:
+        batched = batched_block(args, torch, local)
+    if rank == 0 and not args.no_served:
+        served = served_block(args, torch, local)
+
     if rank != 0:
         if world > 1:
             torch.distributed.destroy_process_group()
         return
     avg_launch_s = dev_time / args.steps
     kernel_pairs_per_s = (pairs / world / args.steps) / avg_launch_s
-    achieved = ALGO_FLOP_PER_PAIR_GZ * kernel_pairs_per_s / 1e12
-    # the probe's peak is in flops (2 per FMA); the FP64 pipe issues 1 instruction per FMA
-    fp64_pipe_frac = FP64_INST_PER_PAIR_GZ * kernel_pairs_per_s / (peak * 1e12 / 2.0)
-    default_step = args.stations_per_step == 5000
-    # the binding hardware resource: warp-instruction issue, against 4 per clock per SM at
-    # the SM clock sampled during the timed steps
-    n_sms = torch.cuda.get_device_properties(dev).multi_processor_count
-    sm_hz = (clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 0.0) * 1e6
-    issue_peak = ISSUE_PER_SM_PER_CLOCK * n_sms * sm_hz
-    issue_rate = WARP_INST_PER_PAIR_GZ * kernel_pairs_per_s
     line = {
         "metric": METRIC,
         "value": value,
@@ -912,6 +1031,7 @@ def main():
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64",
+        "arith": ARITH,
         "data": "synthetic",
         "config": {
             "workload": WORKLOAD,
@@ -920,30 +1040,13 @@ def main():
             "l2": "flushed between timed steps (256 MB write)",
             "parallelism": f"stations sharded over {world} GPU(s), no collective",
         },
-        "roofline": {
-            "bound": "fp64",
-            "achieved": achieved,
-            "peak": peak,
-            "unit": "TFLOP/s",
-            "frac": achieved / peak,
-            "traffic": TRAFFIC_BYTES_GZ_STEP if default_step else None,
-            "flop_per_pair": ALGO_FLOP_PER_PAIR_GZ,
-            "fp64_inst_per_pair": FP64_INST_PER_PAIR_GZ,
-            "fp64_pipe_frac": fp64_pipe_frac,
-            "hw": {
-                "bound": "instruction issue",
-                "achieved": issue_rate / 1e9,
-                "peak": issue_peak / 1e9 if issue_peak else None,
-                "unit": "G warp-instructions/s",
-                "frac": issue_rate / issue_peak if issue_peak else None,
-                "warp_inst_per_pair": WARP_INST_PER_PAIR_GZ,
-                "peak_source": "4 warp instructions per clock per SM x SMs x sampled SM clock",
-            },
-            "peak_source": "measured live: hg_fp64_peak_probe (FP64 FMA chains)",
-        },
+        "roofline": layer_roofline(torch, dev, kernel_pairs_per_s, clocks, B),
         "cpu_baseline": base,
-        "all_fields": all_fields,
         "e2e": e2e,
+        "served": served,
+        "batched": batched,
+        "all_fields": all_fields,
+        "potential": potential,
         "gpu_launches": launches_per_step * args.steps,
         "clocks": clocks,
         "step_ms": step_ms,

@@ -29,8 +29,12 @@ HEADERS = (
 #: translation units compiled into the library
 SOURCES = (
     "prism_forward.cu", "prism_batch.cu", "prism_adjoint.cu", "point_forward.cu",
-    "prism_magnetic.cu", "tesseroid_forward.cu", "bench_probe.cu",
+    "prism_magnetic.cu", "tesseroid_forward.cu",
 )
+#: the benchmark-support library (include/harmonica_gb300_bench.h), kept out
+#: of the product library; it links against the product library
+BENCH_SOURCES = ("bench_probe.cu",)
+BENCH_LIB_PATH = os.path.join(BUILD_DIR, "libhg_bench.so")
 
 ARCH_FLAGS = ("-gencode", "arch=compute_103a,code=sm_103a")
 
@@ -48,12 +52,12 @@ def nvcc_path():
     raise RuntimeError("nvcc not found: cannot build the harmonica_gb300 CUDA library")
 
 
-def _sources():
-    return [os.path.join(CSRC_DIR, s) for s in SOURCES]
+def _sources(names=SOURCES):
+    return [os.path.join(CSRC_DIR, s) for s in names]
 
 
 def _deps():
-    deps = _sources() + list(HEADERS)
+    deps = _sources(SOURCES + BENCH_SOURCES) + list(HEADERS)
     deps += [
         os.path.join(CSRC_DIR, f) for f in os.listdir(CSRC_DIR) if f.endswith((".cuh", ".h"))
     ]
@@ -61,9 +65,9 @@ def _deps():
 
 
 def is_stale():
-    if not os.path.exists(LIB_PATH):
+    if not (os.path.exists(LIB_PATH) and os.path.exists(BENCH_LIB_PATH)):
         return True
-    t = os.path.getmtime(LIB_PATH)
+    t = min(os.path.getmtime(LIB_PATH), os.path.getmtime(BENCH_LIB_PATH))
     return any(os.path.getmtime(d) > t for d in _deps())
 
 
@@ -106,7 +110,7 @@ def _compile_and_link(verbose):
     ]
     procs = []
     objs = []
-    for src in _sources():
+    for src in _sources(SOURCES + BENCH_SOURCES):
         obj = os.path.join(BUILD_DIR, os.path.basename(src) + ".o")
         objs.append(obj)
         cmd = common + ["-c", src, "-o", obj]
@@ -121,12 +125,21 @@ def _compile_and_link(verbose):
             )
         if verbose and out:
             print(out.decode(errors="replace"))
-    tmp = f"{LIB_PATH}.{os.getpid()}.tmp"
-    link = [nvcc, *ARCH_FLAGS, "-shared", "-o", tmp, *objs]
+    n_product = len(SOURCES)
+    _link(nvcc, objs[:n_product], LIB_PATH, [])
+    # the bench library resolves the product library's symbols (errors) at
+    # load time, found next to it
+    _link(nvcc, objs[n_product:], BENCH_LIB_PATH,
+          ["-L", BUILD_DIR, "-lharmonica_gb300", "-Xlinker", "-rpath=$ORIGIN"])
+
+
+def _link(nvcc, objs, path, extra):
+    tmp = f"{path}.{os.getpid()}.tmp"
+    link = [nvcc, *ARCH_FLAGS, "-shared", "-o", tmp, *objs, *extra]
     res = subprocess.run(link, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
     if res.returncode != 0:
         raise RuntimeError("nvcc link failed:\n" + res.stdout.decode(errors="replace"))
-    os.replace(tmp, LIB_PATH)  # atomic: a loader sees the old or the new library
+    os.replace(tmp, path)  # atomic: a loader sees the old or the new library
 
 
 _c_double_p = ctypes.c_void_p  # device pointers travel as integers
@@ -299,9 +312,6 @@ PROTOTYPES = {
         ctypes.c_int,
         [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
          ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p],
-    ),
-    "hg_fp64_peak_probe": (
-        ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_void_p]
     ),
     "hg_prism_forward_noalloc": (
         ctypes.c_int,

@@ -10,6 +10,8 @@ ETOPO-based layers of harmonica's gallery, doc/gallery_src/forward/).
 * ``layer_topography_1e6`` : 1000 x 1000 prisms on a 200 m grid (200 km
   square), bottoms at -10 000 m, Gaussian-sum tops (seed 2), densities
   U(1800, 3100) (seed 2); 500 x 500 stations at 2000 m + N(0, 50 m) (seed 3).
+* ``batched_problems`` : 256 uneven independent problems (g_z / g_zz).
+* ``serving_stream`` : a Poisson stream of forward-solve requests.
 """
 
 import numpy as np
@@ -186,3 +188,58 @@ def tesseroid_layer_andes(spacing=0.1, station_spacing=0.5, height=10e3, seed=9)
     plon, plat = np.meshgrid(slon, slat)
     coords = (plon.ravel(), plat.ravel(), geocentric_radius(plat).ravel() + height)
     return dict(tesseroids=tess, density=density.ravel(), coordinates=coords, shape=glon.shape)
+
+
+def serving_models(n_models=24, seed=7):
+    """Prism models of the serving workload: ``n_models`` random layers of
+    200 m x 200 m prisms with log-uniform 1e3-1e6 prisms each (tops
+    U(-3000, 1000) m, thicknesses U(100, 5000) m, densities U(1800, 3100)),
+    spread over a square of side sqrt(M) x 200 m.  Returns a list of
+    (prisms (M, 6), density (M,), side)."""
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(np.log(1e3), np.log(1e6), n_models)).astype(int)
+    models = []
+    for k, m in enumerate(sizes):
+        r = np.random.default_rng(100 + k)
+        side = np.sqrt(m) * 200.0
+        west = r.uniform(0, side, m)
+        south = r.uniform(0, side, m)
+        top = r.uniform(-3000, 1000, m)
+        prisms = np.column_stack([west, west + 200.0, south, south + 200.0,
+                                  top - r.uniform(100, 5000, m), top])
+        models.append((prisms, r.uniform(1800, 3100, m), side))
+    return models
+
+
+def serving_stream(rate=200.0, seconds=5.0, n_models=24, n_resident=8, resident_share=0.3,
+                   seed=7):
+    """
+    The serving workload: Poisson arrivals at ``rate`` requests/s for
+    ``seconds``; each request is a survey of log-uniform 1e3-2.5e5 stations
+    scattered over one model of :func:`serving_models` at heights
+    U(100, 3000) m, with a field drawn from (g_z, potential, g_zz);
+    ``resident_share`` of the requests use one of the first ``n_resident``
+    models as a resident layer, the others send their prisms.  Returns a list
+    of dicts (t, n_stations, resident, model, field, seed); the stations are
+    drawn from ``seed`` by :func:`serving_request_coordinates`.
+    """
+    rng = np.random.default_rng(seed)
+    fields = ("g_z", "potential", "g_zz")
+    t, out = 0.0, []
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t >= seconds:
+            return out
+        n_st = int(np.exp(rng.uniform(np.log(1e3), np.log(2.5e5))))
+        resident = bool(rng.uniform() < resident_share)
+        k = int(rng.integers(0, n_resident)) if resident else int(rng.integers(n_resident,
+                                                                               n_models))
+        out.append(dict(t=t, n_stations=n_st, resident=resident, model=k,
+                        field=fields[int(rng.integers(0, 3))], seed=int(rng.integers(1 << 30))))
+
+
+def serving_request_coordinates(request, side):
+    """Stations of one request of :func:`serving_stream` over a model of side ``side``."""
+    r = np.random.default_rng(request["seed"])
+    n = request["n_stations"]
+    return (r.uniform(0, side, n), r.uniform(0, side, n), r.uniform(100, 3000, n))

@@ -16,7 +16,7 @@ so empty modules stand in for them (with an empty class for verde's
 the modules are loaded from their files.
 
 Run from the repository root:
-    python tests/golden/make_eqs_golden.py [REFERENCE_ROOT]
+    python tests/golden/make_eqs_golden.py REFERENCE_ROOT
 """
 
 import importlib
@@ -82,7 +82,9 @@ def cases():
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit(f"usage: python {sys.argv[0]} REFERENCE_ROOT (the harmonica source tree)")
+    root = sys.argv[1]
     utils, green_cart, green_sph = load_reference(root)
     cart_data, cart_src, sph_data, sph_src, coefs = cases()
     out = {"cart_data": cart_data, "cart_src": cart_src, "sph_data": sph_data,

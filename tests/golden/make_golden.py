@@ -17,7 +17,7 @@ Generate the golden fixtures in this directory.
    (test/test_prism.py:161-190) for all ten fields, and for a small seeded
    prism layer, kept as regression vectors for the oracle and the GPU path.
 
-Run from the repository root:  python tests/golden/make_golden.py [REFERENCE_ROOT]
+Run from the repository root:  python tests/golden/make_golden.py REFERENCE_ROOT
 """
 
 import json
@@ -105,7 +105,9 @@ def point_sample(ref_root):
 
 
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit(f"usage: python {sys.argv[0]} REFERENCE_ROOT (the harmonica source tree)")
+    ref_root = sys.argv[1]
     if os.path.isdir(ref_root):
         with open(os.path.join(HERE, "reference_doctests.json"), "w") as f:
             json.dump(parse_doctests(ref_root), f, indent=1)

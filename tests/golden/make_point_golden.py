@@ -15,7 +15,7 @@ package ``__init__`` files are not executed; the module is loaded from its
 file.
 
 Run from the repository root:
-    python tests/golden/make_point_golden.py [REFERENCE_ROOT]
+    python tests/golden/make_point_golden.py REFERENCE_ROOT
 """
 
 import importlib
@@ -82,7 +82,9 @@ def cases():
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit(f"usage: python {sys.argv[0]} REFERENCE_ROOT (the harmonica source tree)")
+    root = sys.argv[1]
     point = load_reference(root)
     obs, masses, values = cases()
     out = {"coordinates": obs, "points": masses, "masses": values}

@@ -16,7 +16,7 @@ packages that are absent); the ``harmonica._forward`` modules are loaded
 from their files.
 
 Run from the repository root:
-    python tests/golden/make_tesseroid_golden.py [REFERENCE_ROOT]
+    python tests/golden/make_tesseroid_golden.py REFERENCE_ROOT
 """
 
 import os
@@ -233,4 +233,6 @@ def main(root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit(f"usage: python {sys.argv[0]} REFERENCE_ROOT (the harmonica source tree)")
+    main(sys.argv[1])

@@ -11,9 +11,9 @@ import re
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def declared_functions():
+def declared_functions(header_name="harmonica_gb300.h"):
     names = set()
-    for header in glob.glob(os.path.join(ROOT, "include", "*.h")):
+    for header in glob.glob(os.path.join(ROOT, "include", header_name)):
         text = open(header).read()
         text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
         names.update(re.findall(r"\b(hg_\w+)\s*\(", text))
@@ -31,6 +31,21 @@ def test_library_exports_declared_symbols():
     assert not missing, f"symbols declared but not exported: {missing}"
     # every declared symbol has a ctypes prototype in the Python binding
     assert set(names) <= set(_native.PROTOTYPES), set(names) - set(_native.PROTOTYPES)
+
+
+def test_bench_library_is_separate_and_exports_its_header():
+    """The benchmark probes (include/harmonica_gb300_bench.h) live in their
+    own library, not in the product library."""
+    from harmonica_gb300 import _native
+
+    _native.build()
+    product = ctypes.CDLL(_native.LIB_PATH)
+    bench = ctypes.CDLL(_native.BENCH_LIB_PATH)
+    names = declared_functions("harmonica_gb300_bench.h")
+    assert names
+    for n in names:
+        assert hasattr(bench, n), n
+        assert not hasattr(product, n), n
 
 
 def test_version_and_error_without_gpu():
