@@ -401,10 +401,14 @@ def served_block(args, torch, local):
     for k in range(8):
         srv.register_layer(f"layer{k}", models[k][0], models[k][1])
     coords_of = [synthetic.serving_request_coordinates(r, models[r["model"]][2]) for r in stream]
-    # warm the kernels of the three fields outside the measured stream
-    warm = [srv.submit(coords_of[0], f, layer="layer0") for f in ("g_z", "potential", "g_zz")]
+    # warm the kernels of the three fields outside the measured stream (small
+    # requests, no shedding)
+    srv.max_backlog_s = None
+    small = tuple(c[:1000] for c in coords_of[0])
+    warm = [srv.submit(small, f, layer="layer0") for f in ("g_z", "potential", "g_zz")]
     for f in warm:
         f.result()
+    srv.max_backlog_s = args.max_backlog_s
     srv.rate = srv.nominal_rate  # start the stream from the nominal rate estimate
     offered = sum(r["n_stations"] * models[r["model"]][0].shape[0] for r in stream)
     futures = []

@@ -1185,6 +1185,209 @@ HG_HD __forceinline__ bool pair_diag_p2(const Rel& q, const Tables& T, double& o
   return true;
 }
 
+// ---------------------------------------------------------------------------
+// All ten fields, or the potential alone, on float pairs.
+//
+// The edge logs of one family (the 4 edges parallel to A, at the bounds p of
+// P and q of Q, P < Q in (x, y, z) order: A = x: (y, z); A = y: (x, z);
+// A = z: (x, y)) enter every field only through
+//   MQ_p = L_p1 - L_p0   (merged along Q at P = p, merged_t),
+//   MP_0 = L_10 - L_00   (merged along P at the lower Q bound),
+//   L_00                 (one edge log, single_t),
+//   D    = MQ_1 - MQ_0   (= L_11 - L_10 - L_01 + L_00, the off-diagonal
+//                         tensor combination of the family),
+// since L_10 = L_00 + MP_0, L_01 = L_00 + MQ_0 and L_11 = L_10 + MQ_1:
+//   sum_pq s_p s_q P_p Q_q L_pq = dP dQ L_00 + P_1 dQ MP_0 + Q_1 dP MQ_0 + P_1 Q_1 D
+//   sum_pq s_p s_q Q_q L_pq     = Q_1 D + dQ MP_0
+//   sum_pq s_p s_q P_p L_pq     = P_1 D + dP MQ_0
+// (s_0 = -1, s_1 = +1; dP = P_1 - P_0).  Each right-hand term is of the
+// order of the result, while the left-hand sums of four logs cancel to the
+// second order of the distance (what limits the FP64 geometry far from the
+// prism).  Likewise for the faces normal to an axis u:
+//   u_0 O_0 - u_1 O_1     = u_0 (O_0 - O_1) - du O_1
+//   u_0^2 O_0 - u_1^2 O_1 = u_0^2 (O_0 - O_1) - du (u_0 + u_1) O_1.
+// With these, the combinations of pair_all become
+//   potential = sum_fam E_fam + 1/2 sum_axis (u_0^2 O_0 - u_1^2 O_1),
+//   g_e = QT_z + QT_y + F_x, g_n = QT_x + PT_z + F_y, g_z = PT_y + PT_x + F_z,
+//   g_ee, g_nn, g_zz = O_0 - O_1 of the x, y, z faces,
+//   g_en, g_ez, g_nz = D of the z, y, x families,
+// with E the first sum above, QT and PT the second and third, F the first
+// face identity (u the axis' coordinate).
+
+// t = R - 1 of one edge log ln R, R = (hi + r_hi) / (lo + r_lo) for an edge
+// beyond the point (lo >= 0 after reflection), or (hi + r_hi)(r_lo - lo) / rho2
+// when the point projects inside the edge (lo < 0; rho2 = squared distance
+// from the edge line), as sums of one-signed terms (r_hi - r_lo =
+// dA (hi + lo) / (r_hi + r_lo), r_hi r_lo - rho2 = (hi^2 m^2 + rho2 (hi^2 +
+// m^2)) / (r_hi r_lo + rho2) with m = -lo):
+//   lo >= 0: t = dA (r_hi + r_lo + hi + lo) / ((r_hi + r_lo)(lo + r_lo))
+//   lo < 0:  t = [hi r_lo + hi m + r_hi m + (hi^2 m^2 + rho2 (hi^2 + m^2))
+//                 / (r_hi r_lo + rho2)] / rho2
+// so t keeps its relative accuracy however far the edge is.
+HG_HD __forceinline__ lean::F2 single_t(bool straddle, lean::F2 lo, lean::F2 hi, lean::F2 rl,
+                                        lean::F2 rh, lean::F2 dA, lean::F2 rho2) {
+  using namespace lean;
+  if (!straddle) {
+    const F2 S = f2_add(rh, rl);
+    return f2_div(f2_mul(dA, f2_add(S, f2_add(hi, lo))), f2_mul(S, f2_add(lo, rl)));
+  }
+  const F2 m = f2_neg(lo);
+  const F2 h2 = f2_sq(hi), m2 = f2_sq(m);
+  const F2 x = f2_div(f2_add(f2_mul(h2, m2), f2_mul(rho2, f2_add(h2, m2))),
+                      f2_add(f2_mul(rh, rl), rho2));
+  const F2 num = f2_add(f2_add(f2_mul(hi, rl), f2_mul(hi, m)), f2_add(f2_mul(rh, m), x));
+  return f2_div(num, rho2);
+}
+
+// Float-pair bound k of axis a (a at run time, k a constant: selects only).
+HG_HD __forceinline__ lean::F2 bound_f2(const GeomF2& g, int a, int k) {
+  return a == 0 ? g.c[0][k] : (a == 1 ? g.c[1][k] : g.c[2][k]);
+}
+HG_HD __forceinline__ lean::F2 extent_f2(const GeomF2& g, int a) {
+  return a == 0 ? g.d[0] : (a == 1 ? g.d[1] : g.d[2]);
+}
+HG_HD __forceinline__ lean::F2 f2_sel(bool c, lean::F2 a, lean::F2 b) { return c ? a : b; }
+
+// The logs of edge family `fam` (= its axis A): MQ_0, MQ_1, MP_0, L_00.
+HG_HD __forceinline__ void family_logs(const Rel& q, const GeomF2& g, int fam, const Tables& T,
+                                       lean::F2& mq0, lean::F2& mq1, lean::F2& mp0,
+                                       lean::F2& l00) {
+  using namespace lean;
+  const int P = fam == 0 ? 1 : 0, Q = fam == 2 ? 1 : 2;
+  const AxisCase c = axis_case(rel_bound(q, fam, 0), rel_bound(q, fam, 1));
+  const F2 a0 = bound_f2(g, fam, 0), a1 = bound_f2(g, fam, 1);
+  const F2 lo = c.reflect ? f2_neg(a1) : a0, hi = c.reflect ? f2_neg(a0) : a1;
+  // vertex distance at A-end e, P bound p, Q bound q (family layout)
+  const auto R = [&](int e, int p, int qq) {
+    return fam == 0 ? g.r[e][p][qq] : (fam == 1 ? g.r[p][e][qq] : g.r[p][qq][e]);
+  };
+  const int el = c.reflect ? 1 : 0;  // A-end of lo
+  const auto RL = [&](int p, int qq) { return el ? R(1, p, qq) : R(0, p, qq); };
+  const auto RH = [&](int p, int qq) { return el ? R(0, p, qq) : R(1, p, qq); };
+  const F2 p0 = bound_f2(g, P, 0), p1 = bound_f2(g, P, 1);
+  const F2 q0 = bound_f2(g, Q, 0), q1 = bound_f2(g, Q, 1);
+  const F2 dA = extent_f2(g, fam), dP = extent_f2(g, P), dQ = extent_f2(g, Q);
+  const auto bc = [](F2 v) { return pk(v, v); };
+  // merged along Q, lanes P = 0, 1
+  const P2 tq = merged_t_p2(c.straddle, bc(lo), bc(hi), pk(p0, p1), bc(q1),
+                            pk(RL(0, 0), RL(1, 0)), pk(RL(0, 1), RL(1, 1)),
+                            pk(RH(0, 0), RH(1, 0)), pk(RH(0, 1), RH(1, 1)), bc(dA), bc(dQ),
+                            bc(f2_add(q0, q1)));
+  // merged along P, lane Q = 0; lane 1 carries the single log L_00 instead
+  const P2 tp = merged_t_p2(c.straddle, bc(lo), bc(hi), pk(q0, q1), bc(p1),
+                            pk(RL(0, 0), RL(0, 1)), pk(RL(1, 0), RL(1, 1)),
+                            pk(RH(0, 0), RH(0, 1)), pk(RH(1, 0), RH(1, 1)), bc(dA), bc(dP),
+                            bc(f2_add(p0, p1)));
+  const F2 tl = single_t(c.straddle, lo, hi, RL(0, 0), RH(0, 0), dA,
+                         f2_add(f2_sq(p0), f2_sq(q0)));
+  const P2 mq = log1p_p2(tq, T);
+  const P2 ml = log1p_p2(pk(lane0(tp), tl), T);
+  mq0 = lane0(mq);
+  mq1 = lane1(mq);
+  mp0 = lane0(ml);
+  l00 = lane1(ml);
+}
+
+// The two faces normal to `axis` as float pairs (lanes: lower, upper bound).
+HG_HD __forceinline__ bool face_pair_f2(const Rel& q, const GeomF2& g, int axis,
+                                        const Tables& T, lean::F2& o0, lean::F2& o1) {
+  using namespace lean;
+  const bool X = axis == 0, Y = axis == 1;
+  F2 fr[2][2][2];
+#pragma unroll
+  for (int k = 0; k < 2; k++)
+#pragma unroll
+    for (int bi = 0; bi < 2; bi++)
+#pragma unroll
+      for (int ci = 0; ci < 2; ci++)
+        fr[k][bi][ci] = X ? g.r[k][bi][ci] : (Y ? g.r[bi][k][ci] : g.r[bi][ci][k]);
+  const F2 fa[2] = {bound_f2(g, axis, 0), bound_f2(g, axis, 1)};
+  const F2 fb[2] = {X ? g.c[1][0] : g.c[0][0], X ? g.c[1][1] : g.c[0][1]};
+  const F2 fc[2] = {(X || Y) ? g.c[2][0] : g.c[1][0], (X || Y) ? g.c[2][1] : g.c[1][1]};
+  const F2 fw = X ? g.d[1] : g.d[0];
+  const double ad[2] = {rel_bound(q, axis, 0), rel_bound(q, axis, 1)};
+  const double bd[2] = {X ? q.y1 : q.x1, X ? q.y2 : q.x2};
+  const double cd[2] = {(X || Y) ? q.z1 : q.y1, (X || Y) ? q.z2 : q.y2};
+  P2 o;
+  if (!face_pair_p2(fa, fb, fc, fr, fw, ad, bd, cd, T, o)) return false;
+  o0 = lane0(o);
+  o1 = lane1(o);
+  return true;
+}
+
+// out[0..9] (ALL) or out[0] (the potential alone), the raw combinations of
+// pair_all.  false: a bound is zero or too small for the float-pair scale
+// (the point lies in a face plane or on an edge line, where the identities
+// above would add infinite logs with cancelling coefficients), or the
+// geometry leaves the float range; the caller takes the FP64 geometry.
+template <bool ALL>
+HG_HD __forceinline__ bool pair_all_f2(const Rel& q, const Tables& T, double* out) {
+  using namespace lean;
+  if (is_tiny(q.x1) || is_tiny(q.x2) || is_tiny(q.y1) || is_tiny(q.y2) || is_tiny(q.z1) ||
+      is_tiny(q.z2))
+    return false;
+  GeomF2 g;
+  if (!make_geom_f2(q, g)) return false;
+  const F2 zero{0.0f, 0.0f};
+  F2 pot = zero, ge = zero, gn = zero, gz = zero, Dx = zero, Dy = zero, Dz = zero;
+#pragma unroll 1
+  for (int fam = 0; fam < 3; fam++) {
+    F2 mq0, mq1, mp0, l00;
+    family_logs(q, g, fam, T, mq0, mq1, mp0, l00);
+    const int P = fam == 0 ? 1 : 0, Q = fam == 2 ? 1 : 2;
+    const F2 p1 = bound_f2(g, P, 1), q1 = bound_f2(g, Q, 1);
+    const F2 dP = extent_f2(g, P), dQ = extent_f2(g, Q);
+    const F2 D = f2_sub(mq1, mq0);
+    const F2 E = f2_add(f2_add(f2_mul(f2_mul(dP, dQ), l00), f2_mul(f2_mul(p1, dQ), mp0)),
+                        f2_add(f2_mul(f2_mul(q1, dP), mq0), f2_mul(f2_mul(p1, q1), D)));
+    pot = f2_add(pot, E);
+    if (ALL) {
+      const F2 PT = f2_add(f2_mul(p1, D), f2_mul(dP, mq0));
+      const F2 QT = f2_add(f2_mul(q1, D), f2_mul(dQ, mp0));
+      // g_e = QT_z + QT_y, g_n = QT_x + PT_z, g_z = PT_y + PT_x (edge parts)
+      ge = f2_add(ge, fam == 0 ? zero : QT);
+      gn = f2_add(gn, f2_sel(fam == 0, QT, f2_sel(fam == 2, PT, zero)));
+      gz = f2_add(gz, fam == 2 ? zero : PT);
+      Dx = f2_sel(fam == 0, D, Dx);
+      Dy = f2_sel(fam == 1, D, Dy);
+      Dz = f2_sel(fam == 2, D, Dz);
+    }
+  }
+  F2 faces2 = zero, diff[3] = {zero, zero, zero};
+#pragma unroll 1
+  for (int axis = 0; axis < 3; axis++) {
+    F2 o0, o1;
+    if (!face_pair_f2(q, g, axis, T, o0, o1)) return false;
+    const F2 u0 = bound_f2(g, axis, 0), du = extent_f2(g, axis);
+    const F2 dO = f2_sub(o0, o1);
+    faces2 = f2_add(faces2, f2_sub(f2_mul(f2_sq(u0), dO),
+                                   f2_mul(f2_mul(du, f2_add(u0, bound_f2(g, axis, 1))), o1)));
+    if (ALL) {
+      const F2 F = f2_sub(f2_mul(u0, dO), f2_mul(du, o1));
+      ge = f2_add(ge, axis == 0 ? F : zero);
+      gn = f2_add(gn, axis == 1 ? F : zero);
+      gz = f2_add(gz, axis == 2 ? F : zero);
+#pragma unroll
+      for (int a = 0; a < 3; a++) diff[a] = axis == a ? dO : diff[a];
+    }
+  }
+  pot = f2_add(pot, F2{fmul(0.5f, faces2.h), fmul(0.5f, faces2.l)});
+  const int e1 = g.top - 1023;
+  out[kPotential] = f2_to_double(pot, 2 * e1);
+  if (ALL) {
+    out[kGe] = f2_to_double(ge, e1);
+    out[kGn] = f2_to_double(gn, e1);
+    out[kGz] = f2_to_double(gz, e1);
+    out[kGee] = f2_to_double(diff[0], 0);
+    out[kGnn] = f2_to_double(diff[1], 0);
+    out[kGzz] = f2_to_double(diff[2], 0);
+    out[kGen] = f2_to_double(Dz, 0);
+    out[kGez] = f2_to_double(Dy, 0);
+    out[kGnz] = f2_to_double(Dx, 0);
+  }
+  return true;
+}
+
 // FP64 evaluations for the pairs the float-pair paths decline (out of line).
 template <int F>
 HG_COLD double pair_field_fp64(const Rel& q, const Tables& T);
@@ -1193,7 +1396,24 @@ HG_COLD double pair_field_fp64(const Rel& q, const Tables& T);
 // All ten fields of one pair: the signed edge/face combinations (without G,
 // rho and units).  s = -1 for index 0 (lower bound), +1 for index 1 (upper).
 template <bool LEAN>
+HG_HD __forceinline__ void pair_all_geom(const Rel& q, const Tables& T, double out[kNumFields]);
+
+// The FP64 geometry for the pairs pair_all_f2 declines (out of line: rare).
+HG_COLD void pair_all_fp64(const Rel& q, const Tables& T, double* out);
+
+// All ten fields of one pair: on float pairs (pair_all_f2) with the lean
+// math, else (or where that declines) on the FP64 geometry.
+template <bool LEAN>
 HG_HD __forceinline__ void pair_all(const Rel& q, const Tables& T, double out[kNumFields]) {
+  if (!LEAN) {
+    pair_all_geom<false>(q, T, out);
+  } else if (!pair_all_f2<true>(q, T, out)) {
+    pair_all_fp64(q, T, out);
+  }
+}
+
+template <bool LEAN>
+HG_HD __forceinline__ void pair_all_geom(const Rel& q, const Tables& T, double out[kNumFields]) {
   Geom g;
   make_geom<LEAN>(q, g);
   EdgeSet Ex, Ey, Ez;
@@ -1253,7 +1473,7 @@ template <int F, bool LEAN>
 HG_HD __forceinline__ double pair_field_geom(const Rel& q, const Tables& T) {
   if (F == kPotential) {
     double out[kNumFields];
-    pair_all<LEAN>(q, T, out);
+    pair_all_geom<LEAN>(q, T, out);
     return out[kPotential];
   }
   Geom g;
@@ -1303,12 +1523,21 @@ HG_COLD double pair_field_fp64(const Rel& q, const Tables& T) {
   return pair_field_geom<F, true>(q, T);
 }
 
+HG_COLD void pair_all_fp64(const Rel& q, const Tables& T, double* out) {
+  pair_all_geom<true>(q, T, out);
+}
+
 // One field of one pair.  With the lean math, the acceleration components and
 // the diagonal tensor components run on float pairs (pair_grad_f2,
 // pair_diag_f2); the rest, and the pairs those decline, on the FP64
 // geometry (pair_field_geom).
 template <int F, bool LEAN>
 HG_HD __forceinline__ double pair_field(const Rel& q, const Tables& T) {
+  if (LEAN && F == kPotential) {
+    double v;
+    if (pair_all_f2<false>(q, T, &v)) return v;
+    return pair_field_fp64<F>(q, T);
+  }
   if (LEAN && (F == kGe || F == kGn || F == kGz)) {
     double v;
     if (pair_grad_p2<(F == kGe ? 0 : (F == kGn ? 1 : 2))>(q, T, v, nullptr)) return v;
