@@ -112,7 +112,8 @@ def parse_args():
                    help="layer: the 1e6-prism layer with the batched and served blocks "
                         "(default); the others run one secondary workload alone")
     p.add_argument("--batch-problems", type=int, default=256)
-    p.add_argument("--autotune", action="store_true")
+    p.add_argument("--no-autotune", action="store_true",
+                   help="batched block: run the fixed plan instead of the autotuned shapes")
     p.add_argument("--arrival-seconds", type=float, default=4.0)
     p.add_argument("--rate", type=float, default=200.0)
     p.add_argument("--max-backlog-s", type=float, default=2.0)
@@ -312,25 +313,33 @@ def batched_block(args, torch, local, timed_replays=2):
     from harmonica_gb300.gravity import forward_on_device
 
     problems = synthetic.batched_problems(args.batch_problems, seed=4)
+
+    def graph_time(batch):
+        batch.capture()
+        batch.replay()
+        torch.cuda.synchronize()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record()
+        for _ in range(timed_replays):
+            batch.replay()
+        t1.record()
+        torch.cuda.synchronize()
+        return t0.elapsed_time(t1) * 1e-3 / timed_replays
+
     tuned = None
-    chunk = ctas = 0
-    if args.autotune:
-        tuned = autotune(problems, repeats=1)
-        chunk, ctas = tuned["chunk_prisms"], tuned["n_ctas"]
-    batch = PrismBatch(problems, chunk_prisms=chunk, n_ctas=ctas, validate=False)
+    fixed_s = None
+    if not args.no_autotune:
+        t_tune = time.perf_counter()
+        tuned = autotune(problems, repeats=1, cache=None)
+        tuned["seconds"] = time.perf_counter() - t_tune
+        fixed = PrismBatch(problems, validate=False, shapes=None)
+        fixed_s = graph_time(fixed)
+        fixed.close()
+    batch = PrismBatch(problems, validate=False, shapes=tuned["shapes"] if tuned else None)
     info = batch.info()
     pairs = info["pairs"]
-    batch.capture()
-    batch.replay()
-    torch.cuda.synchronize()
-    t0 = torch.cuda.Event(enable_timing=True)
-    t1 = torch.cuda.Event(enable_timing=True)
-    t0.record()
-    for _ in range(timed_replays):
-        batch.replay()
-    t1.record()
-    torch.cuda.synchronize()
-    batched_s = t0.elapsed_time(t1) * 1e-3 / timed_replays
+    batched_s = graph_time(batch)
     batched = [o.clone() for o in batch.outputs]
 
     # (b) one launch per problem on the batch's resident inputs
@@ -380,7 +389,13 @@ def batched_block(args, torch, local, timed_replays=2):
                                          "resident inputs"},
         "batched_over_per_problem_launches": device_s / batched_s,
         "max_rel_diff_batched_vs_per_problem": worst,
-        "work_items": info["items"], "persistent_ctas": info["ctas"], "tuned": tuned,
+        "work_items": info["items"], "persistent_ctas": info["ctas"],
+        "tuned": None if tuned is None else {
+            "shapes": tuned["shapes"], "tuning_seconds": tuned["seconds"],
+            "candidates_timed": len(tuned["candidates"]),
+            "fixed_plan": {"value": pairs / fixed_s, "unit": "pairs/s",
+                           "plan": "128 points per CTA, automatic chunk and CTAs"},
+            "tuned_over_fixed": fixed_s / batched_s},
         "timed_replays": timed_replays,
     }
 
@@ -409,7 +424,6 @@ def served_block(args, torch, local):
     for f in warm:
         f.result()
     srv.max_backlog_s = args.max_backlog_s
-    srv.rate = srv.nominal_rate  # start the stream from the nominal rate estimate
     offered = sum(r["n_stations"] * models[r["model"]][0].shape[0] for r in stream)
     futures = []
     t0 = time.perf_counter()

@@ -28,8 +28,8 @@ HEADERS = (
 
 #: translation units compiled into the library
 SOURCES = (
-    "prism_forward.cu", "prism_batch.cu", "prism_adjoint.cu", "point_forward.cu",
-    "prism_magnetic.cu", "tesseroid_forward.cu",
+    "prism_forward.cu", "prism_batch.cu", "prism_batch64.cu", "prism_adjoint.cu",
+    "point_forward.cu", "prism_magnetic.cu", "tesseroid_forward.cu",
 )
 #: the benchmark-support library (include/harmonica_gb300_bench.h), kept out
 #: of the product library; it links against the product library
@@ -166,6 +166,16 @@ class HgProblemPlan(ctypes.Structure):
     ]
 
 
+class HgBatchShape(ctypes.Structure):
+    """ctypes mirror of ``hg_batch_shape`` (include/harmonica_gb300.h)."""
+
+    _fields_ = [
+        ("chunk_prisms", ctypes.c_int64),
+        ("points_per_cta", ctypes.c_int32),
+        ("n_ctas", ctypes.c_int32),
+    ]
+
+
 class HgProblem(ctypes.Structure):
     """ctypes mirror of ``hg_problem`` (include/harmonica_gb300.h)."""
 
@@ -210,6 +220,11 @@ PROTOTYPES = {
     "hg_batch_create": (
         ctypes.c_int,
         [ctypes.POINTER(HgProblem), ctypes.c_int64, ctypes.c_int64, ctypes.c_int32,
+         ctypes.POINTER(ctypes.c_void_p)],
+    ),
+    "hg_batch_create_shaped": (
+        ctypes.c_int,
+        [ctypes.POINTER(HgProblem), ctypes.c_int64, ctypes.POINTER(HgBatchShape),
          ctypes.POINTER(ctypes.c_void_p)],
     ),
     "hg_batch_workspace": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t)]),

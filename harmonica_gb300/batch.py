@@ -3,11 +3,13 @@ Many independent prism forward problems in one persistent launch.
 
 :class:`PrismBatch` wraps the C ABI ``hg_batch_*``: it keeps every problem's
 inputs and outputs resident on the device, builds the work list once, and
-runs it with one memset and two launches on the current stream — directly or
-replayed from a captured CUDA graph.  :func:`autotune` picks the prism chunk
-size and the number of persistent CTAs by timing candidate plans on the real
-problem set and caches the choice (keyed by device and a coarse signature of
-the batch) in a JSON file.
+runs it with one memset, one launch per field present and one reduction on
+the current stream — directly or replayed from a captured CUDA graph.
+:func:`autotune` picks, per field, the shape of the work (observation points
+per CTA and per work item, which is also the prism tile staged in shared
+memory; prisms per work item; persistent CTAs) by timing candidate shapes on
+a sample of the real problems, and caches the choice (keyed by device and a
+coarse signature of the batch) in a JSON file.
 
 This replaces a loop of ``harmonica.prism_gravity`` calls, one per problem
 (``src/harmonica/_forward/prisms/gravity.py:51-236``).
@@ -42,20 +44,35 @@ class PrismBatch:
         Host arrays are copied to the device once; torch CUDA tensors of
         float64 are used in place.
     chunk_prisms, n_ctas : int
-        Work-list shape (0 = automatic); see :func:`autotune`.
+        Work-list shape for every field (0 = automatic, 128 points per CTA).
+    shapes : "auto", dict or None
+        Per-field shapes ``{field: {"chunk_prisms", "points_per_cta",
+        "n_ctas"}}`` (as :func:`autotune` returns them); fields not listed
+        take ``chunk_prisms`` / ``n_ctas``.  ``"auto"`` (the default) runs
+        :func:`autotune` on the problems (cached per device and batch
+        signature) unless ``chunk_prisms`` or ``n_ctas`` is given; ``None``
+        takes the fixed plan (128 points per CTA, ``chunk_prisms`` and
+        ``n_ctas``).
     check_singular : bool
         Scan tensor-field problems for points on singular edges/vertices
         (one flag per problem, see :meth:`singular`).
     """
 
     def __init__(self, problems, chunk_prisms=0, n_ctas=0, check_singular=False, device=None,
-                 validate=True):
+                 validate=True, shapes="auto"):
         import torch
 
         from .gravity import _device
 
         self.torch = torch
         self.device = _device(device)
+        if isinstance(shapes, str):
+            if shapes != "auto":
+                raise ValueError(f"shapes must be 'auto', a dict or None, not {shapes!r}")
+            explicit = chunk_prisms or n_ctas
+            shapes = None if explicit or not problems else autotune(
+                problems, device=self.device)["shapes"]
+        self.shapes = shapes
         self.lib = _native.lib()
         self.fields = []
         self.shapes = []
@@ -86,8 +103,14 @@ class PrismBatch:
                 p.out = out.data_ptr() if out.numel() else None
                 p.singular_flag = self.flags[k:].data_ptr()
             handle = ctypes.c_void_p()
-            _native.check(self.lib.hg_batch_create(probs, len(problems), int(chunk_prisms),
-                                                   int(n_ctas), ctypes.byref(handle)))
+            table = (_native.HgBatchShape * len(FIELD_CODES))()
+            for name, code in FIELD_CODES.items():
+                shape = (shapes or {}).get(name, {})
+                table[code].chunk_prisms = int(shape.get("chunk_prisms", chunk_prisms))
+                table[code].points_per_cta = int(shape.get("points_per_cta", 128))
+                table[code].n_ctas = int(shape.get("n_ctas", n_ctas))
+            _native.check(self.lib.hg_batch_create_shaped(probs, len(problems), table,
+                                                          ctypes.byref(handle)))
             self.handle = handle
             ws = ctypes.c_size_t(0)
             _native.check(self.lib.hg_batch_workspace(self.handle, ctypes.byref(ws)))
@@ -175,13 +198,15 @@ class PrismBatch:
             pass
 
 
-def prism_gravity_batch(problems, chunk_prisms=0, n_ctas=0, disable_checks=False, device=None):
+def prism_gravity_batch(problems, chunk_prisms=0, n_ctas=0, disable_checks=False, device=None,
+                        shapes="auto"):
     """
     Forward many problems in one persistent launch; returns a list of arrays
-    equal (within FP64 rounding) to ``prism_gravity`` of each problem.
+    equal (within FP64 rounding) to ``prism_gravity`` of each problem.  The
+    work shape per field is autotuned by default (see :class:`PrismBatch`).
     """
     batch = PrismBatch(problems, chunk_prisms, n_ctas, check_singular=not disable_checks,
-                       device=device, validate=not disable_checks)
+                       device=device, validate=not disable_checks, shapes=shapes)
     try:
         batch.run()
         results = batch.results()
@@ -211,16 +236,45 @@ def _load_cache(path):
         return {}
 
 
-def autotune(problems, chunks=(2048, 8192, 32768), cta_multipliers=(1, 2),
-             repeats=1, cache=DEFAULT_CACHE, device=None, sample=32):
-    """
-    Pick (chunk_prisms, n_ctas) for a problem set by timing candidate plans.
+def _time_batch(problems, shapes, repeats, dev):
+    """Best of ``repeats`` timed runs (ms, CUDA events) after one warm-up."""
+    import torch
 
-    Each candidate is built as a :class:`PrismBatch` over an evenly strided
-    sample of at most ``sample`` problems and run ``repeats`` times after one
-    warm-up (CUDA events); the fastest is returned and cached under
-    ``(device name, signature(problems))``.  Returns a dict with the choice
-    and the timings.
+    b = PrismBatch(problems, device=dev, validate=False, shapes=shapes)  # None: fixed plan
+    try:
+        b.run()
+        torch.cuda.synchronize(dev)
+        best = float("inf")
+        for _ in range(repeats):
+            t0 = torch.cuda.Event(enable_timing=True)
+            t1 = torch.cuda.Event(enable_timing=True)
+            t0.record()
+            b.run()
+            t1.record()
+            torch.cuda.synchronize(dev)
+            best = min(best, t0.elapsed_time(t1))
+        return best, b.info()["ctas"]
+    finally:
+        b.close()
+
+
+def autotune(problems, chunks=(2048, 8192, 32768), points_per_cta=(64, 128),
+             cta_multipliers=(1, 2), repeats=1, cache=DEFAULT_CACHE, device=None, sample=8):
+    """
+    Pick, per field of a problem set, the work shape by timing candidates.
+
+    For each field present, an evenly strided sample of at most ``sample`` of
+    its problems is run with every combination of points per CTA (the point
+    tile of a work item and the prism tile staged in shared memory), prisms
+    per work item and persistent CTAs (``cta_multipliers`` x the occupancy
+    of one wave, divided by the largest multiplier), ``repeats`` timed runs
+    after one warm-up (CUDA events), and against the fixed shape (128 points
+    per CTA, automatic chunk and CTAs).  The fastest shape per field is
+    returned and cached under ``(device name, signature(problems))``::
+
+        {"shapes": {field: {"chunk_prisms", "points_per_cta", "n_ctas", "ms",
+                            "fixed_ms", "gain"}},
+         "candidates": [...]}
     """
     import torch
 
@@ -232,33 +286,27 @@ def autotune(problems, chunks=(2048, 8192, 32768), cta_multipliers=(1, 2),
     table = _load_cache(cache) if cache else {}
     if key in table:
         return table[key]
-    if sample and len(problems) > sample:
-        step = len(problems) / sample
-        problems = [problems[int(k * step)] for k in range(sample)]
-    base = PrismBatch(problems, device=dev, validate=False)
-    occ = base.info()["ctas"]
-    base.close()
-    timings = []
-    for chunk in chunks:
-        for mult in cta_multipliers:
-            b = PrismBatch(problems, chunk_prisms=chunk, n_ctas=occ * mult // max(cta_multipliers),
-                           device=dev, validate=False)
-            b.run()
-            torch.cuda.synchronize(dev)
-            best = float("inf")
-            for _ in range(repeats):
-                t0 = torch.cuda.Event(enable_timing=True)
-                t1 = torch.cuda.Event(enable_timing=True)
-                t0.record()
-                b.run()
-                t1.record()
-                torch.cuda.synchronize(dev)
-                best = min(best, t0.elapsed_time(t1))
-            timings.append({"chunk_prisms": chunk, "n_ctas": b.info()["ctas"], "ms": best})
-            b.close()
-    choice = min(timings, key=lambda t: t["ms"])
-    result = {"chunk_prisms": choice["chunk_prisms"], "n_ctas": choice["n_ctas"],
-              "ms": choice["ms"], "candidates": timings}
+    fields = sorted({p["field"] for p in problems}, key=lambda f: FIELD_CODES[f])
+    result = {"shapes": {}, "candidates": []}
+    for field in fields:
+        mine = [p for p in problems if p["field"] == field]
+        if sample and len(mine) > sample:
+            step = len(mine) / sample
+            mine = [mine[int(k * step)] for k in range(sample)]
+        fixed_ms, occ = _time_batch(mine, None, repeats, dev)
+        best = None
+        for ppc in points_per_cta:
+            for chunk in chunks:
+                for mult in cta_multipliers:
+                    ctas = max(1, occ * (128 // ppc) * mult // max(cta_multipliers))
+                    shape = {"chunk_prisms": int(chunk), "points_per_cta": int(ppc),
+                             "n_ctas": int(ctas)}
+                    ms, _ = _time_batch(mine, {field: shape}, repeats, dev)
+                    result["candidates"].append({"field": field, **shape, "ms": ms})
+                    if best is None or ms < best["ms"]:
+                        best = {**shape, "ms": ms}
+        best.update(fixed_ms=fixed_ms, gain=fixed_ms / best["ms"])
+        result["shapes"][field] = best
     if cache:
         table[key] = result
         os.makedirs(os.path.dirname(cache), exist_ok=True)

@@ -82,11 +82,14 @@ struct LayerSource {
 };
 
 // ---------------------------------------------------------------------------
-struct SmemTile {
-  double w[kTile], e[kTile], s[kTile], n[kTile], b[kTile], t[kTile], rho[kTile];
-  double dx[kTile], dy[kTile], dz[kTile];  // extents
-  int null[kTile];
+// A tile of TILE prisms staged in shared memory (structure of arrays).
+template <int TILE>
+struct SmemTileT {
+  double w[TILE], e[TILE], s[TILE], n[TILE], b[TILE], t[TILE], rho[TILE];
+  double dx[TILE], dy[TILE], dz[TILE];  // extents
+  int null[TILE];
 };
+using SmemTile = SmemTileT<kTile>;
 
 struct SmemTables {
   double logc[lean::kLogTableSize], logl[lean::kLogTableSize];
@@ -112,18 +115,19 @@ struct SmemTables {
 };
 
 // Adds to acc[] the field(s) F of prisms [p0, p1) of `src` at this thread's
-// point (pe, pn, pu).  Must be called by every thread of the CTA (it
-// synchronises around each shared-memory tile).  With check_singular, ORs
-// into `singular` whether the point is a singular point of any prism (null
-// prisms included, as gravity.py:207-214 scans before discarding) for the
-// tensor fields in sing_mask.  Tensor values at singular points are NaN.
-template <int F, class Source>
+// point (pe, pn, pu), staging TILE prisms at a time (the CTA has TILE
+// threads).  Must be called by every thread of the CTA (it synchronises
+// around each shared-memory tile).  With check_singular, ORs into `singular`
+// whether the point is a singular point of any prism (null prisms included,
+// as gravity.py:207-214 scans before discarding) for the tensor fields in
+// sing_mask.  Tensor values at singular points are NaN.
+template <int F, class Source, int TILE = kTile>
 __device__ __forceinline__ void accumulate(const Source& src, int64_t p0, int64_t p1, double pe,
                                            double pn, double pu, bool active, bool check_singular,
-                                           uint32_t sing_mask, SmemTile& sh, const Tables& T,
-                                           double* acc, bool& singular) {
-  for (int64_t base = p0; base < p1; base += kTile) {
-    const int cnt = (int)min((int64_t)kTile, p1 - base);
+                                           uint32_t sing_mask, SmemTileT<TILE>& sh,
+                                           const Tables& T, double* acc, bool& singular) {
+  for (int64_t base = p0; base < p1; base += TILE) {
+    const int cnt = (int)min((int64_t)TILE, p1 - base);
     __syncthreads();
     if ((int)threadIdx.x < cnt) {
       double w, e, s, n, b, t, rho;

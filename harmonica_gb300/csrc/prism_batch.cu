@@ -19,7 +19,7 @@
 #include <vector>
 
 #include "../../include/harmonica_gb300.h"
-#include "forward_core.cuh"
+#include "batch_core.cuh"
 
 namespace hg {
 
@@ -28,87 +28,8 @@ namespace hg {
 int set_error(int code, const std::string& msg);
 int cuda_check(cudaError_t e, const char* what);
 
-struct ProblemDev {
-  const double* e;
-  const double* n;
-  const double* u;
-  int64_t n_obs;
-  const double* soa;
-  int64_t stride;
-  int64_t n_prisms;
-  int64_t chunk;        // prisms per work item
-  int64_t n_chunks;
-  int64_t part_offset;  // first partial (in doubles) of this problem in the workspace
-  double* out;
-  int32_t* flag;
-  int32_t field;
-  int32_t check_singular;
-};
-
-struct WorkItem {
-  int32_t problem;
-  int32_t tile;
-  int32_t chunk;
-  int32_t pad;
-};
-
-template <int F>
-__device__ __forceinline__ void run_item(const ProblemDev& P, const WorkItem& w, SmemTile& sh,
-                                         const Tables& T, double* __restrict__ part) {
-  const int64_t i = (int64_t)w.tile * kThreads + threadIdx.x;
-  const bool active = i < P.n_obs;
-  const double pe = active ? P.e[i] : 0.0;
-  const double pn = active ? P.n[i] : 0.0;
-  const double pu = active ? P.u[i] : 0.0;
-  const int64_t p0 = (int64_t)w.chunk * P.chunk;
-  const int64_t p1 = min(p0 + P.chunk, P.n_prisms);
-  double acc[1] = {0.0};
-  bool singular = false;
-  const bool check = P.check_singular && P.flag != nullptr;
-  accumulate<F>(ListSource{P.soa, P.stride}, p0, p1, pe, pn, pu, active, check, 1u << F, sh, T,
-                acc, singular);
-  if (singular) atomicOr(P.flag, 1);
-  if (active) part[P.part_offset + (int64_t)w.chunk * P.n_obs + i] = acc[0];
-}
-
-// Persistent kernel for the work items of one field F (the items of a batch
-// are grouped by field and each group runs its own launch): specialised per
-// field, so it keeps that field's register budget and instruction footprint.
-template <int F>
-__global__ void __launch_bounds__(kThreads, MinBlocks<F>::value)
-    batch_kernel(const ProblemDev* __restrict__ probs, const WorkItem* __restrict__ items,
-                 int64_t n_items, unsigned long long* __restrict__ counter,
-                 double* __restrict__ part) {
-  __shared__ SmemTile sh;
-  __shared__ SmemTables tabs;
-  __shared__ long long next;
-  const Tables T = tabs.stage();
-  for (;;) {
-    __syncthreads();  // everyone is done with `next` and the previous tile
-    if (threadIdx.x == 0) next = (long long)atomicAdd(counter, 1ull);
-    __syncthreads();
-    const long long it = next;
-    if (it >= n_items) break;
-    const WorkItem w = items[it];
-    run_item<F>(probs[w.problem], w, sh, T, part);
-  }
-}
-
-using BatchKernel = void (*)(const ProblemDev*, const WorkItem*, int64_t, unsigned long long*,
-                             double*);
-BatchKernel batch_kernel_for(int f) {
-  switch (f) {
-    case kPotential: return batch_kernel<kPotential>;
-    case kGe: return batch_kernel<kGe>;
-    case kGn: return batch_kernel<kGn>;
-    case kGz: return batch_kernel<kGz>;
-    case kGee: return batch_kernel<kGee>;
-    case kGnn: return batch_kernel<kGnn>;
-    case kGzz: return batch_kernel<kGzz>;
-    case kGen: return batch_kernel<kGen>;
-    case kGez: return batch_kernel<kGez>;
-    default: return batch_kernel<kGnz>;
-  }
+BatchKernel batch_kernel_for(int f, int threads) {
+  return threads == 64 ? batch_kernel_for64(f) : batch_kernel_table<kThreads>(f);
 }
 
 // out_p[i] = scale(field_p) * sum_c part_p[c][i], chunks in order.
@@ -134,6 +55,7 @@ struct hg_batch {
   int64_t seg_begin[kNumFields] = {};  // the items of field f: [seg_begin, seg_begin + seg_count)
   int64_t seg_count[kNumFields] = {};
   int32_t seg_ctas[kNumFields] = {};   // CTAs of field f's persistent launch
+  int32_t seg_threads[kNumFields] = {};  // points per CTA of field f's launch
   int64_t n_ctas = 0;
   int64_t partials = 0;  // doubles
   double pairs = 0.0;
@@ -152,34 +74,38 @@ int64_t round_up(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
 
 extern "C" {
 
-int hg_batch_create(const hg_problem* problems, int64_t n_problems, int64_t chunk_prisms,
-                    int32_t n_ctas, hg_batch** batch) {
-  if (!batch || n_problems < 0 || (n_problems > 0 && !problems))
+int hg_batch_create_shaped(const hg_problem* problems, int64_t n_problems,
+                           const hg_batch_shape* shapes, hg_batch** batch) {
+  if (!batch || !shapes || n_problems < 0 || (n_problems > 0 && !problems))
     return set_error(HG_ERR_INVALID, "bad arguments");
   if (n_problems > 65535) return set_error(HG_ERR_INVALID, "at most 65535 problems per batch");
   *batch = nullptr;
+  for (int f = 0; f < kNumFields; f++)
+    if (shapes[f].points_per_cta != 0 && shapes[f].points_per_cta != 64 &&
+        shapes[f].points_per_cta != 128)
+      return set_error(HG_ERR_INVALID, "points_per_cta must be 0, 64 or 128");
   int device = 0;
   int rc = cuda_check(cudaGetDevice(&device), "cudaGetDevice");
   if (rc != HG_OK) return rc;
   int sms = kSmCount;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-  // CTAs of each field's persistent launch: the given count, else one full
-  // wave of that field's kernel
-  int32_t ctas_for[kNumFields];
+  // per field: points per CTA, and the CTAs of its persistent launch (the
+  // given count, else one full wave of that field's kernel)
+  int32_t threads_for[kNumFields], ctas_for[kNumFields];
   for (int f = 0; f < kNumFields; f++) {
-    ctas_for[f] = n_ctas;
-    if (n_ctas <= 0) {
+    threads_for[f] = shapes[f].points_per_cta > 0 ? shapes[f].points_per_cta : kThreads;
+    ctas_for[f] = shapes[f].n_ctas;
+    if (ctas_for[f] <= 0) {
       int per_sm = 0;
       rc = cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                          &per_sm, batch_kernel_for(f), kThreads, 0),
+                          &per_sm, batch_kernel_for(f, threads_for[f]), threads_for[f], 0),
                       "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
       if (rc != HG_OK) return rc;
       ctas_for[f] = (int32_t)std::max(1, per_sm) * sms;
     }
   }
-  if (n_ctas <= 0) n_ctas = ctas_for[kGz];
   std::vector<ProblemDev> probs((size_t)n_problems);
-  int64_t total_pairs_all = 0;
+  double field_pairs[kNumFields] = {};
   for (int64_t p = 0; p < n_problems; p++) {
     const hg_problem& q = problems[p];
     if (q.n_obs < 0 || q.n_prisms < 0 || q.prism_stride < q.n_prisms || q.field < 0 ||
@@ -189,15 +115,21 @@ int hg_batch_create(const hg_problem* problems, int64_t n_problems, int64_t chun
       return set_error(HG_ERR_INVALID, "null pointer in problem " + std::to_string(p));
     if (q.n_prisms > 0 && !q.prisms_soa)
       return set_error(HG_ERR_INVALID, "null prisms in problem " + std::to_string(p));
-    total_pairs_all += q.n_obs * q.n_prisms;
+    field_pairs[q.field] += (double)q.n_obs * (double)q.n_prisms;
   }
-  // Chunk size: enough items to keep every CTA busy ~16 times over, with
-  // chunks a multiple of the shared-memory tile.
-  int64_t chunk_default = kTile;
-  if (chunk_prisms <= 0) {
-    const double target_items = 16.0 * n_ctas;
-    const double pairs_per_item = std::max(1.0, (double)total_pairs_all / target_items);
-    chunk_default = round_up(std::max<int64_t>(kTile, (int64_t)(pairs_per_item / kThreads)), kTile);
+  // Chunk size per field: the given one (rounded up to whole prism tiles of
+  // that field's CTA shape), else enough items to keep every CTA of the
+  // field's launch busy ~16 times over.
+  int64_t chunk_for[kNumFields];
+  for (int f = 0; f < kNumFields; f++) {
+    const int64_t tile = threads_for[f];
+    if (shapes[f].chunk_prisms > 0) {
+      chunk_for[f] = round_up(shapes[f].chunk_prisms, tile);
+    } else {
+      const double target_items = 16.0 * ctas_for[f];
+      const double pairs_per_item = std::max(1.0, field_pairs[f] / target_items);
+      chunk_for[f] = round_up(std::max<int64_t>(tile, (int64_t)(pairs_per_item / tile)), tile);
+    }
   }
   std::vector<WorkItem> items;
   std::vector<double> cost;
@@ -213,7 +145,7 @@ int hg_batch_create(const hg_problem* problems, int64_t n_problems, int64_t chun
     d.soa = q.prisms_soa;
     d.stride = q.prism_stride;
     d.n_prisms = q.n_prisms;
-    d.chunk = chunk_prisms > 0 ? round_up(chunk_prisms, kTile) : chunk_default;
+    d.chunk = chunk_for[q.field];
     d.n_chunks = q.n_prisms > 0 ? (q.n_prisms + d.chunk - 1) / d.chunk : 0;
     d.part_offset = part;
     d.out = q.out;
@@ -222,14 +154,15 @@ int hg_batch_create(const hg_problem* problems, int64_t n_problems, int64_t chun
     d.check_singular = q.check_singular;
     part += d.n_chunks * q.n_obs;
     pairs += (double)q.n_obs * (double)q.n_prisms;
-    const int64_t tiles = (q.n_obs + kThreads - 1) / kThreads;
+    const int64_t threads = threads_for[q.field];
+    const int64_t tiles = (q.n_obs + threads - 1) / threads;
     if (tiles > INT32_MAX || d.n_chunks > INT32_MAX || n_problems > INT32_MAX)
       return set_error(HG_ERR_INVALID, "problem too large for the work list");
     for (int64_t t = 0; t < tiles; t++)
       for (int64_t c = 0; c < d.n_chunks; c++) {
         items.push_back(WorkItem{(int32_t)p, (int32_t)t, (int32_t)c, 0});
         const double np = (double)std::min(d.chunk, q.n_prisms - c * d.chunk);
-        cost.push_back(np);  // every item runs kThreads threads over np prisms
+        cost.push_back(np * (double)threads);  // threads x prisms of the item
       }
   }
   // grouped by field; within a field longest items first (list
@@ -251,10 +184,13 @@ int hg_batch_create(const hg_problem* problems, int64_t n_problems, int64_t chun
     if (b->seg_count[f] == 0) b->seg_begin[f] = (int64_t)k;
     b->seg_count[f]++;
   }
-  for (int f = 0; f < kNumFields; f++) b->seg_ctas[f] = ctas_for[f];
+  for (int f = 0; f < kNumFields; f++) {
+    b->seg_ctas[f] = ctas_for[f];
+    b->seg_threads[f] = threads_for[f];
+  }
   b->n_problems = n_problems;
   b->n_items = (int64_t)sorted.size();
-  b->n_ctas = n_ctas;
+  b->n_ctas = ctas_for[kGz];
   b->partials = part;
   b->pairs = pairs;
   b->device = device;
@@ -280,6 +216,13 @@ int hg_batch_create(const hg_problem* problems, int64_t n_problems, int64_t chun
   }
   *batch = b;
   return HG_OK;
+}
+
+int hg_batch_create(const hg_problem* problems, int64_t n_problems, int64_t chunk_prisms,
+                    int32_t n_ctas, hg_batch** batch) {
+  hg_batch_shape shapes[kNumFields];
+  for (int f = 0; f < kNumFields; f++) shapes[f] = hg_batch_shape{chunk_prisms, kThreads, n_ctas};
+  return hg_batch_create_shaped(problems, n_problems, shapes, batch);
 }
 
 int hg_batch_workspace(const hg_batch* batch, size_t* bytes) {
@@ -312,7 +255,8 @@ int hg_batch_run(const hg_batch* batch, void* workspace, size_t workspace_bytes,
   if (rc != HG_OK) return rc;
   for (int f = 0; f < kNumFields; f++) {
     if (batch->seg_count[f] == 0) continue;
-    batch_kernel_for(f)<<<(unsigned)batch->seg_ctas[f], kThreads, 0, st>>>(
+    const int threads = batch->seg_threads[f];
+    batch_kernel_for(f, threads)<<<(unsigned)batch->seg_ctas[f], threads, 0, st>>>(
         batch->d_probs, batch->d_items + batch->seg_begin[f], batch->seg_count[f], counter + f,
         part);
     rc = cuda_check(cudaGetLastError(), "batch_kernel launch");

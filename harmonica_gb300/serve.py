@@ -22,9 +22,10 @@ arrive at any time through :meth:`PrismServer.submit` and get a
   waiting for the earlier ones to finish;
 * optionally **sheds load** (``max_backlog_s``): a request is refused at
   submission (its future fails with :class:`ServerOverloaded`) when the
-  pairs not yet finished, its own included, would take longer than that at
-  the measured rate, so the latency of the accepted requests stays bounded
-  under overload;
+  unfinished work, its own included, would take longer than that; work is
+  priced per field at the pairs/s measured on the GPU (each round times
+  each field's launch with CUDA events), so the latency of the accepted
+  requests stays bounded under overload;
 * finishes requests with ``hg_round_reduce`` (each point's chunks added in
   fixed order), copies results to pinned host memory and resolves the
   futures, recording arrival-to-result latency.
@@ -133,12 +134,12 @@ class PrismServer:
         Largest prism chunk of a work item.
     nominal_rate : float
         Pairs per second used for the virtual deadlines of the scheduling
-        order and as the first estimate of the GPU's rate for load shedding
-        (then replaced by the measured rate of finished rounds).
+        order and as the first estimate of every field's rate for load
+        shedding (then replaced by each field's measured rate).
     max_backlog_s : float or None
         Refuse new requests (:class:`ServerOverloaded`) while the unfinished
-        pairs, the new request's included, exceed this many seconds of work;
-        ``None`` accepts everything.
+        work, the new request's included, exceeds this many seconds at the
+        measured rates; ``None`` accepts everything.
     """
 
     def __init__(self, device=None, memory_budget=120e9, round_pairs=4e8, max_active=1024,
@@ -160,10 +161,10 @@ class PrismServer:
         self.rounds_in_flight = int(rounds_in_flight)
         self.nominal_rate = float(nominal_rate)
         self.max_backlog_s = None if max_backlog_s is None else float(max_backlog_s)
-        self.rate = float(nominal_rate)  # measured pairs/s of finished rounds
-        self.backlog_pairs = 0.0         # pairs of accepted requests not yet finished
+        # measured pairs/s of each field's launches (field code -> rate)
+        self.rates = {code: float(nominal_rate) for code in FIELD_CODES.values()}
+        self.backlog_s = 0.0  # estimated seconds of accepted, unfinished work
         self.rejected = 0
-        self._busy_since = None
         self.layers = collections.OrderedDict()
         self.inbox = queue.Queue()
         self.pending = collections.deque()
@@ -265,17 +266,18 @@ class PrismServer:
             n_prisms = known.n_prisms if known is not None else (req.n_prisms or 0)
             req.pairs = float(req.n_obs) * float(n_prisms)
             req.deadline = req.t_submit + req.pairs / self.nominal_rate
-            if (self.max_backlog_s is not None and self.backlog_pairs > 0
-                    and (self.backlog_pairs + req.pairs) / self.rate > self.max_backlog_s):
+            req.cost_s = req.pairs / self.rates[FIELD_CODES[field]]
+            if (self.max_backlog_s is not None and self.backlog_s > 0
+                    and self.backlog_s + req.cost_s > self.max_backlog_s):
                 self.rejected += 1
                 req.future.set_exception(ServerOverloaded(
-                    f"request of {req.pairs:.3g} pairs refused: the backlog of "
-                    f"{self.backlog_pairs:.3g} pairs is {self.backlog_pairs / self.rate:.2f} s "
-                    f"of work (limit {self.max_backlog_s} s)"))
+                    f"request of {req.pairs:.3g} pairs ({req.cost_s:.2f} s of work) refused: "
+                    f"the backlog is {self.backlog_s:.2f} s of work (limit "
+                    f"{self.max_backlog_s} s)"))
                 return req.future
             req.id = self._ids
             self._ids += 1
-            self.backlog_pairs += req.pairs
+            self.backlog_s += req.cost_s
         req.future.add_done_callback(self._forget_backlog(req))
         self.inbox.put(req)
         if self._broken is not None:  # the scheduler stopped while this was queued
@@ -283,12 +285,12 @@ class PrismServer:
         return req.future
 
     def _forget_backlog(self, req):
-        """Callback for a request's future: its pairs leave the backlog when
+        """Callback for a request's future: its work leaves the backlog when
         it finishes, fails or is cancelled."""
 
         def done(_future):
             with self._lock:
-                self.backlog_pairs = max(0.0, self.backlog_pairs - req.pairs)
+                self.backlog_s = max(0.0, self.backlog_s - req.cost_s)
 
         return done
 
@@ -308,7 +310,8 @@ class PrismServer:
         lat = np.array([r.t_done - r.t_submit for r in self.completed])
         out = {"completed": len(self.completed), "rounds": self.rounds,
                "pairs_done": self.pairs_done, "errors": len(self.errors),
-               "rejected": self.rejected, "rate_pairs_per_s": self.rate}
+               "rejected": self.rejected,
+               "rates_pairs_per_s": {name: self.rates[code] for name, code in FIELD_CODES.items()}}
         if lat.size:
             out.update(p50_ms=float(np.percentile(lat, 50) * 1e3),
                        p99_ms=float(np.percentile(lat, 99) * 1e3),
@@ -491,14 +494,14 @@ class PrismServer:
         """Items for the next round: earliest virtual deadline first (ties in
         arrival order), then grouped by field (each field runs its own
         specialised persistent launch).  Returns (items, per-field item
-        counts, finishing requests)."""
+        counts, finishing requests, per-field point-prism pairs)."""
         reqs = [r for r in self.active.values() if r.next_item < r.n_items]
         if not reqs:
-            return None, None, [], 0.0
+            return None, None, [], None
         reqs.sort(key=lambda r: (r.deadline, r.id))
         budget = self.round_pairs
         parts, finishing = [], []
-        pairs = 0.0
+        pairs = np.zeros(10)
         for r in reqs:
             if budget <= 0:
                 break
@@ -513,7 +516,7 @@ class PrismServer:
             n_prisms = r.layer.n_prisms if r.layer else r.n_prisms
             pts = np.minimum(KTHREADS, r.n_obs - items[:, 1].astype(np.int64) * KTHREADS)
             prs = np.minimum(r.chunk, n_prisms - items[:, 2].astype(np.int64) * r.chunk)
-            pairs += float(np.dot(pts, prs))
+            pairs[FIELD_CODES[r.field]] += float(np.dot(pts, prs))
             parts.append((FIELD_CODES[r.field], items))
             r.next_item += take
             budget -= take * per_item
@@ -547,10 +550,21 @@ class PrismServer:
             self.table_dev.copy_(buf["table"], non_blocking=True)
             items_dev = buf["items"][: items.size].to(self.dev, non_blocking=True)
             stream = self.compute.cuda_stream
-            field_counts = (ctypes.c_int64 * 10)(*counts.tolist())
-            _native.check(self.lib.hg_round_run(self.table_dev.data_ptr(), items_dev.data_ptr(),
-                                                field_counts, self.n_ctas,
-                                                self.counter.data_ptr(), stream))
+            # one launch per field, each between two events: the field's
+            # measured rate prices its requests for load shedding
+            timed, begin = [], 0
+            for code in np.nonzero(counts)[0]:
+                field_counts = (ctypes.c_int64 * 10)()
+                field_counts[code] = int(counts[code])
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(self.compute)
+                _native.check(self.lib.hg_round_run(
+                    self.table_dev.data_ptr(), items_dev.data_ptr() + 16 * begin, field_counts,
+                    self.n_ctas, self.counter.data_ptr(), stream))
+                e1.record(self.compute)
+                timed.append((int(code), float(pairs[code]), e0, e1))
+                begin += int(counts[code])
             if ids.size:
                 ids_dev = buf["ids"][: ids.size].to(self.dev, non_blocking=True)
                 _native.check(self.lib.hg_round_reduce(self.table_dev.data_ptr(),
@@ -561,19 +575,19 @@ class PrismServer:
             ev = torch.cuda.Event()
             ev.record(self.compute)
         buf["event"] = ev
-        self.in_flight.append((ev, finishing, pairs, time.perf_counter()))
+        self.in_flight.append((ev, finishing, timed))
         self.rounds += 1
 
     def _retire(self, block=False):
         while self.in_flight:
-            ev, finishing, pairs, launched = self.in_flight[0]
+            ev, finishing, timed = self.in_flight[0]
             if not block and not ev.query():
                 return
             ev.synchronize()
             self.in_flight.popleft()
             block = False
             now = time.perf_counter()
-            self._measure_rate(pairs, launched, now)
+            self._measure_rates(timed)
             flags = None
             if any(r.check_singular for r in finishing):
                 with self.torch.cuda.stream(self.compute):
@@ -590,15 +604,15 @@ class PrismServer:
                 self.completed.append(r)
                 r.future.set_result(result)
 
-    def _measure_rate(self, pairs, launched, now):
-        """Update the measured rate (pairs/s) from a finished round: its
-        pairs over the time since the later of its launch and the previous
-        round's end (rounds in flight overlap), smoothed over rounds."""
-        start = launched if self._busy_since is None else max(launched, self._busy_since)
-        self._busy_since = now if self.in_flight else None
-        if pairs > 0 and now > start:
-            sample = pairs / (now - start)
-            self.rate = sample if self.rounds <= 2 else 0.8 * self.rate + 0.2 * sample
+    def _measure_rates(self, timed):
+        """Update each field's measured rate (pairs/s) from the finished
+        round's launches (CUDA events around each), smoothed over rounds;
+        launches shorter than a millisecond are too short to time."""
+        for code, pairs, e0, e1 in timed:
+            ms = e0.elapsed_time(e1)
+            if pairs > 0 and ms >= 1.0:
+                with self._lock:
+                    self.rates[code] = 0.7 * self.rates[code] + 0.3 * pairs / (ms * 1e-3)
 
     def _release(self, r):
         self.active.pop(r.id, None)

@@ -177,10 +177,35 @@ typedef struct hg_batch hg_batch; /* opaque plan */
  * plan keeps device pointers of the problems, which must stay valid until
  * hg_batch_destroy).  chunk_prisms <= 0 and n_ctas <= 0 choose automatically
  * (about 16 work items per CTA; per field, one full wave of that field's
- * kernel).  A given n_ctas applies to every field's launch.
+ * kernel).  A given n_ctas applies to every field's launch; every field runs
+ * 128 points per CTA.
  */
 int hg_batch_create(const hg_problem *problems, int64_t n_problems, int64_t chunk_prisms,
                     int32_t n_ctas, hg_batch **batch);
+
+/*
+ * Shape of the work of one field in a batch (chosen per field by the
+ * autotuner of harmonica_gb300.batch):
+ *   chunk_prisms   : prisms per work item, rounded up to whole prism tiles
+ *                    (0: about 16 work items per CTA of the field's launch)
+ *   points_per_cta : observation points per CTA and per work item, which is
+ *                    also the prisms staged per shared-memory tile: 64 or 128
+ *                    (0: 128)
+ *   n_ctas         : CTAs of the field's persistent launch (0: one full wave)
+ */
+typedef struct hg_batch_shape {
+  int64_t chunk_prisms;
+  int32_t points_per_cta;
+  int32_t n_ctas;
+} hg_batch_shape;
+
+/*
+ * hg_batch_create with one shape per field code (shapes[0..9]); a problem's
+ * result is bitwise the same alone and in any batch built with the same
+ * shape for its field.
+ */
+int hg_batch_create_shaped(const hg_problem *problems, int64_t n_problems,
+                           const hg_batch_shape *shapes, hg_batch **batch);
 
 /* Bytes of device workspace hg_batch_run needs. */
 int hg_batch_workspace(const hg_batch *batch, size_t *bytes);

@@ -98,14 +98,34 @@ def test_empty_problems_and_flags(gpu_lib):
         hg.prism_gravity_batch(probs)
 
 
-def test_autotune_returns_a_candidate(gpu_lib, tmp_path):
+def test_autotune_picks_a_shape_per_field_and_caches_it(gpu_lib, tmp_path):
     probs = small_set(seed=3, n=8)
-    choice = hg.autotune(probs, chunks=(256, 1024), cta_multipliers=(1,), repeats=1,
-                         cache=str(tmp_path / "tune.json"))
-    assert choice["chunk_prisms"] in (256, 1024)
-    again = hg.autotune(probs, chunks=(256, 1024), cta_multipliers=(1,), repeats=1,
-                        cache=str(tmp_path / "tune.json"))
-    assert again == choice
+    kw = dict(chunks=(256, 1024), points_per_cta=(64, 128), cta_multipliers=(1,), repeats=1,
+              cache=str(tmp_path / "tune.json"))
+    choice = hg.autotune(probs, **kw)
+    fields = {p["field"] for p in probs}
+    assert set(choice["shapes"]) == fields
+    for shape in choice["shapes"].values():
+        assert shape["chunk_prisms"] in (256, 1024) and shape["points_per_cta"] in (64, 128)
+        assert shape["gain"] > 0
+    assert len(choice["candidates"]) == 4 * len(fields)
+    assert hg.autotune(probs, **kw) == choice  # from the cache
+
+
+def test_every_shape_gives_the_same_results(gpu_lib, oracle):
+    """64 and 128 points per CTA (prism tiles of the same size) and several
+    chunks give the same results, within rounding, as the oracle."""
+    probs = small_set(seed=5, n=10)
+    ref = [oracle.prism_gravity(p["coordinates"], p["prisms"], p["density"], p["field"],
+                                disable_checks=True) for p in probs]
+    for ppc in (64, 128):
+        for chunk in (64, 320, 4096):
+            shapes = {f: {"chunk_prisms": chunk, "points_per_cta": ppc, "n_ctas": 0}
+                      for f in hg.FIELDS}
+            res = hg.prism_gravity_batch(probs, disable_checks=True, shapes=shapes)
+            for r, e in zip(res, ref):
+                npt.assert_allclose(r, e, rtol=1e-8, atol=1e-9 * np.abs(e).max(),
+                                    err_msg=f"{ppc} points per CTA, chunk {chunk}")
 
 
 def test_batched_workload_full_size_against_oracle(gpu_lib, oracle):

@@ -53,10 +53,9 @@ def _skeleton(budget=1e9, max_active=4):
     srv._broken = None
     srv.nominal_rate = 1e10
     srv.max_backlog_s = None
-    srv.rate = 1e10
-    srv.backlog_pairs = 0.0
+    srv.rates = {code: 1e10 for code in range(10)}
+    srv.backlog_s = 0.0
     srv.rejected = 0
-    srv._busy_since = None
     srv.table = (_native.HgProblemPlan * max_active)()
     srv.flags = torch.zeros(max_active, dtype=torch.int32)
     srv.uploads = []
@@ -294,23 +293,31 @@ def test_earliest_virtual_deadline_first_lets_no_request_starve():
 
 
 def test_load_shedding_refuses_requests_beyond_the_backlog_and_counts_them():
+    """Work is priced per field at its measured rate: a request is refused
+    when the backlog plus its own work exceeds max_backlog_s."""
     from harmonica_gb300.serve import ServerOverloaded
 
     srv = _skeleton()
     srv.max_backlog_s = 1.0
-    srv.rate = 1000.0  # pairs/s
-    first = _submit(srv, n_obs=200, n_prisms=3)  # 600 pairs: 0.6 s of work
-    assert srv.backlog_pairs == 600
+    srv.rates[3] = 1000.0  # g_z pairs/s
+    srv.rates[0] = 250.0   # potential: four times the cost per pair
+    first = _submit(srv, n_obs=200, n_prisms=3)  # 600 g_z pairs: 0.6 s of work
+    assert srv.backlog_s == pytest.approx(0.6)
     coords, prisms, density = _problem(n_obs=200, n_prisms=3)
     refused = srv.submit(coords, "g_z", prisms=prisms, density=density)  # 1.2 s > 1 s
     with pytest.raises(ServerOverloaded, match="backlog"):
         refused.result(0)
-    assert srv.rejected == 1 and srv.inbox.empty() and srv.backlog_pairs == 600
-    fits = _submit(srv, n_obs=100, n_prisms=3)  # 0.9 s with the first: accepted
-    assert srv.backlog_pairs == 900
+    assert srv.rejected == 1 and srv.inbox.empty()
+    assert srv.backlog_s == pytest.approx(0.6)
+    coords, prisms, density = _problem(n_obs=40, n_prisms=3)  # 120 pairs of potential: 0.48 s
+    too_costly = srv.submit(coords, "potential", prisms=prisms, density=density)
+    with pytest.raises(ServerOverloaded):
+        too_costly.result(0)
+    fits = _submit(srv, n_obs=100, n_prisms=3)  # 0.3 s of g_z with the first: accepted
+    assert srv.backlog_s == pytest.approx(0.9)
     # a finished or failed request leaves the backlog
     first.set_running_or_notify_cancel()
     first.set_result(np.zeros(200))
-    assert srv.backlog_pairs == 300
-    assert fits.cancel() and srv.backlog_pairs == 0
-    assert srv.stats()["rejected"] == 1
+    assert srv.backlog_s == pytest.approx(0.3)
+    assert fits.cancel() and srv.backlog_s == pytest.approx(0.0)
+    assert srv.stats()["rejected"] == 2
