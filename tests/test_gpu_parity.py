@@ -93,8 +93,11 @@ def test_fused_all_fields_match_single(gpu_lib):
 
 
 def test_many_chunks_and_ragged_sizes(gpu_lib, oracle):
-    """Few points and many prisms (split across CTAs), sizes not multiples of the tiles."""
-    for n_obs, n_prisms in ((1, 1), (3, 129), (7, 5000), (129, 1), (300, 3001)):
+    """Sizes not multiples of the tiles, and the ways the launch splits the
+    work: one point tile over many prism chunks (few points, many prisms),
+    many point tiles and one chunk (many points, few prisms), and both."""
+    for n_obs, n_prisms in ((1, 1), (3, 129), (7, 5000), (129, 1), (300, 3001), (1000, 700),
+                            (2000, 20000), (64, 100000), (20000, 130)):
         coords, prisms, density = random_problem(n_obs + n_prisms, n_prisms, n_obs)
         ref = oracle.prism_gravity(coords, prisms, density, "g_z")
         res = hg.prism_gravity(coords, prisms, density, field="g_z")
