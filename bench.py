@@ -78,17 +78,23 @@ ISSUE_PER_SM_PER_CLOCK = 4  # one warp instruction per clock per SM sub-partitio
 # Kernel sources whose hash keys the ncu counts below.
 KERNEL_SOURCES = ("prism_math.cuh", "lean_math.cuh", "lean_packed.cuh", "lean_tables.inc",
                   "forward_core.cuh", "prism_forward.cu")
-# ncu counts of the layer g_z kernel (forward_kernel<3, LayerSource>) per pair:
-# smsp__inst_executed.sum (warp instructions), sm__sass_thread_inst_executed_op_fp64_pred_on.sum
-# (FP64 thread instructions) and dram__bytes_read.sum + dram__bytes_write.sum per station of
-# a step (the step's kernels read the layer once and write and read the chunk partial sums),
-# from the capture summarised under profiles/, for the kernel sources of `sources_sha`.
+# ncu counts of the layer g_z kernel (forward_kernel<3, LayerSource>): warp instructions
+# (smsp__inst_executed.sum) and FP64 thread instructions
+# (sm__sass_thread_inst_executed_op_fp64_pred_on.sum) per pair, from a capture of a
+# 1000-station step (1e9 pairs per launch, two launches); and the DRAM bytes
+# (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of the default 5000-station
+# step (the step's kernels read the layer once; the chunk partial sums stay mostly in L2).
+# Summarised under profiles/; valid for the kernel sources that hash to `sources_sha`.
 KERNEL_COUNTS = {
-    "sources_sha": None,
-    "warp_inst_per_pair": None,
-    "fp64_inst_per_pair": None,
-    "dram_bytes_per_step_station": None,
-    "capture": None,
+    "sources_sha": "98effa340f59154f",
+    "warp_inst_per_pair": 65.87,
+    "fp64_inst_per_pair": 9.40,
+    "dram_bytes_default_step": None,
+    "default_step_stations": 5000,
+    # the same capture's utilisations (fractions of peak over the active cycles)
+    "ncu_utilisation": {"issue_active": 0.631, "fma_pipe": 0.707, "fmaheavy_pipe": 0.732,
+                        "fmalite_pipe": 0.681, "alu_pipe": 0.347, "fp64_pipe": 0.183},
+    "capture": "profiles/forward_kernel_gz_layer1e6.md",
 }
 
 
@@ -823,7 +829,7 @@ def run_tesseroids(args, rank, world, local):
 # --------------------------------------------------------------------------
 # the headline
 
-def layer_roofline(torch, dev, kernel_pairs_per_s, clocks, stations_per_step):
+def layer_roofline(torch, dev, kernel_pairs_per_s, clocks, stations_per_step, algo_bytes):
     """Roofline of the layer g_z kernel on its binding resource (instruction
     issue), with the algorithmic FP64 figure beside it."""
     peak = fp64_peak(torch)
@@ -857,10 +863,13 @@ def layer_roofline(torch, dev, kernel_pairs_per_s, clocks, stations_per_step):
     }
     if fresh:
         issue_rate = counts["warp_inst_per_pair"] * kernel_pairs_per_s
+        same_step = stations_per_step == counts["default_step_stations"]
         roof.update(achieved=issue_rate / 1e9,
                     frac=issue_rate / issue_peak if issue_peak else None,
                     warp_inst_per_pair=counts["warp_inst_per_pair"],
-                    traffic=counts["dram_bytes_per_step_station"] * stations_per_step,
+                    ncu_utilisation=counts["ncu_utilisation"],
+                    traffic=counts["dram_bytes_default_step"] if same_step else None,
+                    algorithmic_bytes=algo_bytes,
                     fp64={"inst_per_pair": counts["fp64_inst_per_pair"],
                           "pipe_frac": counts["fp64_inst_per_pair"] * kernel_pairs_per_s
                           / (peak * 1e12 / 2.0)})
@@ -1058,7 +1067,11 @@ def main():
             "l2": "flushed between timed steps (256 MB write)",
             "parallelism": f"stations sharded over {world} GPU(s), no collective",
         },
-        "roofline": layer_roofline(torch, dev, kernel_pairs_per_s, clocks, B),
+        # algorithmic bytes of a step: the layer (centres, top, bottom, density)
+        # and the step's stations read once, its results written once
+        "roofline": layer_roofline(torch, dev, kernel_pairs_per_s, clocks, B,
+                                   8 * (layer["easting"].size + layer["northing"].size
+                                        + 3 * n_prisms + 3 * B + B)),
         "cpu_baseline": base,
         "e2e": e2e,
         "served": served,
