@@ -89,7 +89,7 @@ KERNEL_COUNTS = {
     "sources_sha": "98effa340f59154f",
     "warp_inst_per_pair": 65.87,
     "fp64_inst_per_pair": 9.40,
-    "dram_bytes_default_step": None,
+    "dram_bytes_default_step": 43115000,  # 25.39 MB read + 17.73 MB written (two launches)
     "default_step_stations": 5000,
     # the same capture's utilisations (fractions of peak over the active cycles)
     "ncu_utilisation": {"issue_active": 0.631, "fma_pipe": 0.707, "fmaheavy_pipe": 0.732,
@@ -422,13 +422,17 @@ def served_block(args, torch, local):
     for k in range(8):
         srv.register_layer(f"layer{k}", models[k][0], models[k][1])
     coords_of = [synthetic.serving_request_coordinates(r, models[r["model"]][2]) for r in stream]
-    # warm the kernels of the three fields outside the measured stream (small
-    # requests, no shedding)
+    # warm the kernels of the three fields outside the measured stream, with
+    # requests large enough (~1e9 pairs) for each field's rate to be timed
     srv.max_backlog_s = None
-    small = tuple(c[:1000] for c in coords_of[0])
-    warm = [srv.submit(small, f, layer="layer0") for f in ("g_z", "potential", "g_zz")]
-    for f in warm:
-        f.result()
+    big = max(range(8), key=lambda k: models[k][0].shape[0])
+    side = models[big][2]
+    n_warm = int(min(20000, max(1000, 1e9 / models[big][0].shape[0])))
+    rw = np.random.default_rng(99)
+    warm_coords = (rw.uniform(0, side, n_warm), rw.uniform(0, side, n_warm),
+                   rw.uniform(100, 3000, n_warm))
+    for f in ("g_z", "potential", "g_zz"):
+        srv.submit(warm_coords, f, layer=f"layer{big}").result()
     srv.max_backlog_s = args.max_backlog_s
     offered = sum(r["n_stations"] * models[r["model"]][0].shape[0] for r in stream)
     futures = []

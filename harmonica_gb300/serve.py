@@ -55,6 +55,14 @@ from .gravity import _prepare, pack_prisms
 KTHREADS = 128  # points per work item (the kernels' tile)
 
 
+# Cost of a pair of each field relative to g_z, from the layer kernels on
+# GB300 (g_z 1.21e10, potential 3.41e9, g_zz 2.39e10 pairs/s; the other
+# first derivatives cost as g_z, the other tensor components as g_zz): the
+# prior of the per-field rates until each field's launches have been timed.
+FIELD_COST = {"potential": 3.55, "g_e": 1.0, "g_n": 1.0, "g_z": 1.0, "g_ee": 0.5, "g_nn": 0.5,
+              "g_zz": 0.5, "g_en": 0.5, "g_ez": 0.5, "g_nz": 0.5}
+
+
 class ServerOverloaded(RuntimeError):
     """A request refused at submission because the server's backlog would
     exceed its ``max_backlog_s``."""
@@ -133,9 +141,10 @@ class PrismServer:
     chunk : int
         Largest prism chunk of a work item.
     nominal_rate : float
-        Pairs per second used for the virtual deadlines of the scheduling
-        order and as the first estimate of every field's rate for load
-        shedding (then replaced by each field's measured rate).
+        g_z pairs per second; with the relative costs of ``FIELD_COST`` it
+        gives the work of a request for the virtual deadlines of the
+        scheduling order and the first estimate of each field's rate for
+        load shedding (then replaced by the field's measured rate).
     max_backlog_s : float or None
         Refuse new requests (:class:`ServerOverloaded`) while the unfinished
         work, the new request's included, exceeds this many seconds at the
@@ -162,7 +171,8 @@ class PrismServer:
         self.nominal_rate = float(nominal_rate)
         self.max_backlog_s = None if max_backlog_s is None else float(max_backlog_s)
         # measured pairs/s of each field's launches (field code -> rate)
-        self.rates = {code: float(nominal_rate) for code in FIELD_CODES.values()}
+        self.rates = {code: float(nominal_rate) / FIELD_COST[name]
+                      for name, code in FIELD_CODES.items()}
         self.backlog_s = 0.0  # estimated seconds of accepted, unfinished work
         self.rejected = 0
         self.layers = collections.OrderedDict()
@@ -265,7 +275,7 @@ class PrismServer:
             known = self.layers.get(layer) if layer is not None else None
             n_prisms = known.n_prisms if known is not None else (req.n_prisms or 0)
             req.pairs = float(req.n_obs) * float(n_prisms)
-            req.deadline = req.t_submit + req.pairs / self.nominal_rate
+            req.deadline = req.t_submit + req.pairs * FIELD_COST[field] / self.nominal_rate
             req.cost_s = req.pairs / self.rates[FIELD_CODES[field]]
             if (self.max_backlog_s is not None and self.backlog_s > 0
                     and self.backlog_s + req.cost_s > self.max_backlog_s):
