@@ -94,7 +94,8 @@ KERNEL_COUNTS = {
     # the same capture's utilisations (fractions of peak over the active cycles)
     "ncu_utilisation": {"issue_active": 0.631, "fma_pipe": 0.707, "fmaheavy_pipe": 0.732,
                         "fmalite_pipe": 0.681, "alu_pipe": 0.347, "fp64_pipe": 0.183},
-    "capture": "profiles/forward_kernel_gz_layer1e6.md",
+    "capture": "ncu on GB300: per-pair counts from two launches of a 1000-station step, "
+               "DRAM bytes from two launches of the default step (1-pass metrics)",
 }
 
 

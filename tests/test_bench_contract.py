@@ -46,4 +46,4 @@ def test_kernel_counts_match_the_kernel_sources():
     if counts["sources_sha"] is not None:
         for key in ("warp_inst_per_pair", "fp64_inst_per_pair", "capture"):
             assert counts[key] is not None, key
-        assert os.path.exists(os.path.join(ROOT, counts["capture"]))
+        assert counts["dram_bytes_default_step"] > 0
