@@ -164,14 +164,39 @@ __device__ __forceinline__ void accumulate(const Source& src, int64_t p0, int64_
       }
       if (sh.null[p]) continue;  // uniform across the CTA
       const double rho = sh.rho[p];
-      if (F == kAll) {
-        double v[kNumFields];
-        pair_all<true>(q, T, v);
+      if (F == kAll || F == kPotential) {
+        // The float-pair form needs only the float-pair geometry: the FP64
+        // bounds are dead after make_geom_f2 (fewer live registers through
+        // the long evaluation) and are rebuilt from shared memory for the
+        // rare pair it declines (a zero or tiny bound), which is also the
+        // only kind of pair that can lie on a singular point.
+        constexpr bool ALL = F == kAll;
+        double v[ALL ? kNumFields : 1];
+        GeomF2 g;
+        const bool fast = !any_zero_bound(q) && make_geom_f2(q, g);
+        if (!(fast && pair_all_f2_geom<ALL>(g, T, v))) {
+          const volatile double* vs = &sh.w[p];  // forces the reload (no reuse of q)
+          Rel r;
+          r.x1 = vs[0] - pe;
+          r.x2 = sh.e[p] - pe;
+          r.y1 = sh.s[p] - pn;
+          r.y2 = sh.n[p] - pn;
+          r.z1 = sh.b[p] - pu;
+          r.z2 = sh.t[p] - pu;
+          r.dx = sh.dx[p];
+          r.dy = sh.dy[p];
+          r.dz = sh.dz[p];
+          if (ALL) {
+            pair_all_fp64(r, T, v);
 #pragma unroll
-        for (int f = 0; f < kNumFields; f++) {
-          if (is_tensor(f) && singular_for(f, q)) v[f] = quiet_nan();
-          acc[f] = fma(rho, v[f], acc[f]);
+            for (int f = kGee; f <= kGnz; f++)
+              if (singular_for(f, r)) v[ALL ? f : 0] = quiet_nan();
+          } else {
+            v[0] = pair_field_fp64<kPotential>(r, T);
+          }
         }
+#pragma unroll
+        for (int f = 0; f < (ALL ? kNumFields : 1); f++) acc[f] = fma(rho, v[f], acc[f]);
       } else {
         double v = pair_field<(F < kNumFields ? F : 0), true>(q, T);
         if (is_tensor(F) && singular_for(F, q)) v = quiet_nan();

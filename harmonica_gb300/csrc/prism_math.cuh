@@ -949,10 +949,34 @@ HG_HD __forceinline__ lean::P2 face_core_p2(lean::P2 fa, lean::P2 fb1, lean::P2 
 // from their inputs: bounds along the normal (fa, ad), along the in-plane
 // axes b and c (fb, bd, fc, cd), vertex distances fr[k][bi][ci] and the b
 // width.  false: a coordinate is too small for the face's scale (FP64 path).
+HG_HD __forceinline__ bool face_pair_core_p2(const lean::F2 fa[2], const lean::F2 fb[2],
+                                             const lean::F2 fc[2], const lean::F2 fr[2][2][2],
+                                             lean::F2 fw, bool same_sign, const Tables& T,
+                                             lean::P2& o);
+
 HG_HD __forceinline__ bool face_pair_p2(const lean::F2 fa[2], const lean::F2 fb[2],
                                         const lean::F2 fc[2], const lean::F2 fr[2][2][2],
                                         lean::F2 fw, const double ad[2], const double bd[2],
                                         const double cd[2], const Tables& T, lean::P2& o) {
+  using namespace lean;
+  const bool same_sign = !(neg_not_tiny(bd[0]) && !nonpos_or_tiny(bd[1]));
+  if (!face_pair_core_p2(fa, fb, fc, fr, fw, same_sign, T, o)) return false;
+  // a point in a face plane: that face's outside limit
+  if (is_tiny(ad[0]) || is_tiny(ad[1])) {
+    F2 o0 = lane0(o), o1 = lane1(o);
+    if (is_tiny(ad[0])) o0 = face_limit_f2(bd[0], bd[1], cd[0], cd[1], false);
+    if (is_tiny(ad[1])) o1 = face_limit_f2(bd[0], bd[1], cd[0], cd[1], true);
+    o = pk(o0, o1);
+  }
+  return true;
+}
+
+// The two faces from float-pair inputs alone (same_sign: the b bounds have
+// one sign); false when a coordinate is too small for the face's scale.
+HG_HD __forceinline__ bool face_pair_core_p2(const lean::F2 fa[2], const lean::F2 fb[2],
+                                             const lean::F2 fc[2], const lean::F2 fr[2][2][2],
+                                             lean::F2 fw, bool same_sign, const Tables& T,
+                                             lean::P2& o) {
   using namespace lean;
   const auto fe = [](F2 a) { return (int)((f2u(a.h) >> 23) & 0xffu); };
   int ftop[2];
@@ -969,7 +993,6 @@ HG_HD __forceinline__ bool face_pair_p2(const lean::F2 fa[2], const lean::F2 fb[
   const auto both = [&](F2 a) { return p2_scale(pk(a, a), sc); };
   const auto per = [&](F2 a0, F2 a1) { return p2_scale(pk(a0, a1), sc); };
   const bool n0 = fa[0].h < 0.0f, n1 = fa[1].h < 0.0f;
-  const bool same_sign = !(neg_not_tiny(bd[0]) && !nonpos_or_tiny(bd[1]));
   o = face_core_p2(per(n0 ? f2_neg(fa[0]) : fa[0], n1 ? f2_neg(fa[1]) : fa[1]), both(fb[0]),
                    both(fb[1]), both(fc[0]), both(fc[1]), per(fr[0][0][0], fr[1][0][0]),
                    per(fr[0][0][1], fr[1][0][1]), per(fr[0][1][0], fr[1][1][0]),
@@ -977,11 +1000,6 @@ HG_HD __forceinline__ bool face_pair_p2(const lean::F2 fa[2], const lean::F2 fb[
   F2 o0 = lane0(o), o1 = lane1(o);
   if (n0) o0 = f2_neg(o0);
   if (n1) o1 = f2_neg(o1);
-  // a point in a face plane: that face's outside limit
-  if (is_tiny(ad[0]) || is_tiny(ad[1])) {
-    if (is_tiny(ad[0])) o0 = face_limit_f2(bd[0], bd[1], cd[0], cd[1], false);
-    if (is_tiny(ad[1])) o1 = face_limit_f2(bd[0], bd[1], cd[0], cd[1], true);
-  }
   o = pk(o0, o1);
   return true;
 }
@@ -1249,13 +1267,18 @@ HG_HD __forceinline__ lean::F2 extent_f2(const GeomF2& g, int a) {
 HG_HD __forceinline__ lean::F2 f2_sel(bool c, lean::F2 a, lean::F2 b) { return c ? a : b; }
 
 // The logs of edge family `fam` (= its axis A): MQ_0, MQ_1, MP_0, L_00.
-HG_HD __forceinline__ void family_logs(const Rel& q, const GeomF2& g, int fam, const Tables& T,
+// (The bounds are all nonzero here, so the case of the family's axis follows
+// from the signs of the float-pair bounds: reflect when the upper bound is
+// negative, straddle when the lower one is negative and the upper positive.)
+HG_HD __forceinline__ void family_logs(const GeomF2& g, int fam, const Tables& T,
                                        lean::F2& mq0, lean::F2& mq1, lean::F2& mp0,
                                        lean::F2& l00) {
   using namespace lean;
   const int P = fam == 0 ? 1 : 0, Q = fam == 2 ? 1 : 2;
-  const AxisCase c = axis_case(rel_bound(q, fam, 0), rel_bound(q, fam, 1));
   const F2 a0 = bound_f2(g, fam, 0), a1 = bound_f2(g, fam, 1);
+  AxisCase c;
+  c.reflect = a1.h < 0.0f;
+  c.straddle = !c.reflect && a0.h < 0.0f;
   const F2 lo = c.reflect ? f2_neg(a1) : a0, hi = c.reflect ? f2_neg(a0) : a1;
   // vertex distance at A-end e, P bound p, Q bound q (family layout)
   const auto R = [&](int e, int p, int qq) {
@@ -1288,9 +1311,10 @@ HG_HD __forceinline__ void family_logs(const Rel& q, const GeomF2& g, int fam, c
   l00 = lane1(ml);
 }
 
-// The two faces normal to `axis` as float pairs (lanes: lower, upper bound).
-HG_HD __forceinline__ bool face_pair_f2(const Rel& q, const GeomF2& g, int axis,
-                                        const Tables& T, lean::F2& o0, lean::F2& o1) {
+// The two faces normal to `axis` as float pairs (lanes: lower, upper bound),
+// for a pair with no zero bound (no face-plane limit to take).
+HG_HD __forceinline__ bool face_pair_f2(const GeomF2& g, int axis, const Tables& T,
+                                        lean::F2& o0, lean::F2& o1) {
   using namespace lean;
   const bool X = axis == 0, Y = axis == 1;
   F2 fr[2][2][2];
@@ -1305,11 +1329,9 @@ HG_HD __forceinline__ bool face_pair_f2(const Rel& q, const GeomF2& g, int axis,
   const F2 fb[2] = {X ? g.c[1][0] : g.c[0][0], X ? g.c[1][1] : g.c[0][1]};
   const F2 fc[2] = {(X || Y) ? g.c[2][0] : g.c[1][0], (X || Y) ? g.c[2][1] : g.c[1][1]};
   const F2 fw = X ? g.d[1] : g.d[0];
-  const double ad[2] = {rel_bound(q, axis, 0), rel_bound(q, axis, 1)};
-  const double bd[2] = {X ? q.y1 : q.x1, X ? q.y2 : q.x2};
-  const double cd[2] = {(X || Y) ? q.z1 : q.y1, (X || Y) ? q.z2 : q.y2};
   P2 o;
-  if (!face_pair_p2(fa, fb, fc, fr, fw, ad, bd, cd, T, o)) return false;
+  if (!face_pair_core_p2(fa, fb, fc, fr, fw, !(fb[0].h < 0.0f && fb[1].h > 0.0f), T, o))
+    return false;
   o0 = lane0(o);
   o1 = lane1(o);
   return true;
@@ -1320,20 +1342,30 @@ HG_HD __forceinline__ bool face_pair_f2(const Rel& q, const GeomF2& g, int axis,
 // (the point lies in a face plane or on an edge line, where the identities
 // above would add infinite logs with cancelling coefficients), or the
 // geometry leaves the float range; the caller takes the FP64 geometry.
+HG_HD __forceinline__ bool any_zero_bound(const Rel& q) {
+  return is_tiny(q.x1) || is_tiny(q.x2) || is_tiny(q.y1) || is_tiny(q.y2) || is_tiny(q.z1) ||
+         is_tiny(q.z2);
+}
+
+// pair_all_f2 on a geometry with no zero bound, already on float pairs.
+template <bool ALL>
+HG_HD __forceinline__ bool pair_all_f2_geom(const GeomF2& g, const Tables& T, double* out);
+
 template <bool ALL>
 HG_HD __forceinline__ bool pair_all_f2(const Rel& q, const Tables& T, double* out) {
-  using namespace lean;
-  if (is_tiny(q.x1) || is_tiny(q.x2) || is_tiny(q.y1) || is_tiny(q.y2) || is_tiny(q.z1) ||
-      is_tiny(q.z2))
-    return false;
   GeomF2 g;
-  if (!make_geom_f2(q, g)) return false;
+  return !any_zero_bound(q) && make_geom_f2(q, g) && pair_all_f2_geom<ALL>(g, T, out);
+}
+
+template <bool ALL>
+HG_HD __forceinline__ bool pair_all_f2_geom(const GeomF2& g, const Tables& T, double* out) {
+  using namespace lean;
   const F2 zero{0.0f, 0.0f};
   F2 pot = zero, ge = zero, gn = zero, gz = zero, Dx = zero, Dy = zero, Dz = zero;
 #pragma unroll 1
   for (int fam = 0; fam < 3; fam++) {
     F2 mq0, mq1, mp0, l00;
-    family_logs(q, g, fam, T, mq0, mq1, mp0, l00);
+    family_logs(g, fam, T, mq0, mq1, mp0, l00);
     const int P = fam == 0 ? 1 : 0, Q = fam == 2 ? 1 : 2;
     const F2 p1 = bound_f2(g, P, 1), q1 = bound_f2(g, Q, 1);
     const F2 dP = extent_f2(g, P), dQ = extent_f2(g, Q);
@@ -1357,7 +1389,7 @@ HG_HD __forceinline__ bool pair_all_f2(const Rel& q, const Tables& T, double* ou
 #pragma unroll 1
   for (int axis = 0; axis < 3; axis++) {
     F2 o0, o1;
-    if (!face_pair_f2(q, g, axis, T, o0, o1)) return false;
+    if (!face_pair_f2(g, axis, T, o0, o1)) return false;
     const F2 u0 = bound_f2(g, axis, 0), du = extent_f2(g, axis);
     const F2 dO = f2_sub(o0, o1);
     faces2 = f2_add(faces2, f2_sub(f2_mul(f2_sq(u0), dO),
