@@ -262,6 +262,12 @@ HG_HD __forceinline__ F2 f2_add(F2 a, F2 b) {
   const F2 s = two_sum(a.h, b.h);
   return quick_two_sum(s.h, fadd(s.l, fadd(a.l, b.l)));
 }
+// a + b for |a.h| >= |b.h| (or within a rounding of each other): Fast2Sum
+// on the high parts (p2_add_big lane by lane)
+HG_HD __forceinline__ F2 f2_add_big(F2 a, F2 b) {
+  const F2 s = quick_two_sum(a.h, b.h);
+  return quick_two_sum(s.h, fadd(s.l, fadd(a.l, b.l)));
+}
 HG_HD __forceinline__ F2 f2_neg(F2 a) { return F2{-a.h, -a.l}; }
 HG_HD __forceinline__ F2 f2_sub(F2 a, F2 b) { return f2_add(a, f2_neg(b)); }
 HG_HD __forceinline__ F2 f2_sq(F2 a) {

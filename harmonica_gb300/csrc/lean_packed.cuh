@@ -72,6 +72,13 @@ HG_HD __forceinline__ P2 p2_add(P2 a, P2 b) {
   const P2 s = two_sum2(a.h, b.h);
   return quick_two_sum2(s.h, add2(s.l, add2(a.l, b.l)));
 }
+// a + b when |a.h| >= |b.h| (or the two are within a rounding of each
+// other): the high parts' rounding error by Fast2Sum instead of TwoSum, 3 of
+// 11 FP32 operations fewer, same result.
+HG_HD __forceinline__ P2 p2_add_big(P2 a, P2 b) {
+  const P2 s = quick_two_sum2(a.h, b.h);
+  return quick_two_sum2(s.h, add2(s.l, add2(a.l, b.l)));
+}
 HG_HD __forceinline__ P2 p2_neg(P2 a) { return P2{neg2(a.h), neg2(a.l)}; }
 HG_HD __forceinline__ P2 p2_sub(P2 a, P2 b) { return p2_add(a, p2_neg(b)); }
 HG_HD __forceinline__ P2 p2_sq(P2 a) {
@@ -152,6 +159,7 @@ HG_HD __forceinline__ P2 log1p_series_p2(P2 t) {
 // ln(1 + t) lane-wise (log1p_f2), always through the table reduction: near
 // 1 it selects c = 1, E = 0, so the reduced argument is t itself.
 HG_HD __forceinline__ P2 log1p_p2(P2 t, const Tables& T) {
+  if (fabsf(t.h.x) < 0.0026f && fabsf(t.h.y) < 0.0026f) return log1p_series_p2(t);
   const P2 w = p2_add(P2{sp2(1.0f), sp2(0.0f)}, t);
   const auto plan = [&](float wh, float& cp, int& k, float& ef) {
     const unsigned uw = f2u(wh);
@@ -230,8 +238,12 @@ HG_HD __forceinline__ P2 arg_near_p2(P2 pr, P2 pi, float est0, float est1, const
     if (!ok0) j0 = 0;
     if (!ok1) j1 = 0;
   }
-  const int ka = 2 * (j0 + kArgTableHalf), kb = 2 * (j1 + kArgTableHalf);
-  a = p2_add(a, P2{mk2(T.thf[ka], T.thf[kb]), mk2(T.thf[ka + 1], T.thf[kb + 1])});
+  if (j0 != 0 || j1 != 0) {  // th_j (th_0 = 0: only the renormalisation)
+    const int ka = 2 * (j0 + kArgTableHalf), kb = 2 * (j1 + kArgTableHalf);
+    a = p2_add(a, P2{mk2(T.thf[ka], T.thf[kb]), mk2(T.thf[ka + 1], T.thf[kb + 1])});
+  } else {
+    a = quick_two_sum2(a.h, a.l);
+  }
   if (q0 != 0 || q1 != 0) {  // q pi/2 with pi/2 in three floats (q * F1 exact)
     const float2 qf = mk2((float)q0, (float)q1);
     P2 p = two_prod2(qf, sp2(kPio2F2));

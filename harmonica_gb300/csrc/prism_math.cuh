@@ -1077,10 +1077,12 @@ HG_HD __forceinline__ lean::P2 merged_t_p2(bool straddle, lean::P2 lo, lean::P2 
   const P2 Sl = p2_add(rl0, rl1), Sh = p2_add(rh0, rh1);
   const P2 Dl = p2_div(dQ, Sl), Dh = p2_div(dQ, Sh);
   if (!straddle) {
-    const P2 D0 = p2_add(lo, rl0), D1 = p2_add(lo, rl1), N0 = p2_add(hi, rh0);
-    const P2 P0 = p2_add(rl0, rh0), P1 = p2_add(rl1, rh1);
-    const P2 inner = p2_add(p2_mul(D0, p2_add(Dl, Dh)), p2_mul(Dl, P1));
-    const P2 br = p2_add(Dl, p2_div(p2_mul(p2_add(hi, lo), inner), p2_mul(P0, P1)));
+    // 0 <= lo <= hi, so r_lo >= lo, r_hi >= hi, r_hi >= r_lo and |Dl| >= |Dh|
+    // (one sign): those sums take the ordered addition
+    const P2 D0 = p2_add_big(rl0, lo), D1 = p2_add_big(rl1, lo), N0 = p2_add_big(rh0, hi);
+    const P2 P0 = p2_add_big(rh0, rl0), P1 = p2_add_big(rh1, rl1);
+    const P2 inner = p2_add(p2_mul(D0, p2_add_big(Dl, Dh)), p2_mul(Dl, P1));
+    const P2 br = p2_add(Dl, p2_div(p2_mul(p2_add_big(hi, lo), inner), p2_mul(P0, P1)));
     return p2_neg(p2_div(p2_mul(dA, br), p2_mul(D1, N0)));
   }
   const P2 M0 = p2_sub(rl0, lo), M1 = p2_sub(rl1, lo);
@@ -1246,8 +1248,9 @@ HG_HD __forceinline__ lean::F2 single_t(bool straddle, lean::F2 lo, lean::F2 hi,
                                         lean::F2 rh, lean::F2 dA, lean::F2 rho2) {
   using namespace lean;
   if (!straddle) {
-    const F2 S = f2_add(rh, rl);
-    return f2_div(f2_mul(dA, f2_add(S, f2_add(hi, lo))), f2_mul(S, f2_add(lo, rl)));
+    // 0 <= lo <= hi: r_hi >= r_lo >= lo, S >= hi + lo (ordered additions)
+    const F2 S = f2_add_big(rh, rl);
+    return f2_div(f2_mul(dA, f2_add_big(S, f2_add_big(hi, lo))), f2_mul(S, f2_add_big(rl, lo)));
   }
   const F2 m = f2_neg(lo);
   const F2 h2 = f2_sq(hi), m2 = f2_sq(m);
