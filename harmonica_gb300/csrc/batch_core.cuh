@@ -60,7 +60,7 @@ __device__ __forceinline__ void run_item(const ProblemDev& P, const WorkItem& w,
 // tile, and as many resident CTAs per SM as the 128-point kernel times
 // 128 / THREADS (the same registers per thread).
 template <int F, int THREADS>
-__global__ void __launch_bounds__(THREADS, MinBlocks<F>::value * (kThreads / THREADS))
+__global__ void __launch_bounds__(THREADS, BatchMinBlocks<F>::value * (kThreads / THREADS))
     batch_kernel(const ProblemDev* __restrict__ probs, const WorkItem* __restrict__ items,
                  int64_t n_items, unsigned long long* __restrict__ counter,
                  double* __restrict__ part) {

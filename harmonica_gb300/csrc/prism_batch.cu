@@ -303,7 +303,7 @@ __device__ __forceinline__ void run_plan_item(const hg_problem_plan& P, const hg
 
 // Persistent kernel over the work items of one field F in a round.
 template <int F>
-__global__ void __launch_bounds__(kThreads, MinBlocks<F>::value)
+__global__ void __launch_bounds__(kThreads, BatchMinBlocks<F>::value)
     round_kernel(const hg_problem_plan* __restrict__ probs, const hg_work_item* __restrict__ items,
                  int64_t n_items, unsigned long long* __restrict__ counter) {
   __shared__ SmemTile sh;
