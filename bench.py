@@ -83,17 +83,18 @@ KERNEL_SOURCES = ("prism_math.cuh", "lean_math.cuh", "lean_packed.cuh", "lean_ta
 # (sm__sass_thread_inst_executed_op_fp64_pred_on.sum) per pair, from a capture of a
 # 1000-station step (1e9 pairs per launch, two launches); and the DRAM bytes
 # (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of the default 5000-station
-# step (the step's kernels read the layer once; the chunk partial sums stay mostly in L2).
+# step (the layer is read once; the writes are the kernel's register spills, written back
+# from L2 at ~1.5 GB/s, and the chunk partial sums).
 # Summarised under profiles/; valid for the kernel sources that hash to `sources_sha`.
 KERNEL_COUNTS = {
-    "sources_sha": "98effa340f59154f",
-    "warp_inst_per_pair": 65.87,
+    "sources_sha": "c5b04bd8517f9e0b",
+    "warp_inst_per_pair": 57.31,
     "fp64_inst_per_pair": 9.40,
-    "dram_bytes_default_step": 43115000,  # 25.39 MB read + 17.73 MB written (two launches)
+    "dram_bytes_default_step": 540357000,  # 26.01 MB read + 514.35 MB written (two launches)
     "default_step_stations": 5000,
     # the same capture's utilisations (fractions of peak over the active cycles)
-    "ncu_utilisation": {"issue_active": 0.631, "fma_pipe": 0.707, "fmaheavy_pipe": 0.732,
-                        "fmalite_pipe": 0.681, "alu_pipe": 0.347, "fp64_pipe": 0.183},
+    "ncu_utilisation": {"issue_active": 0.647, "fma_pipe": 0.684, "fmaheavy_pipe": 0.706,
+                        "fmalite_pipe": 0.662, "alu_pipe": 0.367, "fp64_pipe": 0.215},
     "capture": "ncu on GB300: per-pair counts from two launches of a 1000-station step, "
                "DRAM bytes from two launches of the default step (1-pass metrics)",
 }
@@ -125,6 +126,10 @@ def parse_args():
     p.add_argument("--rate", type=float, default=200.0)
     p.add_argument("--max-backlog-s", type=float, default=2.0)
     p.add_argument("--plain-sample-seconds", type=float, default=8.0)
+    p.add_argument("--serve-round-pairs", type=float, default=None,
+                   help="served block: point-prism pairs per round (PrismServer default if unset)")
+    p.add_argument("--serve-chunk", type=int, default=None,
+                   help="served block: largest prism chunk of a work item (default if unset)")
     return p.parse_args()
 
 
@@ -419,7 +424,13 @@ def served_block(args, torch, local):
 
     models = synthetic.serving_models()
     stream = synthetic.serving_stream(rate=args.rate, seconds=args.arrival_seconds)
-    srv = PrismServer(memory_budget=120e9, max_active=4096, max_backlog_s=args.max_backlog_s)
+    shape = {}
+    if args.serve_round_pairs is not None:
+        shape["round_pairs"] = args.serve_round_pairs
+    if args.serve_chunk is not None:
+        shape["chunk"] = args.serve_chunk
+    srv = PrismServer(memory_budget=120e9, max_active=4096, max_backlog_s=args.max_backlog_s,
+                      **shape)
     for k in range(8):
         srv.register_layer(f"layer{k}", models[k][0], models[k][1])
     coords_of = [synthetic.serving_request_coordinates(r, models[r["model"]][2]) for r in stream]
@@ -497,6 +508,7 @@ def served_block(args, torch, local):
         "latency_over": "every accepted request (all finished); refused requests are answered "
                         "at once with ServerOverloaded",
         "measured_seconds": elapsed, "rounds": st["rounds"],
+        "round_pairs": srv.round_pairs, "chunk": srv.max_chunk,
         "accepted_fields": fields,
         "plain": {"value": plain_rate, "unit": "pairs/s", "requests": n_plain,
                   "path": "harmonica_gb300.prism_gravity once per request, numpy inputs, the "

@@ -135,11 +135,18 @@ class PrismServer:
         Device bytes the server may hold for admitted requests and resident
         layers (admission stops when the next request would not fit).
     round_pairs : float
-        Target point-prism pairs per round (a round is one persistent launch).
+        Target point-prism pairs per round (a round is one persistent launch
+        per field).
     max_active : int
         Size of the device problem table (admitted requests at once).
     chunk : int
-        Largest prism chunk of a work item.
+        Largest prism chunk of a work item.  A work item (128 points x the
+        chunk) runs on one CTA, so the last items of a launch leave SMs idle
+        for up to one item's time: the defaults (1.6e9-pair rounds of
+        128 x 512 items) keep each field's launch many items deep.  Measured
+        on the served stream of a GB300 (Poisson 200 req/s, g_z / potential /
+        g_zz): 4e8-pair rounds of 2048-prism items 7.5e9 pairs/s; 4e8 and 512
+        1.13e10; 1.6e9 and 2048 1.17e10; 1.6e9 and 512 1.24e10.
     nominal_rate : float
         g_z pairs per second; with the relative costs of ``FIELD_COST`` it
         gives the work of a request for the virtual deadlines of the
@@ -151,8 +158,8 @@ class PrismServer:
         measured rates; ``None`` accepts everything.
     """
 
-    def __init__(self, device=None, memory_budget=120e9, round_pairs=4e8, max_active=1024,
-                 chunk=2048, n_ctas=0, rounds_in_flight=2, nominal_rate=1e10,
+    def __init__(self, device=None, memory_budget=120e9, round_pairs=1.6e9, max_active=1024,
+                 chunk=512, n_ctas=0, rounds_in_flight=2, nominal_rate=1e10,
                  max_backlog_s=None):
         import torch
 

@@ -29,7 +29,7 @@ def _requests(seed, n, scale=0.01):
 
 def test_results_match_drop_in(gpu_lib):
     probs = _requests(20, 9)
-    # 5.4e5 pairs in all, one work item of 1.5e5: at least four rounds
+    # 5.4e5 pairs in all, work items of at most 128 x 512 pairs: many rounds
     srv = PrismServer(round_pairs=1e5)
     futs = [srv.submit(p["coordinates"], p["field"], prisms=p["prisms"], density=p["density"])
             for p in probs]
