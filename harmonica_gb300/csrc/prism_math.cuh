@@ -1212,8 +1212,8 @@ HG_HD __forceinline__ bool pair_diag_p2(const Rel& q, const Tables& T, double& o
 // P and q of Q, P < Q in (x, y, z) order: A = x: (y, z); A = y: (x, z);
 // A = z: (x, y)) enter every field only through
 //   MQ_p = L_p1 - L_p0   (merged along Q at P = p, merged_t),
-//   MP_0 = L_10 - L_00   (merged along P at the lower Q bound),
-//   L_00                 (one edge log, single_t),
+//   MP_0 = L_10 - L_00   (along P at the lower Q bound),
+//   L_00                 (one edge log, single_t_p2),
 //   D    = MQ_1 - MQ_0   (= L_11 - L_10 - L_01 + L_00, the off-diagonal
 //                         tensor combination of the family),
 // since L_10 = L_00 + MP_0, L_01 = L_00 + MQ_0 and L_11 = L_10 + MQ_1:
@@ -1233,6 +1233,15 @@ HG_HD __forceinline__ bool pair_diag_p2(const Rel& q, const Tables& T, double& o
 //   g_en, g_ez, g_nz = D of the z, y, x families,
 // with E the first sum above, QT and PT the second and third, F the first
 // face identity (u the axis' coordinate).
+//
+// D multiplies P_1 Q_1 (of the order of the squared distance), so it needs
+// the merged logs MQ_p: their difference keeps the relative accuracy of a
+// first difference.  MP_0 multiplies P_1 dQ or dQ alone, so it is taken as
+// the difference of the two single logs L_10 - L_00 (one packed single_t_p2
+// for both): its rounding, ~2^-44 |L_00|, enters E as ~2^-44 |P_1| dQ |L_00|
+// against |E| ~ dP dQ |L_00|, i.e. a relative error of ~2^-44 |P_1| / dP --
+// 6e-10 at 1e4 prism widths, where the reference's own FP64 sum has lost
+// ~1e-8 -- for one single log in place of a merged one.
 
 // t = R - 1 of one edge log ln R, R = (hi + r_hi) / (lo + r_lo) for an edge
 // beyond the point (lo >= 0 after reflection), or (hi + r_hi)(r_lo - lo) / rho2
@@ -1244,20 +1253,23 @@ HG_HD __forceinline__ bool pair_diag_p2(const Rel& q, const Tables& T, double& o
 //   lo < 0:  t = [hi r_lo + hi m + r_hi m + (hi^2 m^2 + rho2 (hi^2 + m^2))
 //                 / (r_hi r_lo + rho2)] / rho2
 // so t keeps its relative accuracy however far the edge is.
-HG_HD __forceinline__ lean::F2 single_t(bool straddle, lean::F2 lo, lean::F2 hi, lean::F2 rl,
-                                        lean::F2 rh, lean::F2 dA, lean::F2 rho2) {
+//
+// Evaluated for the two edges of one family at P bounds 0 and 1 (lanes), at
+// the same Q bound: same edge extent and case, own vertex distances and rho2.
+HG_HD __forceinline__ lean::P2 single_t_p2(bool straddle, lean::P2 lo, lean::P2 hi, lean::P2 rl,
+                                           lean::P2 rh, lean::P2 dA, lean::P2 rho2) {
   using namespace lean;
   if (!straddle) {
     // 0 <= lo <= hi: r_hi >= r_lo >= lo, S >= hi + lo (ordered additions)
-    const F2 S = f2_add_big(rh, rl);
-    return f2_div(f2_mul(dA, f2_add_big(S, f2_add_big(hi, lo))), f2_mul(S, f2_add_big(rl, lo)));
+    const P2 S = p2_add_big(rh, rl);
+    return p2_div(p2_mul(dA, p2_add_big(S, p2_add_big(hi, lo))), p2_mul(S, p2_add_big(rl, lo)));
   }
-  const F2 m = f2_neg(lo);
-  const F2 h2 = f2_sq(hi), m2 = f2_sq(m);
-  const F2 x = f2_div(f2_add(f2_mul(h2, m2), f2_mul(rho2, f2_add(h2, m2))),
-                      f2_add(f2_mul(rh, rl), rho2));
-  const F2 num = f2_add(f2_add(f2_mul(hi, rl), f2_mul(hi, m)), f2_add(f2_mul(rh, m), x));
-  return f2_div(num, rho2);
+  const P2 m = p2_neg(lo);
+  const P2 h2 = p2_sq(hi), m2 = p2_sq(m);
+  const P2 x = p2_div(p2_add(p2_mul(h2, m2), p2_mul(rho2, p2_add(h2, m2))),
+                      p2_add(p2_mul(rh, rl), rho2));
+  const P2 num = p2_add(p2_add(p2_mul(hi, rl), p2_mul(hi, m)), p2_add(p2_mul(rh, m), x));
+  return p2_div(num, rho2);
 }
 
 // Float-pair bound k of axis a (a at run time, k a constant: selects only).
@@ -1299,19 +1311,17 @@ HG_HD __forceinline__ void family_logs(const GeomF2& g, int fam, const Tables& T
                             pk(RL(0, 0), RL(1, 0)), pk(RL(0, 1), RL(1, 1)),
                             pk(RH(0, 0), RH(1, 0)), pk(RH(0, 1), RH(1, 1)), bc(dA), bc(dQ),
                             bc(f2_add(q0, q1)));
-  // merged along P, lane Q = 0; lane 1 carries the single log L_00 instead
-  const P2 tp = merged_t_p2(c.straddle, bc(lo), bc(hi), pk(q0, q1), bc(p1),
-                            pk(RL(0, 0), RL(0, 1)), pk(RL(1, 0), RL(1, 1)),
-                            pk(RH(0, 0), RH(0, 1)), pk(RH(1, 0), RH(1, 1)), bc(dA), bc(dP),
-                            bc(f2_add(p0, p1)));
-  const F2 tl = single_t(c.straddle, lo, hi, RL(0, 0), RH(0, 0), dA,
-                         f2_add(f2_sq(p0), f2_sq(q0)));
+  (void)dP;
+  const P2 q0b = bc(q0);
+  const P2 ts = single_t_p2(c.straddle, bc(lo), bc(hi), pk(RL(0, 0), RL(1, 0)),
+                            pk(RH(0, 0), RH(1, 0)), bc(dA),
+                            p2_add(p2_sq(pk(p0, p1)), p2_sq(q0b)));
   const P2 mq = log1p_p2(tq, T);
-  const P2 ml = log1p_p2(pk(lane0(tp), tl), T);
+  const P2 ml = log1p_p2(ts, T);
   mq0 = lane0(mq);
   mq1 = lane1(mq);
-  mp0 = lane0(ml);
-  l00 = lane1(ml);
+  l00 = lane0(ml);
+  mp0 = f2_sub(lane1(ml), l00);
 }
 
 // The two faces normal to `axis` as float pairs (lanes: lower, upper bound),

@@ -89,3 +89,36 @@ def test_empty_request_and_unknown_layer(gpu_lib):
     with pytest.raises(KeyError):
         srv.submit((np.zeros(3), np.zeros(3), np.ones(3)), "g_z", layer="nope").result(60)
     srv.close()
+
+
+def test_serving_stream_with_full_size_models(gpu_lib, oracle):
+    """The first 12 requests of the serving workload with their full prism
+    models (1e3-1e6 prisms; the resident share served from registered
+    layers), station counts capped at 4000 to keep the test short.  Every
+    served result equals the drop-in within 1e-10 (same FP64 sums, other
+    chunking) and the CPU oracle on 16 strided stations within 1e-8."""
+    models = synthetic.serving_models()
+    stream = synthetic.serving_stream(seconds=0.5)[:12]
+    srv = PrismServer(round_pairs=1.6e9)
+    for k in sorted({r["model"] for r in stream if r["resident"]}):
+        prisms, density, _ = models[k]
+        srv.register_layer(f"model{k}", prisms, density)
+    futs, inputs = [], []
+    for req in stream:
+        prisms, density, side = models[req["model"]]
+        coords = synthetic.serving_request_coordinates(
+            dict(req, n_stations=min(req["n_stations"], 4000)), side)
+        if req["resident"]:
+            futs.append(srv.submit(coords, req["field"], layer=f"model{req['model']}"))
+        else:
+            futs.append(srv.submit(coords, req["field"], prisms=prisms, density=density))
+        inputs.append((coords, prisms, density, req["field"]))
+    results = [f.result(timeout=300) for f in futs]
+    srv.close()
+    assert max(p.shape[0] for _, p, _, _ in inputs) > 1e5  # the large models are in
+    for (coords, prisms, density, field), got in zip(inputs, results):
+        ref = hg.prism_gravity(coords, prisms, density, field=field)
+        npt.assert_allclose(got, ref, rtol=1e-10, atol=1e-11 * np.abs(ref).max())
+        idx = np.linspace(0, coords[0].size - 1, 16).astype(int)
+        truth = oracle.prism_gravity(tuple(c[idx] for c in coords), prisms, density, field)
+        npt.assert_allclose(got[idx], truth, rtol=1e-8, atol=1e-9 * np.abs(truth).max())
