@@ -189,6 +189,11 @@ HG_HD __forceinline__ P2 log1p_p2(P2 t, const Tables& T) {
   return p2_add(p2_add(eln2, lc), lp);
 }
 
+// arg_core_f2 on the quarter-turn-rotated vector, out of line: the rare lane
+// whose FP32 estimate was too far off (keeps ~5 KB of code per call site out
+// of the hot loops' instruction footprint).
+HG_COLD F2 arg_generic_f2(F2 re, F2 im, Tables T) { return arg_core_f2(re, im, 0, 0, T); }
+
 // Argument of two vectors (lane-wise lm_arg_near_f2) on the branches of the
 // FP32 estimates est0, est1.  The table rotation runs when either lane needs
 // it (the other rotates by 0: exact); a lane whose residual is not small
@@ -232,8 +237,8 @@ HG_HD __forceinline__ P2 arg_near_p2(P2 pr, P2 pi, float est0, float est1, const
     // estimate too far off or non-finite input: generic path on the
     // quarter-turn-rotated vector for that lane, th_j then not added
     F2 a0 = lane0(a), a1 = lane1(a);
-    if (!ok0) a0 = arg_core_f2(lane0(re0), lane0(im0), 0, 0, T);
-    if (!ok1) a1 = arg_core_f2(lane1(re0), lane1(im0), 0, 0, T);
+    if (!ok0) a0 = arg_generic_f2(lane0(re0), lane0(im0), T);
+    if (!ok1) a1 = arg_generic_f2(lane1(re0), lane1(im0), T);
     a = pk(a0, a1);
     if (!ok0) j0 = 0;
     if (!ok1) j1 = 0;

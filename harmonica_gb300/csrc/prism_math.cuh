@@ -1316,8 +1316,15 @@ HG_HD __forceinline__ void family_logs(const GeomF2& g, int fam, const Tables& T
   const P2 ts = single_t_p2(c.straddle, bc(lo), bc(hi), pk(RL(0, 0), RL(1, 0)),
                             pk(RH(0, 0), RH(1, 0)), bc(dA),
                             p2_add(p2_sq(pk(p0, p1)), p2_sq(q0b)));
-  const P2 mq = log1p_p2(tq, T);
-  const P2 ml = log1p_p2(ts, T);
+  // one copy of the logarithm for both (a smaller loop body: the fused and
+  // potential kernels wait on instruction fetch)
+  P2 mq, ml;
+#pragma unroll 1
+  for (int w = 0; w < 2; w++) {
+    const P2 L = log1p_p2(w ? ts : tq, T);
+    if (w) ml = L;
+    else mq = L;
+  }
   mq0 = lane0(mq);
   mq1 = lane1(mq);
   l00 = lane0(ml);
