@@ -39,6 +39,13 @@ template <int F> struct MinBlocks { static constexpr int value = HG_FWD_MIN_BLOC
 template <> struct MinBlocks<kAll> { static constexpr int value = HG_FWD_MIN_BLOCKS_ALL; };
 // the potential needs every log and face angle, like the fused kernel
 template <> struct MinBlocks<kPotential> { static constexpr int value = HG_FWD_MIN_BLOCKS_ALL; };
+// the two launches of the potential and fused all-field forwards (PART 1, 2)
+#ifndef HG_FWD_MIN_BLOCKS_PART
+#define HG_FWD_MIN_BLOCKS_PART 4
+#endif
+template <int F, int PART> struct PartMinBlocks {
+  static constexpr int value = PART == 0 ? MinBlocks<F>::value : HG_FWD_MIN_BLOCKS_PART;
+};
 template <int F> struct BatchMinBlocks { static constexpr int value = HG_BATCH_MIN_BLOCKS; };
 template <> struct BatchMinBlocks<kAll> { static constexpr int value = HG_FWD_MIN_BLOCKS_ALL; };
 template <> struct BatchMinBlocks<kPotential> {
@@ -131,7 +138,13 @@ struct SmemTables {
 // whether the point is a singular point of any prism (null prisms included,
 // as gravity.py:207-214 scans before discarding) for the tensor fields in
 // sing_mask.  Tensor values at singular points are NaN.
-template <int F, class Source, int TILE = kTile>
+// PART (all fields and the potential): 0 adds the whole pair; 1 its edge-log
+// terms, and the whole pair for the pairs the float-pair form declines or
+// that fail faces_fit_f2; 2 its face terms, nothing for those pairs.  Parts
+// 1 and 2 run as two launches whose sums add up to part 0's, each with about
+// half of the hot loop's code: the whole loop outgrows the instruction
+// cache and both kernels then wait on instruction fetch.
+template <int F, class Source, int TILE = kTile, int PART = 0>
 __device__ __forceinline__ void accumulate(const Source& src, int64_t p0, int64_t p1, double pe,
                                            double pn, double pu, bool active, bool check_singular,
                                            uint32_t sing_mask, SmemTileT<TILE>& sh,
@@ -183,8 +196,24 @@ __device__ __forceinline__ void accumulate(const Source& src, int64_t p0, int64_
         constexpr bool ALL = F == kAll;
         double v[ALL ? kNumFields : 1];
         GeomF2 g;
-        const bool fast = !any_zero_bound(q) && make_geom_f2(q, g);
-        if (!(fast && pair_all_f2_geom<ALL>(g, T, v))) {
+        bool fast = !any_zero_bound(q) && make_geom_f2(q, g);
+        if (PART != 0) fast = fast && faces_fit_f2(g);
+        if (PART == 2) {
+          // evaluated whole by part 1 when declined; otherwise the faces fit
+          if (!(fast && pair_all_f2_geom<ALL, 2>(g, T, v))) continue;
+#pragma unroll
+          for (int f = 0; f < (ALL ? kNumFields : 1); f++)
+            if (!ALL || !(f == kGen || f == kGez || f == kGnz)) acc[f] = fma(rho, v[f], acc[f]);
+          continue;
+        }
+        if (PART == 1 && fast) {
+          pair_all_f2_geom<ALL, 1>(g, T, v);
+#pragma unroll
+          for (int f = 0; f < (ALL ? kNumFields : 1); f++)
+            if (!ALL || !(f == kGee || f == kGnn || f == kGzz)) acc[f] = fma(rho, v[f], acc[f]);
+          continue;
+        }
+        if (!(fast && pair_all_f2_geom<ALL, PART>(g, T, v))) {
           const volatile double* vs = &sh.w[p];  // forces the reload (no reuse of q)
           Rel r;
           r.x1 = vs[0] - pe;

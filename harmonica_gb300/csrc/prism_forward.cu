@@ -36,8 +36,10 @@ int cuda_check(cudaError_t e, const char* what) {
 }
 
 // out_mask: for kAll, which of the ten fields are written (compact rows).
-template <int F, class Source>
-__global__ void __launch_bounds__(kThreads, MinBlocks<F>::value) forward_kernel(
+// PART (accumulate()): 0 writes the whole sums; 1 writes the edge-log part
+// (and the pairs taken whole); 2 adds the face part to what part 1 wrote.
+template <int F, class Source, int PART = 0>
+__global__ void __launch_bounds__(kThreads, PartMinBlocks<F, PART>::value) forward_kernel(
     const double* __restrict__ oe, const double* __restrict__ on, const double* __restrict__ ou,
     int64_t n_obs, Source src, int64_t n_prisms, int64_t chunk, uint32_t out_mask,
     double* __restrict__ dst, int64_t dst_chunk_stride, int scale_output, int check_singular,
@@ -60,8 +62,8 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<F>::value) forward_kernel(
   const uint32_t sing_mask = F == kAll ? out_mask : (1u << (F < kNumFields ? F : 0));
   const int64_t p0 = (int64_t)blockIdx.y * chunk;
   const int64_t p1 = min(p0 + chunk, n_prisms);
-  accumulate<F>(src, p0, p1, pe, pn, pu, active, check_singular != 0, sing_mask, sh, T, acc,
-                singular_seen);
+  accumulate<F, Source, kTile, PART>(src, p0, p1, pe, pn, pu, active, check_singular != 0,
+                                     sing_mask, sh, T, acc, singular_seen);
   if (singular_seen) atomicOr(flag, 1);
   if (!active) return;
   double* d = dst + (int64_t)blockIdx.y * dst_chunk_stride;
@@ -70,12 +72,15 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<F>::value) forward_kernel(
 #pragma unroll
     for (int f = 0; f < kNumFields; f++) {
       if ((out_mask >> f) & 1u) {
-        d[(int64_t)row * n_obs + i] = scale_output ? acc[f] * field_scale(f) : acc[f];
+        const double v = scale_output ? acc[f] * field_scale(f) : acc[f];
+        double* o = d + (int64_t)row * n_obs + i;
+        *o = PART == 2 ? *o + v : v;
         row++;
       }
     }
   } else {
-    d[i] = scale_output ? acc[0] * field_scale(F) : acc[0];
+    const double v = scale_output ? acc[0] * field_scale(F) : acc[0];
+    d[i] = PART == 2 ? d[i] + v : v;
   }
 }
 
@@ -236,9 +241,19 @@ int launch_forward(const Plan& plan, const double* oe, const double* on, const d
   const int scale = direct ? 1 : 0;
   const int cs = check_singular ? 1 : 0;
   int32_t* fl = flag;
-  if (plan.all) {
-    forward_kernel<kAll, Source><<<grid, kThreads, 0, stream>>>(
-        oe, on, ou, n_obs, src, n_prisms, plan.chunk, mask, dst, chunk_stride, scale, cs, fl);
+  if (plan.all || plan.single_field == kPotential) {
+    // edge-log part, then face part added in place (same stream: ordered)
+    if (plan.all) {
+      forward_kernel<kAll, Source, 1><<<grid, kThreads, 0, stream>>>(
+          oe, on, ou, n_obs, src, n_prisms, plan.chunk, mask, dst, chunk_stride, scale, cs, fl);
+      forward_kernel<kAll, Source, 2><<<grid, kThreads, 0, stream>>>(
+          oe, on, ou, n_obs, src, n_prisms, plan.chunk, mask, dst, chunk_stride, scale, 0, fl);
+    } else {
+      forward_kernel<kPotential, Source, 1><<<grid, kThreads, 0, stream>>>(
+          oe, on, ou, n_obs, src, n_prisms, plan.chunk, mask, dst, chunk_stride, scale, cs, fl);
+      forward_kernel<kPotential, Source, 2><<<grid, kThreads, 0, stream>>>(
+          oe, on, ou, n_obs, src, n_prisms, plan.chunk, mask, dst, chunk_stride, scale, 0, fl);
+    }
   } else {
     switch (plan.single_field) {
 #define HG_CASE(FF)                                                                            \
@@ -247,7 +262,7 @@ int launch_forward(const Plan& plan, const double* oe, const double* on, const d
                                                              plan.chunk, mask, dst,            \
                                                              chunk_stride, scale, cs, fl);     \
     break;
-      HG_CASE(0) HG_CASE(1) HG_CASE(2) HG_CASE(3) HG_CASE(4)
+      HG_CASE(1) HG_CASE(2) HG_CASE(3) HG_CASE(4)
       HG_CASE(5) HG_CASE(6) HG_CASE(7) HG_CASE(8) HG_CASE(9)
 #undef HG_CASE
       default: return set_error(HG_ERR_INVALID, "bad field");

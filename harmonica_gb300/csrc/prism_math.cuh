@@ -1368,8 +1368,25 @@ HG_HD __forceinline__ bool any_zero_bound(const Rel& q) {
 }
 
 // pair_all_f2 on a geometry with no zero bound, already on float pairs.
-template <bool ALL>
+// PART 0: the whole pair; 1: the edge-log terms alone; 2: the face terms
+// alone (the two parts add up to part 0; see faces_fit_f2).
+template <bool ALL, int PART = 0>
 HG_HD __forceinline__ bool pair_all_f2_geom(const GeomF2& g, const Tables& T, double* out);
+
+// A sufficient test that no face of the pair declines the float-pair scale
+// (face_pair_core_p2): every bound and extent within 2^14 of the largest
+// bound (the face inputs must be within 2^16 of the face's largest vertex
+// distance, itself below 4 x the largest bound).  The kernels that evaluate
+// the edge and face parts in two launches take the FP64 path for the pairs
+// that fail it, in the edge launch, and skip them in the face launch.
+HG_HD __forceinline__ bool faces_fit_f2(const GeomF2& g) {
+  using namespace lean;
+  const auto fe = [](F2 a) { return (int)((f2u(a.h) >> 23) & 0xffu); };
+  int m = min(fe(g.d[0]), min(fe(g.d[1]), fe(g.d[2])));
+#pragma unroll
+  for (int a = 0; a < 3; a++) m = min(m, min(fe(g.c[a][0]), fe(g.c[a][1])));
+  return m >= 127 - 14;
+}
 
 template <bool ALL>
 HG_HD __forceinline__ bool pair_all_f2(const Rel& q, const Tables& T, double* out) {
@@ -1379,11 +1396,12 @@ HG_HD __forceinline__ bool pair_all_f2(const Rel& q, const Tables& T, double* ou
 
 // The potential alone: the combinations on scalar float pairs (measured
 // faster for this kernel than the packed form of the fused one below).
+template <int PART>
 HG_HD __forceinline__ bool potential_f2_geom(const GeomF2& g, const Tables& T, double* out) {
   using namespace lean;
   F2 pot{0.0f, 0.0f}, faces2{0.0f, 0.0f};
 #pragma unroll 1
-  for (int fam = 0; fam < 3; fam++) {
+  for (int fam = 0; fam < (PART == 2 ? 0 : 3); fam++) {
     F2 mq0, mq1, mp0, l00;
     family_logs(g, fam, T, mq0, mq1, mp0, l00);
     const int P = fam == 0 ? 1 : 0, Q = fam == 2 ? 1 : 2;
@@ -1396,7 +1414,7 @@ HG_HD __forceinline__ bool potential_f2_geom(const GeomF2& g, const Tables& T, d
     pot = f2_add(pot, E);
   }
 #pragma unroll 1
-  for (int axis = 0; axis < 3; axis++) {
+  for (int axis = 0; axis < (PART == 1 ? 0 : 3); axis++) {
     F2 o0, o1;
     if (!face_pair_f2(g, axis, T, o0, o1)) return false;
     const F2 u0 = bound_f2(g, axis, 0), du = extent_f2(g, axis);
@@ -1409,10 +1427,10 @@ HG_HD __forceinline__ bool potential_f2_geom(const GeomF2& g, const Tables& T, d
   return true;
 }
 
-template <bool ALL>
+template <bool ALL, int PART>
 HG_HD __forceinline__ bool pair_all_f2_geom(const GeomF2& g, const Tables& T, double* out) {
   using namespace lean;
-  if (!ALL) return potential_f2_geom(g, T, out);
+  if (!ALL) return potential_f2_geom<PART>(g, T, out);
   const F2 zero{0.0f, 0.0f};
   // The combinations below run two products or sums per packed instruction:
   // pot2 holds the potential's edge terms in two lanes (dP dQ L00 + q1 dP
@@ -1421,7 +1439,7 @@ HG_HD __forceinline__ bool pair_all_f2_geom(const GeomF2& g, const Tables& T, do
   P2 pot2{sp2(0.0f), sp2(0.0f)}, face2{sp2(0.0f), sp2(0.0f)};
   F2 ge = zero, gn = zero, gz = zero, Dx = zero, Dy = zero, Dz = zero;
 #pragma unroll 1
-  for (int fam = 0; fam < 3; fam++) {
+  for (int fam = 0; fam < (PART == 2 ? 0 : 3); fam++) {
     F2 mq0, mq1, mp0, l00;
     family_logs(g, fam, T, mq0, mq1, mp0, l00);
     const int P = fam == 0 ? 1 : 0, Q = fam == 2 ? 1 : 2;
@@ -1448,7 +1466,7 @@ HG_HD __forceinline__ bool pair_all_f2_geom(const GeomF2& g, const Tables& T, do
   }
   F2 diff[3] = {zero, zero, zero};
 #pragma unroll 1
-  for (int axis = 0; axis < 3; axis++) {
+  for (int axis = 0; axis < (PART == 1 ? 0 : 3); axis++) {
     F2 o0, o1;
     if (!face_pair_f2(g, axis, T, o0, o1)) return false;
     const F2 u0 = bound_f2(g, axis, 0), du = extent_f2(g, axis);
@@ -1481,12 +1499,14 @@ HG_HD __forceinline__ bool pair_all_f2_geom(const GeomF2& g, const Tables& T, do
     out[kGe] = f2_to_double(ge, e1);
     out[kGn] = f2_to_double(gn, e1);
     out[kGz] = f2_to_double(gz, e1);
-    out[kGee] = f2_to_double(diff[0], 0);
-    out[kGnn] = f2_to_double(diff[1], 0);
-    out[kGzz] = f2_to_double(diff[2], 0);
-    out[kGen] = f2_to_double(Dz, 0);
-    out[kGez] = f2_to_double(Dy, 0);
-    out[kGnz] = f2_to_double(Dx, 0);
+    // the diagonal tensor components are face terms alone, the off-diagonal
+    // ones edge terms alone
+    out[kGee] = PART == 1 ? 0.0 : f2_to_double(diff[0], 0);
+    out[kGnn] = PART == 1 ? 0.0 : f2_to_double(diff[1], 0);
+    out[kGzz] = PART == 1 ? 0.0 : f2_to_double(diff[2], 0);
+    out[kGen] = PART == 2 ? 0.0 : f2_to_double(Dz, 0);
+    out[kGez] = PART == 2 ? 0.0 : f2_to_double(Dy, 0);
+    out[kGnz] = PART == 2 ? 0.0 : f2_to_double(Dx, 0);
   }
   return true;
 }
