@@ -23,10 +23,15 @@ HG_HD __forceinline__ bool is_tensor(int f) { return f >= kGee && f <= kGnz; }
 
 // Resident CTAs per SM the register allocation must allow (more warps hide
 // the arithmetic latency; the fused all-field kernel needs more registers).
-// Measured on the 1e6-prism layer: the single-field forward kernels at 6
-// (80 registers) run g_z 1.4 % and g_zz 2.8 % faster than at 5 (96).
+// Measured on the 1e6-prism layer: the tensor kernels at 6 (80 registers)
+// run g_zz 3 % faster than at 5; the first-derivative kernels (g_e, g_n,
+// g_z: merged logs and faces) at 5 (96 registers, less than half the
+// spills) run 4 % faster than at 6.
 #ifndef HG_FWD_MIN_BLOCKS
 #define HG_FWD_MIN_BLOCKS 6
+#endif
+#ifndef HG_FWD_MIN_BLOCKS_GRAD
+#define HG_FWD_MIN_BLOCKS_GRAD 5
 #endif
 #ifndef HG_FWD_MIN_BLOCKS_ALL
 #define HG_FWD_MIN_BLOCKS_ALL 4
@@ -35,7 +40,10 @@ HG_HD __forceinline__ bool is_tensor(int f) { return f >= kGee && f <= kGnz; }
 #ifndef HG_BATCH_MIN_BLOCKS
 #define HG_BATCH_MIN_BLOCKS 5
 #endif
-template <int F> struct MinBlocks { static constexpr int value = HG_FWD_MIN_BLOCKS; };
+template <int F> struct MinBlocks {
+  static constexpr int value =
+      (F == kGe || F == kGn || F == kGz) ? HG_FWD_MIN_BLOCKS_GRAD : HG_FWD_MIN_BLOCKS;
+};
 template <> struct MinBlocks<kAll> { static constexpr int value = HG_FWD_MIN_BLOCKS_ALL; };
 // the potential needs every log and face angle, like the fused kernel
 template <> struct MinBlocks<kPotential> { static constexpr int value = HG_FWD_MIN_BLOCKS_ALL; };

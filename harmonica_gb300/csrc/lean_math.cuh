@@ -324,6 +324,21 @@ HG_HD __forceinline__ F2 scaled_f2(long long b, int top) {
   return (ef == 0 || k < -120) ? F2{0.0f, 0.0f} : m;
 }
 
+// scaled_f2 for a value that is zero or within 2^-40 of the scale (ef >=
+// top - 40, as make_geom_f2 checks first): the high float assembled from the
+// bits (sign, exponent 127 + ef - top, the leading 23 fraction bits), the low
+// one as the other 29 fraction bits times 2^(ef - top - 52) with the same
+// sign -- the same pair as scaled_f2 with fewer instructions.
+HG_HD __forceinline__ F2 scaled_f2_near(long long b, int top) {
+  const unsigned hi = (unsigned)((unsigned long long)b >> 32), lo = (unsigned)b;
+  const int ef = (int)((hi >> 20) & 0x7ffu);
+  const unsigned sign = hi & 0x80000000u;
+  const unsigned frac = ((hi << 3) | (lo >> 29)) & 0x7fffffu;
+  const float h = u2f(sign | ((unsigned)(127 + ef - top) << 23) | frac);
+  const float l = fmul(u32_to_f32(lo & 0x1fffffffu), u2f(sign | ((unsigned)(75 + ef - top) << 23)));
+  return ef == 0 ? F2{0.0f, 0.0f} : F2{h, l};
+}
+
 // The pair as a double times 2^k, assembled with integer instructions: the
 // 24-bit significand of h widened to 53 bits, the significand of l shifted
 // into its place and added or subtracted, one normalisation step.  For

@@ -171,7 +171,9 @@ Plan make_plan(int64_t n_obs, int64_t n_prisms, uint32_t mask) {
   // 1e6 prisms): 1 wave 1.09e10 pairs/s, 2 1.14e10, 4 1.18e10, 16 1.20e10,
   // 32 1.21e10 (the old fixed 8 CTAs per SM was 1.6 waves).
   const bool wide = p.all || p.single_field == kPotential;
-  const int64_t resident = wide ? HG_FWD_MIN_BLOCKS_ALL : HG_FWD_MIN_BLOCKS;
+  const bool grad = p.single_field == kGe || p.single_field == kGn || p.single_field == kGz;
+  const int64_t resident =
+      wide ? HG_FWD_MIN_BLOCKS_PART : (grad ? HG_FWD_MIN_BLOCKS_GRAD : HG_FWD_MIN_BLOCKS);
   const int64_t target = (int64_t)kSmCount * resident * launch_waves();
   int64_t n_prism_tiles = (n_prisms + kTile - 1) / kTile;
   if (n_prism_tiles < 1) n_prism_tiles = 1;

@@ -720,7 +720,7 @@ HG_HD __forceinline__ bool make_geom_f2(const Rel& q, GeomF2& g) {
       tiny_nz(q.z1) || tiny_nz(q.z2) || ex(q.dx) < top - 20 || ex(q.dy) < top - 20 ||
       ex(q.dz) < top - 20)
     return false;
-  const auto f = [&](double v) { return scaled_f2(d2ll(v), top); };
+  const auto f = [&](double v) { return scaled_f2_near(d2ll(v), top); };
   g.top = top;
   g.c[0][0] = f(q.x1);
   g.c[0][1] = f(q.x2);
@@ -989,14 +989,24 @@ HG_HD __forceinline__ bool face_pair_core_p2(const lean::F2 fa[2], const lean::F
             fsmall(fc[1]) || fe(fw) < ftop[k] - 16;
   }
   if (small) return false;
-  const float2 sc = mk2(pow2f(127 - ftop[0]), pow2f(127 - ftop[1]));
-  const auto both = [&](F2 a) { return p2_scale(pk(a, a), sc); };
-  const auto per = [&](F2 a0, F2 a1) { return p2_scale(pk(a0, a1), sc); };
   const bool n0 = fa[0].h < 0.0f, n1 = fa[1].h < 0.0f;
-  o = face_core_p2(per(n0 ? f2_neg(fa[0]) : fa[0], n1 ? f2_neg(fa[1]) : fa[1]), both(fb[0]),
-                   both(fb[1]), both(fc[0]), both(fc[1]), per(fr[0][0][0], fr[1][0][0]),
-                   per(fr[0][0][1], fr[1][0][1]), per(fr[0][1][0], fr[1][1][0]),
-                   per(fr[0][1][1], fr[1][1][1]), both(fw), same_sign, T);
+  P2 v[10] = {pk(n0 ? f2_neg(fa[0]) : fa[0], n1 ? f2_neg(fa[1]) : fa[1]),
+              pk(fb[0], fb[0]), pk(fb[1], fb[1]), pk(fc[0], fc[0]), pk(fc[1], fc[1]),
+              pk(fr[0][0][0], fr[1][0][0]), pk(fr[0][0][1], fr[1][0][1]),
+              pk(fr[0][1][0], fr[1][1][0]), pk(fr[0][1][1], fr[1][1][1]), pk(fw, fw)};
+#ifndef HG_FACE_SCALE_ALWAYS
+  // Scale so that each face's largest vertex distance is in [1, 2), unless
+  // it is already in [1, 4) (the geometry's own scale puts the largest
+  // bound in [1, 2): the common case of a face as far as the farthest
+  // bound): the products below stay in the float range either way.
+  if (ftop[0] < 127 || ftop[1] < 127)
+#endif
+  {
+    const float2 sc = mk2(pow2f(127 - ftop[0]), pow2f(127 - ftop[1]));
+#pragma unroll
+    for (int k = 0; k < 10; k++) v[k] = p2_scale(v[k], sc);
+  }
+  o = face_core_p2(v[0], v[1], v[2], v[3], v[4], v[5], v[6], v[7], v[8], v[9], same_sign, T);
   F2 o0 = lane0(o), o1 = lane1(o);
   if (n0) o0 = f2_neg(o0);
   if (n1) o1 = f2_neg(o1);
