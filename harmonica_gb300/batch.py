@@ -3,8 +3,8 @@ Many independent prism forward problems in one persistent launch.
 
 :class:`PrismBatch` wraps the C ABI ``hg_batch_*``: it keeps every problem's
 inputs and outputs resident on the device, builds the work list once, and
-runs it with one memset, one launch per field present and one reduction on
-the current stream — directly or replayed from a captured CUDA graph.
+runs it with one memset, one launch per field present (two for the
+potential) and one reduction on the current stream — directly or replayed from a captured CUDA graph.
 :func:`autotune` picks, per field, the shape of the work (observation points
 per CTA and per work item, which is also the prism tile staged in shared
 memory; prisms per work item; persistent CTAs) by timing candidate shapes on

@@ -33,7 +33,9 @@ struct WorkItem {
   int32_t pad;
 };
 
-template <int F, int THREADS>
+// PART (the potential: accumulate()): 0 the whole pairs; 1 writes the
+// edge-log part, 2 adds the face part (a second launch over the same items).
+template <int F, int THREADS, int PART = 0>
 __device__ __forceinline__ void run_item(const ProblemDev& P, const WorkItem& w,
                                          SmemTileT<THREADS>& sh, const Tables& T,
                                          double* __restrict__ part) {
@@ -47,10 +49,14 @@ __device__ __forceinline__ void run_item(const ProblemDev& P, const WorkItem& w,
   double acc[1] = {0.0};
   bool singular = false;
   const bool check = P.check_singular && P.flag != nullptr;
-  accumulate<F, ListSource, THREADS>(ListSource{P.soa, P.stride}, p0, p1, pe, pn, pu, active,
-                                     check, 1u << F, sh, T, acc, singular);
+  accumulate<F, ListSource, THREADS, PART>(ListSource{P.soa, P.stride}, p0, p1, pe, pn, pu,
+                                           active, check && PART != 2, 1u << F, sh, T, acc,
+                                           singular);
   if (singular) atomicOr(P.flag, 1);
-  if (active) part[P.part_offset + (int64_t)w.chunk * P.n_obs + i] = acc[0];
+  if (active) {
+    double* o = part + P.part_offset + (int64_t)w.chunk * P.n_obs + i;
+    *o = PART == 2 ? *o + acc[0] : acc[0];
+  }
 }
 
 // Persistent kernel for the work items of one field F (the items of a batch
@@ -59,8 +65,10 @@ __device__ __forceinline__ void run_item(const ProblemDev& P, const WorkItem& w,
 // THREADS points per CTA and per work item, THREADS prisms per shared-memory
 // tile, and as many resident CTAs per SM as the 128-point kernel times
 // 128 / THREADS (the same registers per thread).
-template <int F, int THREADS>
-__global__ void __launch_bounds__(THREADS, BatchMinBlocks<F>::value * (kThreads / THREADS))
+template <int F, int THREADS, int PART = 0>
+__global__ void __launch_bounds__(THREADS, (PART == 0 ? BatchMinBlocks<F>::value
+                                                      : HG_FWD_MIN_BLOCKS_PART) *
+                                               (kThreads / THREADS))
     batch_kernel(const ProblemDev* __restrict__ probs, const WorkItem* __restrict__ items,
                  int64_t n_items, unsigned long long* __restrict__ counter,
                  double* __restrict__ part) {
@@ -75,17 +83,19 @@ __global__ void __launch_bounds__(THREADS, BatchMinBlocks<F>::value * (kThreads 
     const long long it = next;
     if (it >= n_items) break;
     const WorkItem w = items[it];
-    run_item<F, THREADS>(probs[w.problem], w, sh, T, part);
+    run_item<F, THREADS, PART>(probs[w.problem], w, sh, T, part);
   }
 }
 
 using BatchKernel = void (*)(const ProblemDev*, const WorkItem*, int64_t, unsigned long long*,
                              double*);
 
+// The potential runs as two launches over its items (accumulate()): this
+// table gives the first (edge-log part), batch_potential_faces the second.
 template <int THREADS>
 BatchKernel batch_kernel_table(int f) {
   switch (f) {
-    case kPotential: return batch_kernel<kPotential, THREADS>;
+    case kPotential: return batch_kernel<kPotential, THREADS, 1>;
     case kGe: return batch_kernel<kGe, THREADS>;
     case kGn: return batch_kernel<kGn, THREADS>;
     case kGz: return batch_kernel<kGz, THREADS>;
@@ -98,9 +108,17 @@ BatchKernel batch_kernel_table(int f) {
   }
 }
 
-// The kernel of field f for `threads` points per CTA (64 or 128); the
-// 64-point kernels are compiled in their own translation unit.
+template <int THREADS>
+BatchKernel batch_potential_faces() {
+  return batch_kernel<kPotential, THREADS, 2>;
+}
+
+// The kernel of field f for `threads` points per CTA (64 or 128), and the
+// potential's second launch; the 64-point kernels are compiled in their own
+// translation unit.
 BatchKernel batch_kernel_for(int f, int threads);
 BatchKernel batch_kernel_for64(int f);
+BatchKernel batch_potential_faces_for(int threads);
+BatchKernel batch_potential_faces64();
 
 }  // namespace hg

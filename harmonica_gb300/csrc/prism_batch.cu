@@ -31,6 +31,9 @@ int cuda_check(cudaError_t e, const char* what);
 BatchKernel batch_kernel_for(int f, int threads) {
   return threads == 64 ? batch_kernel_for64(f) : batch_kernel_table<kThreads>(f);
 }
+BatchKernel batch_potential_faces_for(int threads) {
+  return threads == 64 ? batch_potential_faces64() : batch_potential_faces<kThreads>();
+}
 
 // out_p[i] = scale(field_p) * sum_c part_p[c][i], chunks in order.
 __global__ void batch_reduce_kernel(const ProblemDev* __restrict__ probs,
@@ -261,6 +264,16 @@ int hg_batch_run(const hg_batch* batch, void* workspace, size_t workspace_bytes,
         part);
     rc = cuda_check(cudaGetLastError(), "batch_kernel launch");
     if (rc != HG_OK) return rc;
+    if (f == kPotential) {  // second launch over the same items: the face part
+      rc = cuda_check(cudaMemsetAsync(counter + f, 0, sizeof(unsigned long long), st),
+                      "cudaMemsetAsync(counter)");
+      if (rc != HG_OK) return rc;
+      batch_potential_faces_for(threads)<<<(unsigned)batch->seg_ctas[f], threads, 0, st>>>(
+          batch->d_probs, batch->d_items + batch->seg_begin[f], batch->seg_count[f],
+          counter + f, part);
+      rc = cuda_check(cudaGetLastError(), "batch_kernel launch");
+      if (rc != HG_OK) return rc;
+    }
   }
   dim3 grid(64, (unsigned)batch->n_problems);
   batch_reduce_kernel<<<grid, 256, 0, st>>>(batch->d_probs, part);
@@ -282,7 +295,7 @@ int hg_batch_destroy(hg_batch* batch) {
 namespace hg {
 namespace {
 
-template <int F>
+template <int F, int PART = 0>
 __device__ __forceinline__ void run_plan_item(const hg_problem_plan& P, const hg_work_item& w,
                                               SmemTile& sh, const Tables& T) {
   const int64_t i = (int64_t)w.tile * kThreads + threadIdx.x;
@@ -295,15 +308,21 @@ __device__ __forceinline__ void run_plan_item(const hg_problem_plan& P, const hg
   double acc[1] = {0.0};
   bool singular = false;
   const bool check = P.check_singular && P.singular_flag != nullptr;
-  accumulate<F>(ListSource{P.prisms_soa, P.prism_stride}, p0, p1, pe, pn, pu, active, check,
-                1u << F, sh, T, acc, singular);
+  accumulate<F, ListSource, kTile, PART>(ListSource{P.prisms_soa, P.prism_stride}, p0, p1, pe,
+                                         pn, pu, active, check && PART != 2, 1u << F, sh, T,
+                                         acc, singular);
   if (singular) atomicOr(P.singular_flag, 1);
-  if (active) P.partials[(int64_t)w.chunk * P.n_obs + i] = acc[0];
+  if (active) {
+    double* o = P.partials + (int64_t)w.chunk * P.n_obs + i;
+    *o = PART == 2 ? *o + acc[0] : acc[0];
+  }
 }
 
-// Persistent kernel over the work items of one field F in a round.
-template <int F>
-__global__ void __launch_bounds__(kThreads, BatchMinBlocks<F>::value)
+// Persistent kernel over the work items of one field F in a round (PART:
+// run_item(); the potential runs parts 1 and 2 as two launches).
+template <int F, int PART = 0>
+__global__ void __launch_bounds__(kThreads,
+                                  PART == 0 ? BatchMinBlocks<F>::value : HG_FWD_MIN_BLOCKS_PART)
     round_kernel(const hg_problem_plan* __restrict__ probs, const hg_work_item* __restrict__ items,
                  int64_t n_items, unsigned long long* __restrict__ counter) {
   __shared__ SmemTile sh;
@@ -317,7 +336,7 @@ __global__ void __launch_bounds__(kThreads, BatchMinBlocks<F>::value)
     const long long it = next;
     if (it >= n_items) break;
     const hg_work_item w = items[it];
-    run_plan_item<F>(probs[w.problem], w, sh, T);
+    run_plan_item<F, PART>(probs[w.problem], w, sh, T);
   }
 }
 
@@ -325,7 +344,7 @@ using RoundKernel = void (*)(const hg_problem_plan*, const hg_work_item*, int64_
                              unsigned long long*);
 RoundKernel round_kernel_for(int f) {
   switch (f) {
-    case kPotential: return round_kernel<kPotential>;
+    case kPotential: return round_kernel<kPotential, 1>;
     case kGe: return round_kernel<kGe>;
     case kGn: return round_kernel<kGn>;
     case kGz: return round_kernel<kGz>;
@@ -387,10 +406,19 @@ int hg_round_run(const hg_problem_plan* problems, const hg_work_item* items,
       ctas = (int64_t)std::max(1, per_sm) * sms;
     }
     ctas = std::min<int64_t>(ctas, n);
-    round_kernel_for(f)<<<(unsigned)ctas, kThreads, 0, st>>>(
-        problems, items + begin, n, static_cast<unsigned long long*>(counter) + f);
+    unsigned long long* cnt = static_cast<unsigned long long*>(counter) + f;
+    round_kernel_for(f)<<<(unsigned)ctas, kThreads, 0, st>>>(problems, items + begin, n, cnt);
     rc = cuda_check(cudaGetLastError(), "round_kernel launch");
     if (rc != HG_OK) return rc;
+    if (f == kPotential) {  // second launch over the same items: the face part
+      rc = cuda_check(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), st),
+                      "cudaMemsetAsync(counter)");
+      if (rc != HG_OK) return rc;
+      round_kernel<kPotential, 2><<<(unsigned)ctas, kThreads, 0, st>>>(problems, items + begin, n,
+                                                                        cnt);
+      rc = cuda_check(cudaGetLastError(), "round_kernel launch");
+      if (rc != HG_OK) return rc;
+    }
     begin += n;
   }
   return HG_OK;

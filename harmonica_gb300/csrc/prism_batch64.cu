@@ -5,5 +5,6 @@
 namespace hg {
 
 BatchKernel batch_kernel_for64(int f) { return batch_kernel_table<64>(f); }
+BatchKernel batch_potential_faces64() { return batch_potential_faces<64>(); }
 
 }  // namespace hg

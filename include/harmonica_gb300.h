@@ -214,8 +214,10 @@ int hg_batch_workspace(const hg_batch *batch, size_t *bytes);
 int hg_batch_info(const hg_batch *batch, int64_t *n_items, int64_t *n_ctas, double *pairs);
 
 /*
- * Run the batch on `stream`: one memset, one launch per field present and
- * one reduction launch, no allocation and no host synchronisation
+ * Run the batch on `stream`: one memset, one launch per field present (two
+ * for the potential, its edge-log and face terms, with a counter reset
+ * between them) and one reduction launch, no allocation and no host
+ * synchronisation
  * (capturable in a CUDA graph; replays recompute from the current contents
  * of the problems' input buffers).
  */
@@ -264,8 +266,9 @@ typedef struct hg_work_item {
  * order, with field_counts[f] (host array of 10) items of field f; every
  * field present gets its own persistent launch over the problem table
  * (device array) with n_ctas CTAs (<= 0: one full wave of that field's
- * kernel).  `counter` is 80 bytes of device memory (one counter per field)
- * the call zeroes and uses.
+ * kernel); the potential gets two (its edge-log terms, then its face terms
+ * added to the same partial sums).  `counter` is 80 bytes of device memory
+ * (one counter per field) the call zeroes and uses.
  */
 int hg_round_run(const hg_problem_plan *problems, const hg_work_item *items,
                  const int64_t *field_counts, int32_t n_ctas, void *counter, void *stream);
