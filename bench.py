@@ -23,13 +23,16 @@ Keys of the JSON line:
   host->device copies of the layer and the batch, the kernels and the
   device->host copy of the result inside the timed region.
 * ``roofline``: the binding hardware resource of the layer kernel.  The pair
-  is evaluated on FP32 float pairs, so the kernel is bound by instruction
-  issue (one warp instruction per clock per SM sub-partition): ``achieved``
-  = warp instructions per pair x the kernel's pairs/s, ``peak`` = 4 x SMs x
-  the SM clock sampled during the timed steps.  The instruction, FP64 and
-  DRAM counts per pair come from one ncu capture of the same kernel and are
-  used only while the kernel sources hash to the value recorded with them
-  (otherwise ``stale`` and no fraction).  ``algorithmic`` holds the survey's
+  is evaluated on FP32 float pairs, so the kernel is bound by the FP32 (FMA)
+  pipes: ``achieved`` = FP32 lane operations per pair (scalar instructions
+  plus twice the packed FADD2/FFMA2/FMUL2) x the kernel's pairs/s, ``peak``
+  = 128 FP32 lanes per SM x SMs x the SM clock sampled during the timed
+  steps; instruction issue, the other near-binding resource, is reported
+  beside it (``issue``: warp instructions per pair x pairs/s against one per
+  clock per SM sub-partition).  The instruction, FP64 and DRAM counts per
+  pair come from one ncu capture of the same kernel and are used only while
+  the kernel sources hash to the value recorded with them (otherwise
+  ``stale`` and no fraction).  ``algorithmic`` holds the survey's
   flop convention for the closed form (720 flop per g_z pair: 8 vertices x
   (~16 basic + sqrt + 2 log + 1 atan2) at basic=1, sqrt=4, log=20,
   atan2=30) against the FP64 FMA rate measured live.
@@ -74,27 +77,30 @@ ARITH = ("FP64 inputs, outputs and accumulation; each pair's closed form evaluat
 WORKLOAD = "layer_topography_1e6: 1000x1000 prisms (200 m grid), 500x500 stations, g_z"
 ALGO_FLOP_PER_PAIR_GZ = 720.0
 ISSUE_PER_SM_PER_CLOCK = 4  # one warp instruction per clock per SM sub-partition
+FP32_LANES_PER_SM_PER_CLOCK = 128  # FMA-heavy + FMA-lite pipes, 16 lanes each per sub-partition
 
 # Kernel sources whose hash keys the ncu counts below.
 KERNEL_SOURCES = ("prism_math.cuh", "lean_math.cuh", "lean_packed.cuh", "lean_tables.inc",
                   "forward_core.cuh", "prism_forward.cu")
-# ncu counts of the layer g_z kernel (forward_kernel<3, LayerSource>): warp instructions
-# (smsp__inst_executed.sum) and FP64 thread instructions
-# (sm__sass_thread_inst_executed_op_fp64_pred_on.sum) per pair, from a capture of a
+# ncu counts of the layer g_z kernel (forward_kernel<3, LayerSource, 0>): warp instructions
+# (smsp__inst_executed.sum), FP32 lane operations (sm__sass_thread_inst_executed_op_fp32_pred_on
+# plus the packed fadd2/ffma2/fmul2 counts once more: two lanes each) and FP64 thread
+# instructions (sm__sass_thread_inst_executed_op_fp64_pred_on) per pair, from a capture of a
 # 1000-station step (1e9 pairs per launch, two launches); and the DRAM bytes
 # (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of the default 5000-station
-# step (the layer is read once; the writes are the kernel's register spills, written back
-# from L2 at ~1.5 GB/s, and the chunk partial sums).
+# step (the layer and the stations are read once; the writes are the chunk partial sums and
+# the kernel's few register spills written back from L2).
 # Summarised under profiles/; valid for the kernel sources that hash to `sources_sha`.
 KERNEL_COUNTS = {
-    "sources_sha": "c5b04bd8517f9e0b",
-    "warp_inst_per_pair": 57.31,
+    "sources_sha": "e06f78809c0bc651",
+    "warp_inst_per_pair": 55.75,
+    "fp32_lane_ops_per_pair": 1924.7,
     "fp64_inst_per_pair": 9.40,
-    "dram_bytes_default_step": 540357000,  # 26.01 MB read + 514.35 MB written (two launches)
+    "dram_bytes_default_step": 33493888,  # 24.98 MB read + 8.51 MB written (two launches)
     "default_step_stations": 5000,
     # the same capture's utilisations (fractions of peak over the active cycles)
-    "ncu_utilisation": {"issue_active": 0.647, "fma_pipe": 0.684, "fmaheavy_pipe": 0.706,
-                        "fmalite_pipe": 0.662, "alu_pipe": 0.367, "fp64_pipe": 0.215},
+    "ncu_utilisation": {"issue_active": 0.648, "fma_pipe": 0.693, "fmaheavy_pipe": 0.726,
+                        "fmalite_pipe": 0.660, "alu_pipe": 0.365, "fp64_pipe": 0.221},
     "capture": "ncu on GB300: per-pair counts from two launches of a 1000-station step, "
                "DRAM bytes from two launches of the default step (1-pass metrics)",
 }
@@ -850,8 +856,8 @@ def run_tesseroids(args, rank, world, local):
 # the headline
 
 def layer_roofline(torch, dev, kernel_pairs_per_s, clocks, stations_per_step, algo_bytes):
-    """Roofline of the layer g_z kernel on its binding resource (instruction
-    issue), with the algorithmic FP64 figure beside it."""
+    """Roofline of the layer g_z kernel on its binding resource (the FP32
+    pipes), with instruction issue and the algorithmic FP64 figure beside it."""
     peak = fp64_peak(torch)
     sha = kernel_sources_sha()
     counts = KERNEL_COUNTS
@@ -860,12 +866,13 @@ def layer_roofline(torch, dev, kernel_pairs_per_s, clocks, stations_per_step, al
     sm_hz = (clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 0.0) * 1e6
     issue_peak = ISSUE_PER_SM_PER_CLOCK * n_sms * sm_hz
     algo = ALGO_FLOP_PER_PAIR_GZ * kernel_pairs_per_s / 1e12
+    fp32_peak = FP32_LANES_PER_SM_PER_CLOCK * n_sms * sm_hz
     roof = {
-        "bound": "instruction issue",
-        "unit": "G warp-instructions/s",
-        "peak": issue_peak / 1e9 if issue_peak else None,
-        "peak_source": "4 warp instructions per clock per SM x SMs x the SM clock sampled "
-                       "during the timed steps",
+        "bound": "fp32 pipe",
+        "unit": "T FP32 lane-ops/s",
+        "peak": fp32_peak / 1e12 if fp32_peak else None,
+        "peak_source": "128 FP32 lanes per clock per SM x SMs x the SM clock sampled during "
+                       "the timed steps (no FP32 figure in the measured peaks)",
         "kernel_sources_sha": sha,
         "counts_from": counts["capture"] if fresh else None,
         "stale": not fresh,
@@ -883,9 +890,16 @@ def layer_roofline(torch, dev, kernel_pairs_per_s, clocks, stations_per_step, al
     }
     if fresh:
         issue_rate = counts["warp_inst_per_pair"] * kernel_pairs_per_s
+        fp32_rate = counts["fp32_lane_ops_per_pair"] * kernel_pairs_per_s
         same_step = stations_per_step == counts["default_step_stations"]
-        roof.update(achieved=issue_rate / 1e9,
-                    frac=issue_rate / issue_peak if issue_peak else None,
+        roof.update(achieved=fp32_rate / 1e12,
+                    frac=fp32_rate / fp32_peak if fp32_peak else None,
+                    fp32_lane_ops_per_pair=counts["fp32_lane_ops_per_pair"],
+                    issue={"achieved": issue_rate / 1e9, "unit": "G warp-instructions/s",
+                           "peak": issue_peak / 1e9 if issue_peak else None,
+                           "frac": issue_rate / issue_peak if issue_peak else None,
+                           "peak_source": "4 warp instructions per clock per SM x SMs x the "
+                                          "SM clock sampled during the timed steps"},
                     warp_inst_per_pair=counts["warp_inst_per_pair"],
                     ncu_utilisation=counts["ncu_utilisation"],
                     traffic=counts["dram_bytes_default_step"] if same_step else None,
