@@ -112,8 +112,30 @@ template <int TILE>
 struct SmemTileT {
   double w[TILE], e[TILE], s[TILE], n[TILE], b[TILE], t[TILE], rho[TILE];
   double dx[TILE], dy[TILE], dz[TILE];  // extents
+  float rhoh[TILE], rhol[TILE];         // the density as a float pair
   int null[TILE];
+  int rnat[TILE];                       // density within 2^-40..2^40 (nat_fields)
 };
+
+// Float-pair sums of the potential and fused all-field launches (PART 1, 2):
+// each pair's fields on float pairs in natural units (times the density, a
+// float pair too) are added to per-thread float-pair sums, which are added to
+// the FP64 sums once per prism tile -- in place of a float-pair -> double
+// conversion (~25 integer instructions) and an FP64 FMA per field and pair.
+// A float-pair sum of at most one tile of terms keeps ~2^-46 of its value.
+// The fields each part carries: the potential and the three first
+// derivatives, then the three off-diagonal (part 1) or diagonal (part 2)
+// tensor components.
+template <bool ALL, int PART> struct NatFields {
+  static constexpr int n = ALL ? 7 : 1;
+  static HG_HD __forceinline__ int field(int k) {
+    return k < 4 ? k : (PART == 1 ? kGen + (k - 4) : kGee + (k - 4));
+  }
+};
+// Pairs whose scale exponent e1 = top - 1023 is within +-30 and whose
+// density is within 2^-40..2^40 keep every natural-unit value and product
+// in the normal float range (the potential scales as 2^(2 e1)).
+constexpr int kNatMaxExp = 30;
 using SmemTile = SmemTileT<kTile>;
 
 struct SmemTables {
@@ -175,8 +197,21 @@ __device__ __forceinline__ void accumulate(const Source& src, int64_t p0, int64_
       sh.dy[threadIdx.x] = n - s;
       sh.dz[threadIdx.x] = t - b;
       sh.null[threadIdx.x] = null;
+      if (PART != 0) {
+        const long long rb = lean::d2ll(rho);
+        const int re = (int)((rb >> 52) & 0x7ff);
+        const lean::F2 rf = lean::scaled_f2(rb, 1023);
+        sh.rhoh[threadIdx.x] = rf.h;
+        sh.rhol[threadIdx.x] = rf.l;
+        sh.rnat[threadIdx.x] = re >= 1023 - 40 && re <= 1023 + 40;
+      }
     }
     __syncthreads();
+    constexpr int NNAT = (F == kAll || F == kPotential) && PART != 0
+                             ? NatFields<F == kAll, PART>::n : 1;
+    lean::F2 nat[NNAT];
+#pragma unroll
+    for (int k = 0; k < NNAT; k++) nat[k] = lean::F2{0.0f, 0.0f};
     for (int p = 0; p < cnt; p++) {
       Rel q;
       q.x1 = sh.w[p] - pe;
@@ -206,19 +241,44 @@ __device__ __forceinline__ void accumulate(const Source& src, int64_t p0, int64_
         GeomF2 g;
         bool fast = !any_zero_bound(q) && make_geom_f2(q, g);
         if (PART != 0) fast = fast && faces_fit_f2(g);
-        if (PART == 2) {
-          // evaluated whole by part 1 when declined; otherwise the faces fit
-          if (!(fast && pair_all_f2_geom<ALL, 2>(g, T, v))) continue;
+        if (PART != 0 && (PART == 2 || fast)) {
+          // part 2 skips the pairs part 1 evaluated whole; the faces of the
+          // others fit, so neither part declines them
+          if (!fast) continue;
+          using NF = NatFields<ALL, PART>;
+          lean::F2 r[ALL ? kNumFields : 1];
+          pair_all_f2_raw<ALL, PART>(g, T, r);
+          const int e1 = g.top - 1023;
+          if (sh.rnat[p] && e1 >= -kNatMaxExp && e1 <= kNatMaxExp) {
+            using namespace lean;
+            const float s1 = pow2f(e1), s2 = pow2f(2 * e1);
+            const F2 rf{sh.rhoh[p], sh.rhol[p]};
+            const P2 rr = pk(rf, rf);
+            if constexpr (!ALL) {
+              nat[0] = f2_add(nat[0], f2_mul(rf, F2{fmul(r[0].h, s2), fmul(r[0].l, s2)}));
+            } else {
+              // (potential, g_e), (g_n, g_z), two tensor components, then one
+              const P2 a = p2_mul(rr, p2_scale(pk(r[kPotential], r[NF::field(1)]), mk2(s2, s1)));
+              const P2 na = p2_add(pk(nat[0], nat[1]), a);
+              nat[0] = lane0(na);
+              nat[1] = lane1(na);
+              const P2 b = p2_mul(rr, p2_scale(pk(r[NF::field(2)], r[NF::field(3)]), sp2(s1)));
+              const P2 nb = p2_add(pk(nat[2], nat[3]), b);
+              nat[2] = lane0(nb);
+              nat[3] = lane1(nb);
+              const P2 c = p2_mul(rr, pk(r[NF::field(4)], r[NF::field(5)]));
+              const P2 nc = p2_add(pk(nat[4], nat[5]), c);
+              nat[4] = lane0(nc);
+              nat[5] = lane1(nc);
+              nat[6] = f2_add(nat[6], f2_mul(rf, r[NF::field(6)]));
+            }
+          } else {
 #pragma unroll
-          for (int f = 0; f < (ALL ? kNumFields : 1); f++)
-            if (!ALL || !(f == kGen || f == kGez || f == kGnz)) acc[f] = fma(rho, v[f], acc[f]);
-          continue;
-        }
-        if (PART == 1 && fast) {
-          pair_all_f2_geom<ALL, 1>(g, T, v);
-#pragma unroll
-          for (int f = 0; f < (ALL ? kNumFields : 1); f++)
-            if (!ALL || !(f == kGee || f == kGnn || f == kGzz)) acc[f] = fma(rho, v[f], acc[f]);
+            for (int k = 0; k < NF::n; k++) {
+              const int f = NF::field(k);
+              acc[f] = fma(rho, f2_to_double(r[f], raw_exponent(f, e1)), acc[f]);
+            }
+          }
           continue;
         }
         if (!(fast && pair_all_f2_geom<ALL, PART>(g, T, v))) {
@@ -249,6 +309,11 @@ __device__ __forceinline__ void accumulate(const Source& src, int64_t p0, int64_
         if (is_tensor(F) && singular_for(F, q)) v = quiet_nan();
         acc[0] = fma(rho, v, acc[0]);
       }
+    }
+    if ((F == kAll || F == kPotential) && PART != 0) {
+#pragma unroll
+      for (int k = 0; k < NNAT; k++)
+        acc[NatFields<F == kAll, PART>::field(k)] += lean::f2_to_double(nat[k], 0);
     }
   }
 }

@@ -1407,7 +1407,7 @@ HG_HD __forceinline__ bool pair_all_f2(const Rel& q, const Tables& T, double* ou
 // The potential alone: the combinations on scalar float pairs (measured
 // faster for this kernel than the packed form of the fused one below).
 template <int PART>
-HG_HD __forceinline__ bool potential_f2_geom(const GeomF2& g, const Tables& T, double* out) {
+HG_HD __forceinline__ bool potential_f2_geom(const GeomF2& g, const Tables& T, lean::F2* out) {
   using namespace lean;
   F2 pot{0.0f, 0.0f}, faces2{0.0f, 0.0f};
 #pragma unroll 1
@@ -1433,12 +1433,16 @@ HG_HD __forceinline__ bool potential_f2_geom(const GeomF2& g, const Tables& T, d
                                    f2_mul(f2_mul(du, f2_add(u0, bound_f2(g, axis, 1))), o1)));
   }
   pot = f2_add(pot, F2{fmul(0.5f, faces2.h), fmul(0.5f, faces2.l)});
-  out[kPotential] = f2_to_double(pot, 2 * (g.top - 1023));
+  out[kPotential] = pot;
   return true;
 }
 
+// pair_all_f2_geom's sums as float pairs at the pair's scale: out[f] times
+// 2^(2 e1) for the potential, 2^e1 for g_e, g_n, g_z and 1 for the tensor
+// components is the field (e1 = g.top - 1023, raw_exponent); the fields a
+// part does not carry are zero.
 template <bool ALL, int PART>
-HG_HD __forceinline__ bool pair_all_f2_geom(const GeomF2& g, const Tables& T, double* out) {
+HG_HD __forceinline__ bool pair_all_f2_raw(const GeomF2& g, const Tables& T, lean::F2* out) {
   using namespace lean;
   if (!ALL) return potential_f2_geom<PART>(g, T, out);
   const F2 zero{0.0f, 0.0f};
@@ -1503,21 +1507,35 @@ HG_HD __forceinline__ bool pair_all_f2_geom(const GeomF2& g, const Tables& T, do
   const F2 faces2 = lane1(face2);
   const F2 pot = f2_add(f2_add(lane0(pot2), lane1(pot2)),
                         F2{fmul(0.5f, faces2.h), fmul(0.5f, faces2.l)});
-  const int e1 = g.top - 1023;
-  out[kPotential] = f2_to_double(pot, 2 * e1);
+  out[kPotential] = pot;
   if (ALL) {
-    out[kGe] = f2_to_double(ge, e1);
-    out[kGn] = f2_to_double(gn, e1);
-    out[kGz] = f2_to_double(gz, e1);
+    out[kGe] = ge;
+    out[kGn] = gn;
+    out[kGz] = gz;
     // the diagonal tensor components are face terms alone, the off-diagonal
     // ones edge terms alone
-    out[kGee] = PART == 1 ? 0.0 : f2_to_double(diff[0], 0);
-    out[kGnn] = PART == 1 ? 0.0 : f2_to_double(diff[1], 0);
-    out[kGzz] = PART == 1 ? 0.0 : f2_to_double(diff[2], 0);
-    out[kGen] = PART == 2 ? 0.0 : f2_to_double(Dz, 0);
-    out[kGez] = PART == 2 ? 0.0 : f2_to_double(Dy, 0);
-    out[kGnz] = PART == 2 ? 0.0 : f2_to_double(Dx, 0);
+    out[kGee] = PART == 1 ? zero : diff[0];
+    out[kGnn] = PART == 1 ? zero : diff[1];
+    out[kGzz] = PART == 1 ? zero : diff[2];
+    out[kGen] = PART == 2 ? zero : Dz;
+    out[kGez] = PART == 2 ? zero : Dy;
+    out[kGnz] = PART == 2 ? zero : Dx;
   }
+  return true;
+}
+
+// Power-of-two exponent of pair_all_f2_raw's output f (see there).
+HG_HD __forceinline__ int raw_exponent(int f, int e1) {
+  return f == kPotential ? 2 * e1 : ((f == kGe || f == kGn || f == kGz) ? e1 : 0);
+}
+
+template <bool ALL, int PART>
+HG_HD __forceinline__ bool pair_all_f2_geom(const GeomF2& g, const Tables& T, double* out) {
+  lean::F2 v[ALL ? kNumFields : 1];
+  if (!pair_all_f2_raw<ALL, PART>(g, T, v)) return false;
+  const int e1 = g.top - 1023;
+#pragma unroll
+  for (int f = 0; f < (ALL ? kNumFields : 1); f++) out[f] = f2_to_double(v[f], raw_exponent(f, e1));
   return true;
 }
 

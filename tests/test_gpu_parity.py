@@ -273,3 +273,40 @@ def test_float32_dtype_at_least_as_accurate_as_the_reference(gpu_lib, oracle):
     exact_sum = -1e5 * raw.sum(axis=1)
     assert np.all(np.abs(ours - exact_sum) <= np.abs(ref32 - exact_sum)
                   + np.spacing(np.abs(ours)))
+
+
+def test_pairs_near_a_plane_of_a_distant_prism(gpu_lib, oracle):
+    """Pairs with one bound far smaller than the largest (a station a few mm
+    to a few m from the plane of a face of a prism kilometres away): the
+    potential and the fused all-field forward run as an edge-log launch and
+    a face launch, which send these pairs whole to the FP64 path (when a
+    bound is below 2^-14 of the pair's scale) in the first and skip them in
+    the second.  Against the oracle at the parity bar, single-field and
+    fused, on both sides of the 2^-14 threshold."""
+    rng = np.random.default_rng(12)
+    prisms, coords = [], ([], [], [])
+    for k in range(40):
+        west = rng.uniform(2e3, 2e4) * rng.choice([-1, 1])
+        south = rng.uniform(-5e3, 5e3)
+        bottom = -rng.uniform(2e3, 8e3)
+        p = [west, west + rng.uniform(100, 800), south, south + rng.uniform(100, 800),
+             bottom, bottom + rng.uniform(100, 2000)]
+        prisms.append(p)
+    prisms = np.array(prisms)
+    density = rng.uniform(1000, 3000, prisms.shape[0])
+    # stations offset from the planes x = west, y = south, z = top of every
+    # prism by 1e-3 .. 10 m (log-uniform), elsewhere at random
+    for p in prisms:
+        for axis in range(3):
+            for off in np.exp(rng.uniform(np.log(1e-3), np.log(10.0), 3)):
+                pt = [rng.uniform(-3e4, 3e4), rng.uniform(-3e4, 3e4), rng.uniform(10, 500)]
+                plane = (p[0], p[2], p[5])[axis]
+                pt[axis] = plane + off * rng.choice([-1, 1])
+                for c in range(3):
+                    coords[c].append(pt[c])
+    coords = tuple(np.array(c) for c in coords)
+    fused = hg.prism_gravity_fields(coords, prisms, density, FIELDS)
+    for f in FIELDS:
+        ref = oracle.prism_gravity(coords, prisms, density, f)
+        assert_parity(hg.prism_gravity(coords, prisms, density, field=f), ref, msg=f)
+        assert_parity(fused[f], ref, msg=f"fused {f}")
