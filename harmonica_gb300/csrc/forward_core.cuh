@@ -54,7 +54,14 @@ template <> struct MinBlocks<kPotential> { static constexpr int value = HG_FWD_M
 template <int F, int PART> struct PartMinBlocks {
   static constexpr int value = PART == 0 ? MinBlocks<F>::value : HG_FWD_MIN_BLOCKS_PART;
 };
-template <int F> struct BatchMinBlocks { static constexpr int value = HG_BATCH_MIN_BLOCKS; };
+// the tensor components' batch and round kernels at 6, like their forward
+// kernels (the batched g_z/g_zz workload 1 % faster than at 5)
+#ifndef HG_BATCH_MIN_BLOCKS_TENSOR
+#define HG_BATCH_MIN_BLOCKS_TENSOR 6
+#endif
+template <int F> struct BatchMinBlocks {
+  static constexpr int value = F >= kGee ? HG_BATCH_MIN_BLOCKS_TENSOR : HG_BATCH_MIN_BLOCKS;
+};
 template <> struct BatchMinBlocks<kAll> { static constexpr int value = HG_FWD_MIN_BLOCKS_ALL; };
 template <> struct BatchMinBlocks<kPotential> {
   static constexpr int value = HG_FWD_MIN_BLOCKS_ALL;

@@ -715,7 +715,10 @@ HG_HD __forceinline__ bool make_geom_f2(const Rel& q, GeomF2& g) {
   const auto ex = [](double v) { return (int)((hi_word(v) >> 20) & 0x7ffu); };
   const int top =
       max(max(ex(q.x1), ex(q.x2)), max(max(ex(q.y1), ex(q.y2)), max(ex(q.z1), ex(q.z2))));
-  const auto tiny_nz = [&](double v) { return !is_tiny(v) && ex(v) < top - 40; };
+  // a nonzero bound below 2^-40 of the scale: 1 <= ef < top - 40, one
+  // unsigned compare (zero and subnormal bounds have ef = 0)
+  const unsigned lim = (unsigned)(top - 41);
+  const auto tiny_nz = [&](double v) { return (unsigned)(ex(v) - 1) < lim; };
   if (top >= 0x7fe || tiny_nz(q.x1) || tiny_nz(q.x2) || tiny_nz(q.y1) || tiny_nz(q.y2) ||
       tiny_nz(q.z1) || tiny_nz(q.z2) || ex(q.dx) < top - 20 || ex(q.dy) < top - 20 ||
       ex(q.dz) < top - 20)
@@ -749,6 +752,21 @@ HG_HD __forceinline__ bool make_geom_f2(const Rel& q, GeomF2& g) {
     }
   }
   return ok;
+}
+
+// A sufficient test that no face of the pair declines the float-pair scale
+// (face_pair_core_p2): every bound and extent within 2^14 of the largest
+// bound (the face inputs must be within 2^16 of the face's largest vertex
+// distance, itself below 4 x the largest bound).  The kernels that evaluate
+// the edge and face parts in two launches take the FP64 path for the pairs
+// that fail it, in the edge launch, and skip them in the face launch.
+HG_HD __forceinline__ bool faces_fit_f2(const GeomF2& g) {
+  using namespace lean;
+  const auto fe = [](F2 a) { return (int)((f2u(a.h) >> 23) & 0xffu); };
+  int m = min(fe(g.d[0]), min(fe(g.d[1]), fe(g.d[2])));
+#pragma unroll
+  for (int a = 0; a < 3; a++) m = min(m, min(fe(g.c[a][0]), fe(g.c[a][1])));
+  return m >= 127 - 14;
 }
 
 // Outside limit of a face angle for a point in the face plane (face_angle):
@@ -952,15 +970,16 @@ HG_HD __forceinline__ lean::P2 face_core_p2(lean::P2 fa, lean::P2 fb1, lean::P2 
 HG_HD __forceinline__ bool face_pair_core_p2(const lean::F2 fa[2], const lean::F2 fb[2],
                                              const lean::F2 fc[2], const lean::F2 fr[2][2][2],
                                              lean::F2 fw, bool same_sign, const Tables& T,
-                                             lean::P2& o);
+                                             lean::P2& o, bool fit);
 
 HG_HD __forceinline__ bool face_pair_p2(const lean::F2 fa[2], const lean::F2 fb[2],
                                         const lean::F2 fc[2], const lean::F2 fr[2][2][2],
                                         lean::F2 fw, const double ad[2], const double bd[2],
-                                        const double cd[2], const Tables& T, lean::P2& o) {
+                                        const double cd[2], const Tables& T, lean::P2& o,
+                                        bool fit = false) {
   using namespace lean;
   const bool same_sign = !(neg_not_tiny(bd[0]) && !nonpos_or_tiny(bd[1]));
-  if (!face_pair_core_p2(fa, fb, fc, fr, fw, same_sign, T, o)) return false;
+  if (!face_pair_core_p2(fa, fb, fc, fr, fw, same_sign, T, o, fit)) return false;
   // a point in a face plane: that face's outside limit
   if (is_tiny(ad[0]) || is_tiny(ad[1])) {
     F2 o0 = lane0(o), o1 = lane1(o);
@@ -973,10 +992,11 @@ HG_HD __forceinline__ bool face_pair_p2(const lean::F2 fa[2], const lean::F2 fb[
 
 // The two faces from float-pair inputs alone (same_sign: the b bounds have
 // one sign); false when a coordinate is too small for the face's scale.
+// fit: the caller has established faces_fit_f2 (the checks cannot fail).
 HG_HD __forceinline__ bool face_pair_core_p2(const lean::F2 fa[2], const lean::F2 fb[2],
                                              const lean::F2 fc[2], const lean::F2 fr[2][2][2],
                                              lean::F2 fw, bool same_sign, const Tables& T,
-                                             lean::P2& o) {
+                                             lean::P2& o, bool fit) {
   using namespace lean;
   const auto fe = [](F2 a) { return (int)((f2u(a.h) >> 23) & 0xffu); };
   int ftop[2];
@@ -985,8 +1005,9 @@ HG_HD __forceinline__ bool face_pair_core_p2(const lean::F2 fa[2], const lean::F
   for (int k = 0; k < 2; k++) {
     ftop[k] = max(max(fe(fr[k][0][0]), fe(fr[k][0][1])), max(fe(fr[k][1][0]), fe(fr[k][1][1])));
     const auto fsmall = [&](F2 a) { return a.h != 0.0f && fe(a) < ftop[k] - 16; };
-    small = small || fsmall(fa[k]) || fsmall(fb[0]) || fsmall(fb[1]) || fsmall(fc[0]) ||
-            fsmall(fc[1]) || fe(fw) < ftop[k] - 16;
+    if (!fit)
+      small = small || fsmall(fa[k]) || fsmall(fb[0]) || fsmall(fb[1]) || fsmall(fc[0]) ||
+              fsmall(fc[1]) || fe(fw) < ftop[k] - 16;
   }
   if (small) return false;
   const bool n0 = fa[0].h < 0.0f, n1 = fa[1].h < 0.0f;
@@ -1037,7 +1058,7 @@ HG_HD __forceinline__ bool faces_p2(const Rel& q, const GeomF2& g, const Tables&
   const double ad[2] = {rel_bound(q, U, 0), rel_bound(q, U, 1)};
   const double bd[2] = {rel_bound(q, B, 0), rel_bound(q, B, 1)};
   const double cd[2] = {rel_bound(q, C, 0), rel_bound(q, C, 1)};
-  return face_pair_p2(g.c[U], g.c[B], g.c[C], fr, g.d[B], ad, bd, cd, T, o);
+  return face_pair_p2(g.c[U], g.c[B], g.c[C], fr, g.d[B], ad, bd, cd, T, o, faces_fit_f2(g));
 }
 
 // All six faces O[axis][k] as three face pairs in a loop over the axis that
@@ -1342,7 +1363,9 @@ HG_HD __forceinline__ void family_logs(const GeomF2& g, int fam, const Tables& T
 }
 
 // The two faces normal to `axis` as float pairs (lanes: lower, upper bound),
-// for a pair with no zero bound (no face-plane limit to take).
+// for a pair with no zero bound (no face-plane limit to take); FIT as
+// face_pair_core_p2.
+template <bool FIT = false>
 HG_HD __forceinline__ bool face_pair_f2(const GeomF2& g, int axis, const Tables& T,
                                         lean::F2& o0, lean::F2& o1) {
   using namespace lean;
@@ -1360,7 +1383,7 @@ HG_HD __forceinline__ bool face_pair_f2(const GeomF2& g, int axis, const Tables&
   const F2 fc[2] = {(X || Y) ? g.c[2][0] : g.c[1][0], (X || Y) ? g.c[2][1] : g.c[1][1]};
   const F2 fw = X ? g.d[1] : g.d[0];
   P2 o;
-  if (!face_pair_core_p2(fa, fb, fc, fr, fw, !(fb[0].h < 0.0f && fb[1].h > 0.0f), T, o))
+  if (!face_pair_core_p2(fa, fb, fc, fr, fw, !(fb[0].h < 0.0f && fb[1].h > 0.0f), T, o, FIT))
     return false;
   o0 = lane0(o);
   o1 = lane1(o);
@@ -1383,20 +1406,6 @@ HG_HD __forceinline__ bool any_zero_bound(const Rel& q) {
 template <bool ALL, int PART = 0>
 HG_HD __forceinline__ bool pair_all_f2_geom(const GeomF2& g, const Tables& T, double* out);
 
-// A sufficient test that no face of the pair declines the float-pair scale
-// (face_pair_core_p2): every bound and extent within 2^14 of the largest
-// bound (the face inputs must be within 2^16 of the face's largest vertex
-// distance, itself below 4 x the largest bound).  The kernels that evaluate
-// the edge and face parts in two launches take the FP64 path for the pairs
-// that fail it, in the edge launch, and skip them in the face launch.
-HG_HD __forceinline__ bool faces_fit_f2(const GeomF2& g) {
-  using namespace lean;
-  const auto fe = [](F2 a) { return (int)((f2u(a.h) >> 23) & 0xffu); };
-  int m = min(fe(g.d[0]), min(fe(g.d[1]), fe(g.d[2])));
-#pragma unroll
-  for (int a = 0; a < 3; a++) m = min(m, min(fe(g.c[a][0]), fe(g.c[a][1])));
-  return m >= 127 - 14;
-}
 
 template <bool ALL>
 HG_HD __forceinline__ bool pair_all_f2(const Rel& q, const Tables& T, double* out) {
@@ -1426,7 +1435,7 @@ HG_HD __forceinline__ bool potential_f2_geom(const GeomF2& g, const Tables& T, l
 #pragma unroll 1
   for (int axis = 0; axis < (PART == 1 ? 0 : 3); axis++) {
     F2 o0, o1;
-    if (!face_pair_f2(g, axis, T, o0, o1)) return false;
+    if (!face_pair_f2<PART != 0>(g, axis, T, o0, o1)) return false;
     const F2 u0 = bound_f2(g, axis, 0), du = extent_f2(g, axis);
     // u0^2 (O0 - O1) - du (u0 + u1) O1
     faces2 = f2_add(faces2, f2_sub(f2_mul(f2_sq(u0), f2_sub(o0, o1)),
@@ -1482,7 +1491,7 @@ HG_HD __forceinline__ bool pair_all_f2_raw(const GeomF2& g, const Tables& T, lea
 #pragma unroll 1
   for (int axis = 0; axis < (PART == 1 ? 0 : 3); axis++) {
     F2 o0, o1;
-    if (!face_pair_f2(g, axis, T, o0, o1)) return false;
+    if (!face_pair_f2<PART != 0>(g, axis, T, o0, o1)) return false;
     const F2 u0 = bound_f2(g, axis, 0), du = extent_f2(g, axis);
     // (dO, su) = (O0 - O1, u0 + u1)
     const P2 ds = p2_add(pk(o0, u0), pk(f2_neg(o1), bound_f2(g, axis, 1)));
