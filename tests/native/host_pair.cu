@@ -31,7 +31,8 @@ extern "C" {
 
 // Sum over prisms (AoS, 6 per row) for each point, harmonica units, with the
 // kernel's null-prism skip and NaN at singular points.  mode: 0 = lean math,
-// 1 = generic library math, 2 = lean math through the fused all-field path.
+// 1 = generic library math, 2 = lean math through the fused all-field path,
+// 3 = the fused path as its edge-log part plus its face part.
 void host_prism_gravity(int field, int64_t n_obs, const double* e, const double* n,
                         const double* u, int64_t m, const double* prisms, const double* rho,
                         double* out, int mode) {
@@ -46,6 +47,21 @@ void host_prism_gravity(int field, int64_t n_obs, const double* e, const double*
       if (mode == 2) {
         double all[kNumFields];
         pair_all<true>(q, lean::host_tables(), all);
+        v = all[field];
+      } else if (mode == 3) {
+        // the two-launch form of the potential and fused all-field kernels:
+        // edge-log part + face part when the faces fit, else the whole pair
+        double all[kNumFields];
+        GeomF2 g;
+        const Tables T = lean::host_tables();
+        if (!any_zero_bound(q) && make_geom_f2(q, g) && faces_fit_f2(g)) {
+          double edges[kNumFields], faces[kNumFields];
+          pair_all_f2_geom<true, 1>(g, T, edges);
+          pair_all_f2_geom<true, 2>(g, T, faces);
+          for (int f = 0; f < kNumFields; f++) all[f] = edges[f] + faces[f];
+        } else {
+          pair_all<true>(q, T, all);
+        }
         v = all[field];
       } else {
         v = mode == 0 ? pair_any<true>(field, q) : pair_any<false>(field, q);

@@ -57,7 +57,7 @@ def parity(a, b, rtol=1e-8, atol_frac=1e-9):
     npt.assert_allclose(np.asarray(a)[fin], b[fin], rtol=rtol, atol=atol)
 
 
-MODES = {"lean": 0, "libm": 1, "fused": 2}
+MODES = {"lean": 0, "libm": 1, "fused": 2, "split": 3}
 
 
 @pytest.mark.parametrize("mode", MODES)
@@ -116,3 +116,25 @@ def test_distant_prism_accuracy_vs_mpmath(host, oracle):
     for ours, base, f, dist in worse:
         assert ours <= max(10 * base, 1e-9), (f, dist, ours, base)
     assert np.median([o for o, _, _, _ in worse]) < np.median([b for _, b, _, _ in worse])
+
+
+@pytest.mark.parametrize("field", FIELDS)
+def test_edge_and_face_parts_add_up_to_the_fused_pair(host, field):
+    """The potential and fused all-field kernels run as an edge-log launch and
+    a face launch whose sums add up to the fused pair (1e-12 relative to the
+    field's largest value), near and far, including pairs that take the FP64
+    path because a bound is tiny against the pair's scale."""
+    rng = np.random.default_rng(9)
+    m, n = 60, 80
+    w = rng.uniform(-5e4, 5e4, m)
+    s = rng.uniform(-5e4, 5e4, m)
+    b = rng.uniform(-8e3, 0, m)
+    prisms = np.column_stack([w, w + rng.uniform(50, 900, m), s, s + rng.uniform(50, 900, m), b,
+                              b + rng.uniform(50, 3000, m)])
+    rho = rng.uniform(1000, 3000, m)
+    e, nn, u = (rng.uniform(-5e4, 5e4, n), rng.uniform(-5e4, 5e4, n), rng.uniform(10, 500, n))
+    e[:10] = prisms[:10, 0] + 1e-3  # 1 mm from a face plane of a distant prism
+    coords = (e, nn, u)
+    fused = host(coords, prisms, rho, field, MODES["fused"])
+    split = host(coords, prisms, rho, field, MODES["split"])
+    npt.assert_allclose(split, fused, rtol=0, atol=1e-12 * np.abs(fused).max())
