@@ -956,10 +956,19 @@ HG_HD __forceinline__ lean::P2 face_core_p2(lean::P2 fa, lean::P2 fb1, lean::P2 
   pair_complex_p2(fa, asq, fb1, fb2, fc1, c1sq, fr11, fr21, same_sign, bdq1, br, bi);
   normalize_p2c(ar, ai);
   normalize_p2c(br, bi);
-  const float est0 = atan2_est(ai.h.x, ar.h.x) - atan2_est(bi.h.x, br.h.x);
-  const float est1 = atan2_est(ai.h.y, ar.h.y) - atan2_est(bi.h.y, br.h.y);
   const P2 pr = p2_add(p2_mul(ar, br), p2_mul(ai, bi));
   const P2 pim = p2_add(p2_mul(ai, br), p2_neg(p2_mul(ar, bi)));
+  float est0, est1;
+  if (same_sign) {
+    // b1 b2 >= 0: both pair products have positive real parts, so their
+    // arguments differ by less than pi and the argument of A conj(B) is the
+    // face angle itself (one estimate per lane instead of two)
+    est0 = atan2_est(pim.h.x, pr.h.x);
+    est1 = atan2_est(pim.h.y, pr.h.y);
+  } else {
+    est0 = atan2_est(ai.h.x, ar.h.x) - atan2_est(bi.h.x, br.h.x);
+    est1 = atan2_est(ai.h.y, ar.h.y) - atan2_est(bi.h.y, br.h.y);
+  }
   return arg_near_p2(pr, pim, est0, est1, T);
 }
 
