@@ -180,13 +180,18 @@ HG_HD __forceinline__ P2 log1p_p2(P2 t, const Tables& T) {
   plan(w.h.x, cp0, k0, e0);
   plan(w.h.y, cp1, k1, e1);
   const float2 cp = mk2(cp0, cp1);
-  const P2 red = p2_add(p2_mul(t, P2{cp, sp2(0.0f)}), two_sum2(cp, sp2(-1.0f)));
+  P2 tc = two_prod2(t.h, cp);  // t c (c a float)
+  tc.l = fma2(t.l, cp, tc.l);
+  const P2 red = p2_add(tc, two_sum2(cp, sp2(-1.0f)));
   const P2 lp = log1p_series_p2(red);
+  const P2 lc{mk2(T.loglf[2 * k0], T.loglf[2 * k1]), mk2(T.loglf[2 * k0 + 1], T.loglf[2 * k1 + 1])};
+  // 1 + t in [0.75, 1.5) in both lanes (E = 0: the far single edge logs):
+  // E ln 2 is zero and (0 + lc) + lp is lc + lp, the same bits
+  if (e0 == 0.0f && e1 == 0.0f) return p2_add(lc, lp);
   const float2 ef = mk2(e0, e1);
   P2 e2 = two_prod2(ef, sp2(kLn2F2));
   e2.l = fma2(ef, sp2(kLn2F3), e2.l);
   const P2 eln2 = p2_add(P2{mul2(ef, sp2(kLn2F1)), sp2(0.0f)}, e2);
-  const P2 lc{mk2(T.loglf[2 * k0], T.loglf[2 * k1]), mk2(T.loglf[2 * k0 + 1], T.loglf[2 * k1 + 1])};
   return p2_add(p2_add(eln2, lc), lp);
 }
 
