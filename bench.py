@@ -92,15 +92,15 @@ KERNEL_SOURCES = ("prism_math.cuh", "lean_math.cuh", "lean_packed.cuh", "lean_ta
 # the kernel's few register spills written back from L2).
 # Summarised under profiles/; valid for the kernel sources that hash to `sources_sha`.
 KERNEL_COUNTS = {
-    "sources_sha": "485e0a1c69da6463",
-    "warp_inst_per_pair": 52.66,
-    "fp32_lane_ops_per_pair": 1853.2,
+    "sources_sha": "260a36036d52a8e4",
+    "warp_inst_per_pair": 52.64,
+    "fp32_lane_ops_per_pair": 1852.2,
     "fp64_inst_per_pair": 9.40,
-    "dram_bytes_default_step": 34071680,  # 25.32 MB read + 8.75 MB written (two launches)
+    "dram_bytes_default_step": 34620160,  # 25.26 MB read + 9.36 MB written (two launches)
     "default_step_stations": 5000,
-    # the same kernel's utilisations (fractions of peak over the active cycles)
-    "ncu_utilisation": {"issue_active": 0.636, "fma_pipe": 0.697, "fmaheavy_pipe": 0.731,
-                        "fmalite_pipe": 0.663, "alu_pipe": 0.346, "fp64_pipe": 0.229},
+    # the same capture's utilisations (fractions of peak over the active cycles)
+    "ncu_utilisation": {"issue_active": 0.634, "fma_pipe": 0.695, "fmaheavy_pipe": 0.730,
+                        "fmalite_pipe": 0.661, "alu_pipe": 0.345, "fp64_pipe": 0.229},
     "capture": "ncu on GB300: per-pair counts from two launches of a 1000-station step, "
                "DRAM bytes from two launches of the default step (1-pass metrics)",
 }
