@@ -1038,7 +1038,8 @@ def main():
                "path": "prism_layer(...).prism_layer.gravity(coords, 'g_z'), numpy inputs"}
 
     def sampled_rate(field_mask, label):
-        """One launch of `field_mask` on sampled stations of the layer."""
+        """One forward call of `field_mask` on sampled stations of the layer (two
+        launches for the potential or the ten fields: edge-log terms, then face terms)."""
         nb = min(args.all_fields_stations, n_total)
         lo = rank * nb % n_total
         sl = slice(lo, lo + nb)
@@ -1052,11 +1053,12 @@ def main():
         torch.cuda.synchronize()
         sec = a0.elapsed_time(a1) * 1e-3
         return {"value": nb * n_prisms / sec, "unit": f"pairs/s ({label})",
-                "sample": f"{nb} stations x all 1e6 prisms, one launch", "ms": sec * 1e3}
+                "sample": f"{nb} stations x all 1e6 prisms, one call (edge-log and face "
+                          "launches)", "ms": sec * 1e3}
 
     all_fields = potential = None
     if not args.no_all_fields:
-        all_fields = sampled_rate(0x3FF, "all 10 fields per pair, one fused launch")
+        all_fields = sampled_rate(0x3FF, "all 10 fields per pair")
         all_fields["field_values_per_s"] = 10 * all_fields["value"]
         potential = sampled_rate(1 << 0, "potential")
 
