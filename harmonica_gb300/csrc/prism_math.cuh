@@ -1422,12 +1422,17 @@ HG_HD __forceinline__ bool pair_all_f2(const Rel& q, const Tables& T, double* ou
   return !any_zero_bound(q) && make_geom_f2(q, g) && pair_all_f2_geom<ALL>(g, T, out);
 }
 
-// The potential alone: the combinations on scalar float pairs (measured
-// faster for this kernel than the packed form of the fused one below).
+// The potential alone.  Each family's E is taken as
+//   E = dQ (dP L00 + p1 MP0) + q1 (dP MQ0 + p1 D)
+// with the two brackets in the lanes of one packed pair (3 packed products,
+// one packed sum, in place of eight scalar products and three sums); the
+// lanes of the family sums and of the face sums are added once at the end.
+// Each bracket times its factor is a sum of two of E's four terms, so its
+// rounding is a rounding of those terms, as in the four-term sum.
 template <int PART>
 HG_HD __forceinline__ bool potential_f2_geom(const GeomF2& g, const Tables& T, lean::F2* out) {
   using namespace lean;
-  F2 pot{0.0f, 0.0f}, faces2{0.0f, 0.0f};
+  P2 pot2{sp2(0.0f), sp2(0.0f)}, face2{sp2(0.0f), sp2(0.0f)};
 #pragma unroll 1
   for (int fam = 0; fam < (PART == 2 ? 0 : 3); fam++) {
     F2 mq0, mq1, mp0, l00;
@@ -1436,21 +1441,30 @@ HG_HD __forceinline__ bool potential_f2_geom(const GeomF2& g, const Tables& T, l
     const F2 p1 = bound_f2(g, P, 1), q1 = bound_f2(g, Q, 1);
     const F2 dP = extent_f2(g, P), dQ = extent_f2(g, Q);
     const F2 D = f2_sub(mq1, mq0);
-    // E = dP dQ L00 + p1 dQ MP0 + q1 dP MQ0 + p1 q1 D
-    const F2 E = f2_add(f2_add(f2_mul(f2_mul(dP, dQ), l00), f2_mul(f2_mul(p1, dQ), mp0)),
-                        f2_add(f2_mul(f2_mul(q1, dP), mq0), f2_mul(f2_mul(p1, q1), D)));
-    pot = f2_add(pot, E);
+    const P2 B = p2_add(p2_mul(pk(dP, dP), pk(l00, mq0)), p2_mul(pk(p1, p1), pk(mp0, D)));
+    pot2 = p2_add(pot2, p2_mul(pk(dQ, q1), B));
   }
 #pragma unroll 1
   for (int axis = 0; axis < (PART == 1 ? 0 : 3); axis++) {
     F2 o0, o1;
     if (!face_pair_f2<PART != 0>(g, axis, T, o0, o1)) return false;
     const F2 u0 = bound_f2(g, axis, 0), du = extent_f2(g, axis);
-    // u0^2 (O0 - O1) - du (u0 + u1) O1
-    faces2 = f2_add(faces2, f2_sub(f2_mul(f2_sq(u0), f2_sub(o0, o1)),
-                                   f2_mul(f2_mul(du, f2_add(u0, bound_f2(g, axis, 1))), o1)));
+    // u0^2 (O0 - O1) - du (u0 + u1) O1 as the lanes (u0 u0 dO, -su du O1)
+    const P2 ds = p2_add(pk(o0, u0), pk(f2_neg(o1), bound_f2(g, axis, 1)));  // (dO, su)
+    const P2 T1 = p2_mul(pk(u0, du), pk(lane0(ds), o1));
+    face2 = p2_add(face2, p2_mul(pk(u0, f2_neg(lane1(ds))), T1));
   }
-  pot = f2_add(pot, F2{fmul(0.5f, faces2.h), fmul(0.5f, faces2.l)});
+  F2 pot;
+  if constexpr (PART == 2) {
+    pot = f2_add(lane0(face2), lane1(face2));
+    pot = F2{fmul(0.5f, pot.h), fmul(0.5f, pot.l)};
+  } else {
+    pot = f2_add(lane0(pot2), lane1(pot2));
+    if constexpr (PART == 0) {
+      const F2 faces2 = f2_add(lane0(face2), lane1(face2));
+      pot = f2_add(pot, F2{fmul(0.5f, faces2.h), fmul(0.5f, faces2.l)});
+    }
+  }
   out[kPotential] = pot;
   return true;
 }
