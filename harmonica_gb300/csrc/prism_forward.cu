@@ -55,7 +55,13 @@ __global__ void __launch_bounds__(kThreads, PartMinBlocks<F, PART>::value) forwa
   const double pn = active ? on[i] : 0.0;
   const double pu = active ? ou[i] : 0.0;
 
-  double acc[NF];
+  // the fused kernel's ten sums in shared memory: they change once per
+  // prism tile (the pairs go to float-pair sums), and in registers they
+  // would hold 20 of the 128 through the whole pair evaluation
+  constexpr bool kSmemAcc = F == kAll;
+  double racc[kSmemAcc ? 1 : NF];
+  __shared__ double sacc[kSmemAcc ? kThreads * NF : 1];
+  double* acc = kSmemAcc ? &sacc[threadIdx.x * NF] : racc;
 #pragma unroll
   for (int f = 0; f < NF; f++) acc[f] = 0.0;
   bool singular_seen = false;
