@@ -92,11 +92,11 @@ KERNEL_SOURCES = ("prism_math.cuh", "lean_math.cuh", "lean_packed.cuh", "lean_ta
 # the kernel's few register spills written back from L2).
 # Summarised under profiles/; valid for the kernel sources that hash to `sources_sha`.
 KERNEL_COUNTS = {
-    "sources_sha": "9595fa4fd1b5ca38",
+    "sources_sha": "493ff81654005ea1",
     "warp_inst_per_pair": 52.64,
     "fp32_lane_ops_per_pair": 1852.2,
     "fp64_inst_per_pair": 9.40,
-    "dram_bytes_default_step": 34472832,  # 25.13 MB read + 9.34 MB written (two launches)
+    "dram_bytes_default_step": 33995008,  # 25.31 MB read + 8.69 MB written (two launches)
     "default_step_stations": 5000,
     # the same capture's utilisations (fractions of peak over the active cycles)
     "ncu_utilisation": {"issue_active": 0.634, "fma_pipe": 0.695, "fmaheavy_pipe": 0.730,
