@@ -300,12 +300,13 @@ def prism_gravity_fields(
     device=None,
 ):
     """
-    Several fields of the same prisms and points in one fused launch.
+    Several fields of the same prisms and points in one fused forward.
 
     Returns a dict ``{field: array}``; every array equals what
     :func:`prism_gravity` returns for that field.  The edge logarithms and
     face angles of each (point, prism) pair are computed once and shared by
-    all requested fields.
+    all requested fields: the logarithms in one launch, the angles in a
+    second that adds its terms to the first's sums.
     """
     for f in fields:
         if f not in FIELD_CODES:

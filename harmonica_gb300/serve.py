@@ -55,10 +55,14 @@ from .gravity import _prepare, pack_prisms
 KTHREADS = 128  # points per work item (the kernels' tile)
 
 
-# Cost of a pair of each field relative to g_z, from the layer kernels on
-# GB300 (g_z 1.21e10, potential 3.41e9, g_zz 2.39e10 pairs/s; the other
-# first derivatives cost as g_z, the other tensor components as g_zz): the
-# prior of the per-field rates until each field's launches have been timed.
+# Weight of a pair of each field relative to g_z: the virtual deadlines of
+# the scheduling order and the prior of the per-field rates until each
+# field's launches have been timed (the other first derivatives as g_z, the
+# other tensor components as g_zz).  The values are the layer kernels'
+# relative costs on GB300 when the served stream was tuned (g_z 1.21e10,
+# potential 3.41e9, g_zz 2.39e10 pairs/s).  The current kernels' ratios
+# (potential 2.76, g_zz 0.59) gave served / plain 1.026 on that stream, these
+# 1.03-1.04 over three runs, so these stay.
 FIELD_COST = {"potential": 3.55, "g_e": 1.0, "g_n": 1.0, "g_z": 1.0, "g_ee": 0.5, "g_nn": 0.5,
               "g_zz": 0.5, "g_en": 0.5, "g_ez": 0.5, "g_nz": 0.5}
 
