@@ -94,6 +94,32 @@ def test_special_points_against_oracle(host, oracle, field, mode):
     parity(host(coords, prism, [1000.0], field, MODES[mode]), ref)
 
 
+@pytest.mark.parametrize("mode", ["lean", "fused", "split"])
+@pytest.mark.parametrize("field", FIELDS)
+def test_extreme_aspect_ratios_against_oracle(host, oracle, field, mode):
+    """Needles, plates and slabs (extents from 0.5 m to 2 km in one prism):
+    the regrouped combinations weight logs by bounds and extents of very
+    different sizes (dP much smaller than p1, or the reverse), at points in
+    and around the prisms and a few prism lengths away."""
+    rng = np.random.default_rng(21)
+    shapes = [(0.5, 500.0, 50.0), (500.0, 0.5, 50.0), (500.0, 50.0, 0.5), (2000.0, 2000.0, 1.0),
+              (1.0, 1.0, 2000.0), (0.5, 2000.0, 0.5)]
+    prisms = []
+    for dx, dy, dz in shapes:
+        for _ in range(4):
+            w, s = rng.uniform(-300, 300, 2)
+            b = rng.uniform(-600, -10)
+            prisms.append([w, w + dx, s, s + dy, b, b + dz])
+    prisms = np.array(prisms)
+    rho = rng.uniform(-3000, 3000, len(prisms))
+    n = 120
+    coords = (rng.uniform(-3e3, 3e3, n), rng.uniform(-3e3, 3e3, n), rng.uniform(-700, 300, n))
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        ref = oracle.prism_gravity(coords, prisms, rho, field)
+    parity(host(coords, prisms, rho, field, MODES[mode]), ref)
+
+
 def test_distant_prism_accuracy_vs_mpmath(host, oracle):
     """At large distance the regrouped form is at least as accurate as the
     8-vertex sum (both measured against 50-digit arithmetic)."""
