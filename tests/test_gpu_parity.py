@@ -84,6 +84,31 @@ def test_random_prisms_against_oracle(gpu_lib, oracle, field):
     assert_parity(res, ref, msg=field)
 
 
+def test_extreme_aspect_ratios_against_oracle(gpu_lib, oracle):
+    """Needles, plates and slabs (extents from 0.5 m to 2 km in one prism),
+    every field alone and the ten fused, against the oracle."""
+    rng = np.random.default_rng(21)
+    shapes = [(0.5, 500.0, 50.0), (500.0, 0.5, 50.0), (500.0, 50.0, 0.5), (2000.0, 2000.0, 1.0),
+              (1.0, 1.0, 2000.0), (0.5, 2000.0, 0.5)]
+    prisms = []
+    for dx, dy, dz in shapes:
+        for _ in range(40):
+            w, s = rng.uniform(-300, 300, 2)
+            b = rng.uniform(-600, -10)
+            prisms.append([w, w + dx, s, s + dy, b, b + dz])
+    prisms = np.array(prisms)
+    rho = rng.uniform(-3000, 3000, len(prisms))
+    n = 300
+    coords = (rng.uniform(-3e3, 3e3, n), rng.uniform(-3e3, 3e3, n), rng.uniform(-700, 300, n))
+    fused = hg.prism_gravity_fields(coords, prisms, rho, FIELDS)
+    for field in FIELDS:
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            ref = oracle.prism_gravity(coords, prisms, rho, field)
+        assert_parity(hg.prism_gravity(coords, prisms, rho, field=field), ref, msg=field)
+        assert_parity(fused[field], ref, msg="fused " + field)
+
+
 def test_fused_all_fields_match_single(gpu_lib):
     coords, prisms, density = random_problem(2, 257, 190)
     fused = hg.prism_gravity_fields(coords, prisms, density, FIELDS)
