@@ -55,6 +55,18 @@ def test_layer_gravity_matches_prism_gravity(gpu_lib, dummy_layer, field):
     npt.assert_allclose(expected, layer.prism_layer.gravity(coords, field=field), rtol=1e-10)
 
 
+def test_layer_progress_bar(gpu_lib, dummy_layer):
+    """test/test_prism_layer.py:401-419: the accessor's results with and
+    without the progress bar match."""
+    e, n = np.meshgrid(np.arange(1, 4, 1.0), np.arange(7, 11, 1.0))
+    coords = (e, n, np.full_like(e, 30.0))
+    (easting, northing), surface, reference, density = dummy_layer
+    layer = hg.prism_layer((easting, northing), surface, reference,
+                           properties={"density": density})
+    npt.assert_allclose(layer.prism_layer.gravity(coords, field="g_z", progressbar=True),
+                        layer.prism_layer.gravity(coords, field="g_z", progressbar=False))
+
+
 def _holes(dummy_layer):
     (easting, northing), surface, reference, density = dummy_layer
     layer = hg.prism_layer((easting, northing), surface, reference,

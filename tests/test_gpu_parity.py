@@ -109,6 +109,19 @@ def test_extreme_aspect_ratios_against_oracle(gpu_lib, oracle):
         assert_parity(fused[field], ref, msg="fused " + field)
 
 
+@pytest.mark.parametrize("field", FIELDS)
+def test_progress_bar(gpu_lib, capsys, field):
+    """test/test_prism.py:367-377: results with and without the progress bar
+    match; here the bar is a line on stderr, printed per chunk of points."""
+    coords, prisms, density = random_problem(4, 60, 250)
+    with_bar = hg.prism_gravity(coords, prisms, density, field=field, progressbar=True)
+    err = capsys.readouterr().err
+    assert "250/250 points" in err and "(100.0%)" in err
+    without = hg.prism_gravity(coords, prisms, density, field=field, progressbar=False)
+    assert capsys.readouterr().err == ""
+    npt.assert_allclose(with_bar, without, rtol=1e-12, atol=1e-13 * np.max(np.abs(without)))
+
+
 def test_fused_all_fields_match_single(gpu_lib):
     coords, prisms, density = random_problem(2, 257, 190)
     fused = hg.prism_gravity_fields(coords, prisms, density, FIELDS)
