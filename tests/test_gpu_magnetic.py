@@ -62,3 +62,22 @@ def test_null_prisms_and_far_field(gpu_lib):
     R = np.linalg.norm(r)
     dip = 1e-7 * (3 * r * np.dot(m, r) / R ** 5 - m / R ** 3) * 1e9
     npt.assert_allclose([c[0] for c in single], dip, rtol=1e-4)
+
+
+def test_parallel_and_progressbar_flags(gpu_lib):
+    """test/test_prism_magnetic.py: results with parallel=False and with the
+    progress bar equal the defaults (both flags are accepted; the GPU path
+    has one evaluation order)."""
+    rng = np.random.default_rng(8)
+    m = 50
+    w = rng.uniform(-500, 500, m)
+    s = rng.uniform(-500, 500, m)
+    t = rng.uniform(-300, -20, m)
+    prisms = np.column_stack([w, w + rng.uniform(20, 200, m), s, s + rng.uniform(20, 200, m),
+                              t - rng.uniform(20, 200, m), t])
+    mag = tuple(rng.uniform(-2, 2, m) for _ in range(3))
+    coords = (rng.uniform(-800, 800, 90), rng.uniform(-800, 800, 90), rng.uniform(0, 100, 90))
+    for f in ("b_e", "b_n", "b_u"):
+        base = hg.prism_magnetic(coords, prisms, mag, f)
+        npt.assert_array_equal(hg.prism_magnetic(coords, prisms, mag, f, parallel=False), base)
+        npt.assert_array_equal(hg.prism_magnetic(coords, prisms, mag, f, progressbar=True), base)

@@ -93,3 +93,23 @@ def test_many_chunks_and_empty(gpu_lib, oracle):
                         oracle.point_gravity(coords, pts, masses, "g_z"), rtol=1e-10)
     assert hg.point_gravity((np.zeros(0),) * 3, pts, masses, "g_z").shape == (0,)
     npt.assert_array_equal(hg.point_gravity(coords, ([], [], []), [], "g_z"), np.zeros(5))
+
+
+@pytest.mark.parametrize("system", ("cartesian", "spherical"))
+def test_parallel_flag(gpu_lib, system):
+    """test/test_point_gravity.py (cartesian and spherical parallel tests):
+    parallel=False gives the default's results."""
+    if system == "cartesian":
+        coords, pts, masses = _random(6, 200, 150)
+    else:
+        rng = np.random.default_rng(6)
+        pts = (rng.uniform(-10, 10, 200), rng.uniform(-10, 10, 200),
+               6.371e6 - rng.uniform(1e3, 5e4, 200))
+        masses = rng.uniform(-1e9, 1e9, 200)
+        coords = (rng.uniform(-12, 12, 150), rng.uniform(-12, 12, 150),
+                  6.371e6 + rng.uniform(0, 1e3, 150))
+    for f in ("potential", "g_z"):
+        base = hg.point_gravity(coords, pts, masses, f, coordinate_system=system)
+        npt.assert_array_equal(
+            hg.point_gravity(coords, pts, masses, f, coordinate_system=system, parallel=False),
+            base)

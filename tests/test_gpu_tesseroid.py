@@ -341,3 +341,14 @@ def test_gpu_shapes_and_dtype():
     npt.assert_allclose(out, ref.astype(np.float32), rtol=1e-6)
     single = hg.tesseroid_gravity([0.0, 0.0, MEAN_RADIUS + 1e3], tess, 2670.0, "potential")
     assert np.ndim(single) == 0 or single.shape == ()
+
+
+@pytest.mark.parametrize("field", ["potential", "g_z"])
+def test_gpu_parallel_and_progressbar_flags(field):
+    """test/test_tesseroid.py (parallel and progress-bar tests): results with
+    parallel=False and with the progress bar equal the defaults."""
+    coords, tess, dens = random_model(12, 40, 60, 100.0, 50e3)
+    base = hg.tesseroid_gravity(coords, tess, dens, field)
+    npt.assert_array_equal(hg.tesseroid_gravity(coords, tess, dens, field, parallel=False), base)
+    npt.assert_array_equal(hg.tesseroid_gravity(coords, tess, dens, field, progressbar=True),
+                           base)
