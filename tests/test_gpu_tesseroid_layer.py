@@ -96,3 +96,12 @@ def test_layer_gravity_discards_thin_tesseroids():
     tess, rho = holes(layer, density, [(3, 3), (2, 1)])
     npt.assert_allclose(layer.tesseroid_layer.gravity(grid, field="g_z", thickness_threshold=1),
                         hg.tesseroid_gravity(grid, tess, rho, field="g_z"))
+
+
+def test_layer_progress_bar():
+    """test/test_tesseroid_layer.py (progress-bar test): the accessor's
+    results with and without the progress bar match."""
+    coords, surface, reference, density, grid = dummy()
+    layer = tesseroid_layer(coords, surface, reference, properties={"density": density})
+    npt.assert_allclose(layer.tesseroid_layer.gravity(grid, field="g_z", progressbar=True),
+                        layer.tesseroid_layer.gravity(grid, field="g_z", progressbar=False))
