@@ -108,3 +108,78 @@ def test_kernel_formulation_against_exact_values(oracle, host, truth, field, mod
               field, mode), truth[f"faces_{field}"], field)
     _bar(host(truth["layer_points"], truth["layer_prisms"], truth["layer_density"], field, mode),
          truth[f"layer_{field}"], field)
+
+
+TENSOR = ("g_ee", "g_nn", "g_zz", "g_en", "g_ez", "g_nz")
+
+
+@pytest.fixture(scope="module")
+def shapes():
+    return np.load(os.path.join(HERE, "golden", "mp_truth_shapes.npz"))
+
+
+def _shape_values(shapes, evaluate, field):
+    P, D, X, W = (shapes[k] for k in ("shape_prisms", "shape_density", "shape_points",
+                                      "shape_which"))
+    return np.array([evaluate(X[i:i + 1], P[W[i]], [D[W[i]]], field)[0]
+                     for i in range(X.shape[0])])
+
+
+@pytest.mark.parametrize("mode", [0, 2, 3], ids=["single-field", "fused", "split"])
+@pytest.mark.parametrize("field", FIELDS)
+def test_thin_prisms_against_exact_values(oracle, host, shapes, field, mode):
+    """Needles, plates and slabs (tests/golden/mp_truth_shapes.npz: one
+    extent 0.5-1 m, the others up to 2 km).  Within 100 m of the prism
+    centre and 2 m off a large face: the parity bar against the exact
+    values, per prism, with the absolute part of a tensor component taken
+    from the tensor's largest component (2 m off the middle of a face the
+    off-diagonal components are a ~1e-4 residual of the tensor).  At 1 and
+    10 km: below 1e-4 relative and no worse than the reference's own FP64
+    algorithm (the oracle), except g_ee (below)."""
+    def ours(pts, p, d, f):
+        return host(pts, p, d, f, mode)
+
+    got = _shape_values(shapes, ours, field)
+    exact = shapes[f"shape_{field}"]
+    klass, which = shapes["shape_class"], shapes["shape_which"]
+    fields = TENSOR if field in TENSOR else (field,)
+    for k in range(len(shapes["shape_prisms"])):
+        near = (which == k) & (klass <= 0.1)
+        scale = max(np.max(np.abs(shapes[f"shape_{f}"][near])) for f in fields)
+        npt.assert_array_less(np.abs(got[near] - exact[near]),
+                              RTOL * np.abs(exact[near]) + ATOL_FRAC * scale)
+    if field == "g_ee":
+        return  # test_thin_needle_g_ee_far_from_the_prism
+    ref = _shape_values(shapes, lambda pts, p, d, f: oracle.prism_gravity(
+        tuple(pts[:, c] for c in range(3)), p, d, f), field)
+    for km in (1.0, 10.0):
+        sel = klass == km
+        mine = np.max(np.abs(got[sel] / exact[sel] - 1))
+        theirs = np.max(np.abs(ref[sel] / exact[sel] - 1))
+        assert mine <= max(theirs, RTOL) and mine <= 1e-4, (km, mine, theirs)
+
+
+@pytest.mark.xfail(strict=True, reason="known limit: the face angle of a face thin in its "
+                   "second in-plane direction keeps that direction's cancellation, and g_ee "
+                   "of a 0.5 m x 2 km x 0.5 m needle subtracts two such faces 0.5 m apart: "
+                   "4e-8 at 1 km, 1.7e-5 at 10 km, against the FP64 sum's 4e-10, 9e-7")
+def test_thin_needle_g_ee_far_from_the_prism(oracle, host, shapes):
+    got = _shape_values(shapes, lambda pts, p, d, f: host(pts, p, d, f, 0), "g_ee")
+    ref = _shape_values(shapes, lambda pts, p, d, f: oracle.prism_gravity(
+        tuple(pts[:, c] for c in range(3)), p, d, f), "g_ee")
+    exact = shapes["shape_g_ee"]
+    for km in (1.0, 10.0):
+        sel = shapes["shape_class"] == km
+        mine = np.max(np.abs(got[sel] / exact[sel] - 1))
+        theirs = np.max(np.abs(ref[sel] / exact[sel] - 1))
+        assert mine <= max(theirs, RTOL), (km, mine, theirs)
+
+
+def test_thin_needle_g_ee_bounded(host, shapes):
+    """The limit above stays bounded: g_ee of every thin prism within 1e-4 of
+    the exact value at 10 km and 1e-7 at 1 km."""
+    got = _shape_values(shapes, lambda pts, p, d, f: host(pts, p, d, f, 0), "g_ee")
+    exact = shapes["shape_g_ee"]
+    for km, bound in ((1.0, 1e-7), (10.0, 1e-4)):
+        sel = shapes["shape_class"] == km
+        assert np.max(np.abs(got[sel] / exact[sel] - 1)) <= bound
